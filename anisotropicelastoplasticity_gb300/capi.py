@@ -1,0 +1,151 @@
+"""ctypes mirror of include/aep.h (the C-ABI of libaep.so).
+
+Structures here must match the C declarations field for field; the
+`tests/test_capi_load.py` checks sizes against the header.  Loading never
+falls back to anything: if libaep.so is missing or cannot be loaded, an
+ImportError/OSError is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from . import _build
+
+AEP_OK = 0
+AEP_INVALID_ARG = 1
+AEP_CUDA_ERROR = 2
+AEP_OVERFLOW = 3
+AEP_OUT_OF_DOMAIN = 4
+AEP_NOT_READY = 5
+AEP_OUT_OF_MEMORY = 6
+AEP_NO_DEVICE = 7
+STATUS_NAMES = {
+    0: "AEP_OK", 1: "AEP_INVALID_ARG", 2: "AEP_CUDA_ERROR", 3: "AEP_OVERFLOW", 4: "AEP_OUT_OF_DOMAIN",
+    5: "AEP_NOT_READY", 6: "AEP_OUT_OF_MEMORY", 7: "AEP_NO_DEVICE",
+}
+
+AEP_SNOW = 0
+AEP_SAND = 1
+
+AEP_SDF_PLANE = 0
+AEP_SDF_SPHERE = 1
+AEP_SDF_WALL2GROUND = 2
+
+AEP_STAGE_P2G = 1
+AEP_STAGE_FORCES = 2
+AEP_STAGE_GRID = 3
+AEP_STAGE_FULL = 4
+
+
+class aep_sdf(C.Structure):
+    _fields_ = [("type", C.c_int32), ("reserved", C.c_int32), ("p", C.c_double * 6)]
+
+
+class aep_grid_desc(C.Structure):
+    _fields_ = [("min", C.c_double * 3), ("max", C.c_double * 3), ("res", C.c_int32 * 3), ("reserved", C.c_int32)]
+
+
+class aep_snow_params(C.Structure):
+    _fields_ = [("E", C.c_double), ("nu", C.c_double), ("theta_c", C.c_double), ("theta_s", C.c_double),
+                ("xi", C.c_double)]
+
+
+class aep_sand_params(C.Structure):
+    _fields_ = [("E", C.c_double), ("nu", C.c_double), ("h0", C.c_double), ("h1", C.c_double),
+                ("h2", C.c_double), ("h3", C.c_double)]
+
+
+class aep_params(C.Structure):
+    _fields_ = [
+        ("snow", aep_snow_params),
+        ("sand", aep_sand_params),
+        ("gravity", C.c_double * 3),
+        ("friction", C.c_double),
+        ("friction_bug", C.c_int32),
+        ("track_plastic_F", C.c_int32),
+        ("particle_damp", C.c_double),
+        ("mass_bits", C.c_int32),
+        ("momentum_bits", C.c_int32),
+        ("reserved", C.c_int64 * 8),
+    ]
+
+
+class aep_stats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int64),
+        ("num_particles", C.c_int64),
+        ("active_blocks", C.c_int64),
+        ("out_of_domain", C.c_int64),
+        ("fp64_fallbacks", C.c_int64),
+        ("overflow", C.c_int64),
+        ("active_nodes", C.c_int64),
+        ("total_mass", C.c_double),
+        ("total_momentum", C.c_double * 3),
+        ("reserved", C.c_double * 7),
+    ]
+
+
+_dp = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+_solver_p = C.c_void_p
+
+# name -> (restype, argtypes); every symbol declared in include/aep.h
+SIGNATURES = {
+    "aep_abi_version": (C.c_int32, []),
+    "aep_default_params": (None, [C.POINTER(aep_params)]),
+    "aep_solver_create": (C.c_int, [C.POINTER(aep_grid_desc), C.POINTER(aep_params), C.POINTER(_solver_p)]),
+    "aep_solver_destroy": (C.c_int, [_solver_p]),
+    "aep_set_particles": (C.c_int, [_solver_p, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _u8p]),
+    "aep_set_levelset": (C.c_int, [_solver_p, C.POINTER(aep_sdf), C.c_int32]),
+    "aep_init_volumes": (C.c_int, [_solver_p]),
+    "aep_step": (C.c_int, [_solver_p, C.c_double]),
+    "aep_synchronize": (C.c_int, [_solver_p]),
+    "aep_get_particles": (C.c_int, [_solver_p, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "aep_get_grid": (C.c_int, [_solver_p, _dp, _dp, _dp, _dp]),
+    "aep_get_stats": (C.c_int, [_solver_p, C.POINTER(aep_stats)]),
+    "aep_step_stage": (C.c_int, [_solver_p, C.c_double, C.c_int32]),
+    "aep_set_stream": (C.c_int, [_solver_p, C.c_void_p]),
+    "aep_set_profiling": (C.c_int, [_solver_p, C.c_int32]),
+    "aep_get_phase_times": (C.c_int, [_solver_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "aep_last_error": (C.c_char_p, [_solver_p]),
+}
+
+PHASES = ["sort", "p2g", "normalize", "force", "grid", "g2p"]
+
+_lib = None
+
+
+def lib_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load libaep.so (building it first when missing).  Raises if it cannot load."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not path.exists():
+        if not build_if_missing:
+            raise ImportError(f"libaep.so not built: {path}")
+        _build.build()
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class AepError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+
+
+def default_params() -> aep_params:
+    p = aep_params()
+    load().aep_default_params(C.byref(p))
+    return p

@@ -1,0 +1,626 @@
+// aep_capi.cu -- the C-ABI of include/aep.h: solver handle, device memory,
+// layout conversion at the boundary, and the per-step launch sequence.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/aep.h"
+#include "aep_kernels.h"
+
+using namespace aep;
+
+namespace {
+
+constexpr int kFloatArrays = 3 + 3 + 9 + 9 + 3;  // x, v, B, F, m, vol, plastic
+constexpr int kFpArrays = 9;
+
+struct ParticleSet {
+    float* f = nullptr;
+    uint8_t* mat = nullptr;
+    int32_t* id = nullptr;
+};
+
+}  // namespace
+
+struct aep_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    aep_grid_desc grid{};
+    aep_params prm{};
+    KParams kp{};
+    int64_t n = 0, cap = 0;
+    ParticleSet set[2];
+    PArrays P[2];
+    int cur = 0;
+    uint32_t* keys = nullptr;
+    uint32_t* keys_sorted = nullptr;
+    int32_t* iota = nullptr;
+    int32_t* perm = nullptr;
+    void* sort_tmp = nullptr;
+    size_t sort_bytes = 0;
+    int key_bits = 0;
+    GArrays G{};
+    size_t nnodes = 0;
+    int nblocks = 0;
+    DevStats* dstats = nullptr;
+    double* staging = nullptr;
+    size_t staging_bytes = 0;
+    double* dforce = nullptr;  // dense f_i after a force-stage stop
+    bool have_particles = false, keys_valid = false, dirty_grid = false;
+    int last_stage = 0;
+    double m_max = 1.0;
+    int64_t steps = 0;
+    int grid_blocks = 1024;
+    cudaStream_t own_stream = nullptr;
+    // phase timing: a ring of per-step event sets, folded into `phase_ms` lazily
+    bool profiling = false;
+    static constexpr int kRing = 32;
+    cudaEvent_t ev[kRing][AEP_NUM_PHASES + 1] = {};
+    bool ev_pending[kRing] = {};
+    int ev_slot = 0;
+    double phase_ms[AEP_NUM_PHASES] = {};
+    int64_t timed_steps = 0;
+    std::string err;
+};
+
+namespace {
+
+aep_status fail(aep_solver* s, aep_status st, const std::string& msg) {
+    if (s) s->err = msg;
+    return st;
+}
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(s, e_ == cudaErrorMemoryAllocation ? AEP_OUT_OF_MEMORY : AEP_CUDA_ERROR,        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+    } while (0)
+
+#define CKLAUNCH() CK(cudaGetLastError())
+
+void lame(double E, double nu, double& lambda, double& mu) {
+    lambda = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+    mu = E / 2.0 / (1.0 + nu);
+}
+
+void fill_kparams(aep_solver* s) {
+    KParams& k = s->kp;
+    const aep_grid_desc& g = s->grid;
+    const aep_params& p = s->prm;
+    double h[3], hmin = 1e300;
+    for (int a = 0; a < 3; ++a) {
+        h[a] = (g.max[a] - g.min[a]) / g.res[a];
+        hmin = std::min(hmin, h[a]);
+        k.min[a] = (float)g.min[a];
+        k.h[a] = (float)h[a];
+        k.inv_h[a] = (float)(1.0 / h[a]);
+        k.res[a] = g.res[a];
+        // base node (padded) <= res + 2; its block and the next one must exist
+        k.nb[a] = ((g.res[a] + 2) >> 2) + 2;
+    }
+    for (int a = 0; a < 3; ++a) k.apic[a] = (float)(3.0 / hmin / hmin * h[a]);
+    k.cell_volume = (float)(h[0] * h[1] * h[2]);
+    double ml = std::ldexp(1.0, p.mass_bits) / s->m_max, pl = std::ldexp(1.0, p.momentum_bits) / s->m_max;
+    k.mass_scale = (float)ml;
+    k.inv_mass_scale = (float)(1.0 / ml);
+    k.mom_scale = (float)pl;
+    k.inv_mom_scale = (float)(1.0 / pl);
+    double l, m;
+    lame(p.snow.E, p.snow.nu, l, m);
+    k.snow_mu = (float)m;
+    k.snow_lambda = (float)l;
+    k.snow_xi = (float)p.snow.xi;
+    k.snow_lo = (float)(1.0 - p.snow.theta_c);
+    k.snow_hi = (float)(1.0 + p.snow.theta_s);
+    lame(p.sand.E, p.sand.nu, l, m);
+    k.sand_mu = (float)m;
+    k.sand_lambda = (float)l;
+    k.sand_h0 = (float)p.sand.h0;
+    k.sand_h1 = (float)p.sand.h1;
+    k.sand_h2 = (float)p.sand.h2;
+    k.sand_h3 = (float)p.sand.h3;
+    k.sand_k = (float)((3.0 * l + 2.0 * m) / 2.0 / m);
+    for (int a = 0; a < 3; ++a) k.gravity[a] = (float)p.gravity[a];
+    k.friction = (float)p.friction;
+    k.friction_bug = p.friction_bug;
+    k.particle_damp = (float)p.particle_damp;
+    k.track_fp = p.track_plastic_F;
+}
+
+void build_parrays(aep_solver* s, int which) {
+    PArrays& P = s->P[which];
+    float* f = s->set[which].f;
+    size_t c = (size_t)s->cap;
+    int k = 0;
+    for (int a = 0; a < 3; ++a) P.x[a] = f + c * k++;
+    for (int a = 0; a < 3; ++a) P.v[a] = f + c * k++;
+    for (int a = 0; a < 9; ++a) P.B[a] = f + c * k++;
+    for (int a = 0; a < 9; ++a) P.F[a] = f + c * k++;
+    P.m = f + c * k++;
+    P.vol = f + c * k++;
+    P.plastic = f + c * k++;
+    for (int a = 0; a < 9; ++a) P.Fp[a] = s->prm.track_plastic_F ? f + c * k++ : nullptr;
+    P.mat = s->set[which].mat;
+    P.id = s->set[which].id;
+}
+
+void free_particles(aep_solver* s) {
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(s->set[i].f);
+        cudaFree(s->set[i].mat);
+        cudaFree(s->set[i].id);
+        s->set[i] = ParticleSet{};
+    }
+    cudaFree(s->keys);
+    cudaFree(s->keys_sorted);
+    cudaFree(s->iota);
+    cudaFree(s->perm);
+    cudaFree(s->sort_tmp);
+    cudaFree(s->staging);
+    s->keys = s->keys_sorted = nullptr;
+    s->iota = s->perm = nullptr;
+    s->sort_tmp = nullptr;
+    s->staging = nullptr;
+    s->cap = 0;
+}
+
+aep_status ensure_capacity(aep_solver* s, int64_t n) {
+    if (n <= s->cap) return AEP_OK;
+    free_particles(s);
+    size_t nf = kFloatArrays + (s->prm.track_plastic_F ? kFpArrays : 0);
+    s->cap = n;
+    for (int i = 0; i < 2; ++i) {
+        CK(cudaMalloc(&s->set[i].f, sizeof(float) * nf * (size_t)n));
+        CK(cudaMalloc(&s->set[i].mat, (size_t)n));
+        CK(cudaMalloc(&s->set[i].id, sizeof(int32_t) * (size_t)n));
+    }
+    CK(cudaMalloc(&s->keys, sizeof(uint32_t) * (size_t)n));
+    CK(cudaMalloc(&s->keys_sorted, sizeof(uint32_t) * (size_t)n));
+    CK(cudaMalloc(&s->iota, sizeof(int32_t) * (size_t)n));
+    CK(cudaMalloc(&s->perm, sizeof(int32_t) * (size_t)n));
+    s->sort_bytes = sort_temp_bytes((int)n, s->key_bits);
+    CK(cudaMalloc(&s->sort_tmp, s->sort_bytes));
+    s->staging_bytes = sizeof(double) * 9 * (size_t)n;
+    CK(cudaMalloc(&s->staging, s->staging_bytes));
+    std::vector<int32_t> io((size_t)n);
+    for (int64_t i = 0; i < n; ++i) io[(size_t)i] = (int32_t)i;
+    CK(cudaMemcpy(s->iota, io.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice));
+    build_parrays(s, 0);
+    build_parrays(s, 1);
+    return AEP_OK;
+}
+
+aep_status upload(aep_solver* s, const double* src, int count, int mode, float* const* dst) {
+    CK(cudaMemcpyAsync(s->staging, src, sizeof(double) * count * (size_t)s->n, cudaMemcpyHostToDevice, s->stream));
+    launch_upload((int)s->n, mode, s->staging, dst, s->stream);
+    CKLAUNCH();
+    return AEP_OK;
+}
+
+aep_status download(aep_solver* s, double* dst, int count, int mode, float* const* src) {
+    const PArrays& P = s->P[s->cur];
+    launch_download((int)s->n, mode, P.id, s->staging, src, s->stream);
+    CKLAUNCH();
+    CK(cudaMemcpyAsync(dst, s->staging, sizeof(double) * count * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return AEP_OK;
+}
+
+aep_status check_overflow(aep_solver* s) {
+    DevStats h;
+    CK(cudaMemcpy(&h, s->dstats, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h.overflow) return fail(s, AEP_OVERFLOW, "fixed-point grid accumulator overflow");
+    return AEP_OK;
+}
+
+aep_status fold_slot(aep_solver* s, int slot) {
+    if (!s->ev_pending[slot]) return AEP_OK;
+    CK(cudaEventSynchronize(s->ev[slot][AEP_NUM_PHASES]));
+    for (int p = 0; p < AEP_NUM_PHASES; ++p) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, s->ev[slot][p], s->ev[slot][p + 1]));
+        s->phase_ms[p] += ms;
+    }
+    s->ev_pending[slot] = false;
+    s->timed_steps++;
+    return AEP_OK;
+}
+
+inline void mark(aep_solver* s, int boundary) {
+    if (s->profiling) cudaEventRecord(s->ev[s->ev_slot][boundary], s->stream);
+}
+
+// P2G of the current particle order (sort + scatter + normalisation)
+aep_status run_p2g(aep_solver* s) {
+    if (s->dirty_grid) {
+        launch_grid_clear(s->G, s->grid_blocks, s->stream);
+        CKLAUNCH();
+        s->dirty_grid = false;
+    }
+    const PArrays& P = s->P[s->cur];
+    CK(cudaMemsetAsync(s->dstats, 0, sizeof(DevStats), s->stream));
+    mark(s, AEP_PHASE_SORT);
+    if (!s->keys_valid) {
+        launch_keys(s->kp, P, (int)s->n, s->keys, s->dstats, s->stream);
+        CKLAUNCH();
+        s->keys_valid = true;
+    }
+    CK(sort_pairs(s->sort_tmp, s->sort_bytes, s->keys, s->keys_sorted, s->iota, s->perm, (int)s->n, s->key_bits,
+                  s->stream));
+    CK(cudaMemsetAsync(s->G.nactive, 0, sizeof(int32_t), s->stream));
+    mark(s, AEP_PHASE_P2G);
+    launch_p2g(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, s->stream);
+    CKLAUNCH();
+    mark(s, AEP_PHASE_NORMALIZE);
+    launch_normalize(s->kp, s->G, s->dstats, s->grid_blocks, s->stream);
+    CKLAUNCH();
+    mark(s, AEP_PHASE_FORCE);
+    return AEP_OK;
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+int32_t aep_abi_version(void) { return AEP_ABI_VERSION; }
+
+void aep_default_params(aep_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->snow.E = 1.4e5;  // ParticleSystem.cpp:173-176
+    p->snow.nu = 0.2;
+    p->snow.theta_c = 2.5e-2;
+    p->snow.theta_s = 7.5e-3;
+    p->snow.xi = 10.0;  // HybridSolver.cpp:267
+    p->sand.E = 3.537e5;  // ParticleSystem.cpp:233-234
+    p->sand.nu = 0.3;
+    p->sand.h0 = 35.0;  // HybridSolver.cpp:641-644
+    p->sand.h1 = 9.0;
+    p->sand.h2 = 0.2;
+    p->sand.h3 = 10.0;
+    p->gravity[0] = 0.0;
+    p->gravity[1] = 0.0;
+    p->gravity[2] = -9.8;  // HybridSolver.cpp:457
+    p->friction = 0.2;     // HybridSolver.cpp:465
+    p->friction_bug = 1;   // HybridSolver.cpp:500-501
+    p->track_plastic_F = 0;
+    p->particle_damp = 0.0;  // HybridSolver.cpp:916
+    p->mass_bits = 34;
+    p->momentum_bits = 40;
+}
+
+aep_status aep_solver_create(const aep_grid_desc* grid, const aep_params* params, aep_solver** out) {
+    aep_solver* s = nullptr;
+    if (!grid || !out) return AEP_INVALID_ARG;
+    *out = nullptr;
+    for (int a = 0; a < 3; ++a) {
+        if (grid->res[a] < 1 || grid->res[a] > 1400 || !(grid->max[a] > grid->min[a])) return AEP_INVALID_ARG;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return AEP_NO_DEVICE;
+    s = new aep_solver();
+    s->grid = *grid;
+    if (params) s->prm = *params;
+    else aep_default_params(&s->prm);
+    if (s->prm.mass_bits <= 0 || s->prm.mass_bits > 50 || s->prm.momentum_bits <= 0 || s->prm.momentum_bits > 50) {
+        delete s;
+        return AEP_INVALID_ARG;
+    }
+    CK(cudaGetDevice(&s->device));
+    CK(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
+    s->stream = s->own_stream;
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+    s->grid_blocks = std::max(1, sms) * 8;
+    fill_kparams(s);
+    s->nblocks = s->kp.nb[0] * s->kp.nb[1] * s->kp.nb[2];
+    s->nnodes = (size_t)s->nblocks * 64;
+    uint64_t maxkey = (uint64_t)s->nblocks * 64;
+    s->key_bits = 1;
+    while ((1ull << s->key_bits) < maxkey) ++s->key_bits;
+    CK(cudaMalloc(&s->G.acc, sizeof(unsigned long long) * 4 * s->nnodes));
+    CK(cudaMalloc(&s->G.vel, sizeof(float4) * s->nnodes));
+    CK(cudaMalloc(&s->G.vbf, sizeof(float4) * s->nnodes));
+    CK(cudaMalloc(&s->G.flag, sizeof(uint32_t) * (size_t)s->nblocks));
+    CK(cudaMalloc(&s->G.active, sizeof(int32_t) * (size_t)s->nblocks));
+    CK(cudaMalloc(&s->G.nactive, sizeof(int32_t)));
+    CK(cudaMalloc(&s->dstats, sizeof(DevStats)));
+    CK(cudaMemsetAsync(s->G.acc, 0, sizeof(unsigned long long) * 4 * s->nnodes, s->stream));
+    CK(cudaMemsetAsync(s->G.vel, 0, sizeof(float4) * s->nnodes, s->stream));
+    CK(cudaMemsetAsync(s->G.vbf, 0, sizeof(float4) * s->nnodes, s->stream));
+    CK(cudaMemsetAsync(s->G.flag, 0, sizeof(uint32_t) * (size_t)s->nblocks, s->stream));
+    CK(cudaMemsetAsync(s->G.nactive, 0, sizeof(int32_t), s->stream));
+    CK(cudaMemsetAsync(s->dstats, 0, sizeof(DevStats), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *out = s;
+    return AEP_OK;
+}
+
+aep_status aep_solver_destroy(aep_solver* s) {
+    if (!s) return AEP_INVALID_ARG;
+    cudaStreamSynchronize(s->stream);
+    free_particles(s);
+    cudaFree(s->G.acc);
+    cudaFree(s->G.vel);
+    cudaFree(s->G.vbf);
+    cudaFree(s->G.flag);
+    cudaFree(s->G.active);
+    cudaFree(s->G.nactive);
+    cudaFree(s->dstats);
+    cudaFree(s->dforce);
+    for (int r = 0; r < aep_solver::kRing; ++r)
+        for (int p = 0; p <= AEP_NUM_PHASES; ++p)
+            if (s->ev[r][p]) cudaEventDestroy(s->ev[r][p]);
+    cudaStreamDestroy(s->own_stream);
+    delete s;
+    return AEP_OK;
+}
+
+aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const double* v, const double* B,
+                             const double* Fe, const double* Fp, const double* m, const double* vol,
+                             const double* plastic, const uint8_t* material) {
+    if (!s) return AEP_INVALID_ARG;
+    if (n <= 0 || n > (int64_t)INT32_MAX / 2 || !x || !Fe || !m)
+        return fail(s, AEP_INVALID_ARG, "aep_set_particles: need n > 0 and non-null x, Fe, m");
+    double mm = 0.0;
+    for (int64_t p = 0; p < n; ++p) {
+        if (!(m[p] >= 0.0) || !std::isfinite(m[p])) return fail(s, AEP_INVALID_ARG, "aep_set_particles: bad mass");
+        mm = std::max(mm, m[p]);
+    }
+    if (material)
+        for (int64_t p = 0; p < n; ++p)
+            if (material[p] > AEP_SAND) return fail(s, AEP_INVALID_ARG, "aep_set_particles: unknown material tag");
+    if (!(mm > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_particles: all masses are zero");
+    CK(cudaStreamSynchronize(s->stream));
+    aep_status st = ensure_capacity(s, n);
+    if (st != AEP_OK) return st;
+    s->n = n;
+    s->cur = 0;
+    s->m_max = mm;
+    fill_kparams(s);
+    PArrays& P = s->P[0];
+    st = upload(s, x, 3, 0, P.x);
+    if (st) return st;
+    if (v) { st = upload(s, v, 3, 0, P.v); if (st) return st; }
+    else for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(P.v[a], 0, sizeof(float) * n, s->stream));
+    if (B) { st = upload(s, B, 9, 1, P.B); if (st) return st; }
+    else for (int a = 0; a < 9; ++a) CK(cudaMemsetAsync(P.B[a], 0, sizeof(float) * n, s->stream));
+    st = upload(s, Fe, 9, 2, P.F);
+    if (st) return st;
+    st = upload(s, m, 1, 3, &P.m);
+    if (st) return st;
+    if (vol) { st = upload(s, vol, 1, 3, &P.vol); if (st) return st; }
+    else CK(cudaMemsetAsync(P.vol, 0, sizeof(float) * n, s->stream));
+    if (plastic) { st = upload(s, plastic, 1, 3, &P.plastic); if (st) return st; }
+    else CK(cudaMemsetAsync(P.plastic, 0, sizeof(float) * n, s->stream));
+    // material tags and ids
+    uint8_t* dmat = nullptr;
+    if (material) {
+        dmat = reinterpret_cast<uint8_t*>(s->staging);
+        CK(cudaMemcpyAsync(dmat, material, (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    }
+    launch_init_particles((int)n, P, dmat, Fp != nullptr, s->prm.track_plastic_F, s->stream);
+    CKLAUNCH();
+    if (s->prm.track_plastic_F && Fp) {
+        st = upload(s, Fp, 9, 2, P.Fp);
+        if (st) return st;
+    }
+    // snow particles: J_P = det F_P into `plastic`
+    double* dFp = nullptr;
+    if (Fp) {
+        dFp = s->staging;
+        CK(cudaMemcpyAsync(dFp, Fp, sizeof(double) * 9 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    }
+    if (!s->prm.track_plastic_F) {
+        launch_snow_jp((int)n, P, dFp, s->stream);
+        CKLAUNCH();
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->have_particles = true;
+    s->keys_valid = false;
+    s->last_stage = 0;
+    return AEP_OK;
+}
+
+aep_status aep_set_levelset(aep_solver* s, const aep_sdf* shapes, int32_t n) {
+    if (!s) return AEP_INVALID_ARG;
+    if (n < 0 || n > kMaxShapes || (n > 0 && !shapes))
+        return fail(s, AEP_INVALID_ARG, "aep_set_levelset: 0..8 shapes");
+    for (int i = 0; i < n; ++i) {
+        if (shapes[i].type < AEP_SDF_PLANE || shapes[i].type > AEP_SDF_WALL2GROUND)
+            return fail(s, AEP_INVALID_ARG, "aep_set_levelset: unknown shape type");
+        s->kp.shapes[i].type = shapes[i].type;
+        for (int k = 0; k < 6; ++k) s->kp.shapes[i].p[k] = (float)shapes[i].p[k];
+    }
+    s->kp.nshapes = n;
+    return AEP_OK;
+}
+
+aep_status aep_init_volumes(aep_solver* s) {
+    if (!s) return AEP_INVALID_ARG;
+    if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_init_volumes: no particles");
+    aep_status st = run_p2g(s);
+    if (st) return st;
+    launch_volumes(s->kp, s->P[s->cur], s->perm, (int)s->n, s->G, s->stream);
+    CKLAUNCH();
+    s->dirty_grid = true;
+    s->last_stage = AEP_STAGE_P2G;
+    CK(cudaStreamSynchronize(s->stream));
+    return check_overflow(s);
+}
+
+aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
+    if (!s) return AEP_INVALID_ARG;
+    if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_step: no particles");
+    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(s, AEP_INVALID_ARG, "aep_step: dt must be > 0");
+    if (stage < AEP_STAGE_P2G || stage > AEP_STAGE_FULL) return fail(s, AEP_INVALID_ARG, "aep_step: bad stage");
+    const bool timed = s->profiling && stage == AEP_STAGE_FULL;
+    const bool prof_saved = s->profiling;
+    if (s->profiling && !timed) s->profiling = false;  // only whole steps are timed
+    if (timed) {
+        aep_status fs = fold_slot(s, s->ev_slot);
+        if (fs) return fs;
+    }
+    aep_status st = run_p2g(s);
+    s->profiling = prof_saved;
+    if (st) return st;
+    s->last_stage = stage;
+    if (stage == AEP_STAGE_P2G) {
+        s->dirty_grid = true;
+        return AEP_OK;
+    }
+    const float dtf = (float)dt;
+    const PArrays& P = s->P[s->cur];
+    launch_force(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, dtf, s->dstats, s->stream);
+    CKLAUNCH();
+    if (timed) mark(s, AEP_PHASE_GRID);
+    if (stage == AEP_STAGE_FORCES) {
+        size_t ng = (size_t)s->grid.res[0] * s->grid.res[1] * s->grid.res[2];
+        if (!s->dforce) CK(cudaMalloc(&s->dforce, sizeof(double) * 3 * ng));
+        CK(cudaMemsetAsync(s->dforce, 0, sizeof(double) * 3 * ng, s->stream));
+        launch_grid(s->kp, s->G, dtf, 1, s->dforce, s->grid_blocks, s->stream);
+        CKLAUNCH();
+        s->dirty_grid = true;
+        return AEP_OK;
+    }
+    launch_grid(s->kp, s->G, dtf, 0, nullptr, s->grid_blocks, s->stream);
+    CKLAUNCH();
+    if (stage == AEP_STAGE_GRID) return AEP_OK;
+    if (timed) mark(s, AEP_PHASE_G2P);
+    const int nx = 1 - s->cur;
+    launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, dtf, s->keys, s->dstats, s->stream);
+    CKLAUNCH();
+    if (timed) {
+        mark(s, AEP_NUM_PHASES);
+        s->ev_pending[s->ev_slot] = true;
+        s->ev_slot = (s->ev_slot + 1) % aep_solver::kRing;
+    }
+    s->cur = nx;
+    s->keys_valid = true;
+    s->steps++;
+    return AEP_OK;
+}
+
+aep_status aep_step(aep_solver* s, double dt) { return aep_step_stage(s, dt, AEP_STAGE_FULL); }
+
+aep_status aep_synchronize(aep_solver* s) {
+    if (!s) return AEP_INVALID_ARG;
+    CK(cudaStreamSynchronize(s->stream));
+    return check_overflow(s);
+}
+
+aep_status aep_get_particles(aep_solver* s, int64_t n, double* x, double* v, double* B, double* Fe, double* Fp,
+                             double* vol, double* plastic) {
+    if (!s) return AEP_INVALID_ARG;
+    if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_get_particles: no particles");
+    if (n != s->n) return fail(s, AEP_INVALID_ARG, "aep_get_particles: n mismatch");
+    if (Fp && !s->prm.track_plastic_F) return fail(s, AEP_INVALID_ARG, "aep_get_particles: Fp needs track_plastic_F");
+    CK(cudaStreamSynchronize(s->stream));
+    PArrays& P = s->P[s->cur];
+    aep_status st;
+    if (x && (st = download(s, x, 3, 0, P.x))) return st;
+    if (v && (st = download(s, v, 3, 0, P.v))) return st;
+    if (B && (st = download(s, B, 9, 1, P.B))) return st;
+    if (Fe && (st = download(s, Fe, 9, 2, P.F))) return st;
+    if (Fp && (st = download(s, Fp, 9, 2, P.Fp))) return st;
+    if (vol && (st = download(s, vol, 1, 3, &P.vol))) return st;
+    if (plastic && (st = download(s, plastic, 1, 3, &P.plastic))) return st;
+    return AEP_OK;
+}
+
+aep_status aep_get_grid(aep_solver* s, double* mass, double* vel, double* vbf, double* force) {
+    if (!s) return AEP_INVALID_ARG;
+    CK(cudaStreamSynchronize(s->stream));
+    size_t ng = (size_t)s->grid.res[0] * s->grid.res[1] * s->grid.res[2];
+    double* d = nullptr;
+    CK(cudaMalloc(&d, sizeof(double) * 7 * ng));
+    CK(cudaMemsetAsync(d, 0, sizeof(double) * 7 * ng, s->stream));
+    if (s->last_stage > 0) {
+        bool has_vbf = s->last_stage >= AEP_STAGE_GRID;
+        launch_grid_dense(s->kp, s->G, d, d + ng, has_vbf ? d + 4 * ng : nullptr, s->grid_blocks, s->stream);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { cudaFree(d); return fail(s, AEP_CUDA_ERROR, cudaGetErrorString(e)); }
+    }
+    cudaError_t e = cudaSuccess;
+    if (mass && e == cudaSuccess) e = cudaMemcpyAsync(mass, d, sizeof(double) * ng, cudaMemcpyDeviceToHost, s->stream);
+    if (vel && e == cudaSuccess) e = cudaMemcpyAsync(vel, d + ng, sizeof(double) * 3 * ng, cudaMemcpyDeviceToHost, s->stream);
+    if (vbf && e == cudaSuccess) e = cudaMemcpyAsync(vbf, d + 4 * ng, sizeof(double) * 3 * ng, cudaMemcpyDeviceToHost, s->stream);
+    if (force && e == cudaSuccess) {
+        if (s->last_stage == AEP_STAGE_FORCES && s->dforce)
+            e = cudaMemcpyAsync(force, s->dforce, sizeof(double) * 3 * ng, cudaMemcpyDeviceToHost, s->stream);
+        else
+            std::memset(force, 0, sizeof(double) * 3 * ng);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(s, AEP_CUDA_ERROR, cudaGetErrorString(e));
+    return AEP_OK;
+}
+
+aep_status aep_get_stats(aep_solver* s, aep_stats* out) {
+    if (!s || !out) return AEP_INVALID_ARG;
+    CK(cudaStreamSynchronize(s->stream));
+    DevStats h;
+    CK(cudaMemcpy(&h, s->dstats, sizeof(h), cudaMemcpyDeviceToHost));
+    int32_t nact = 0;
+    CK(cudaMemcpy(&nact, s->G.nactive, sizeof(nact), cudaMemcpyDeviceToHost));
+    std::memset(out, 0, sizeof(*out));
+    out->steps = s->steps;
+    out->num_particles = s->n;
+    out->active_blocks = nact;
+    out->out_of_domain = (int64_t)h.out_of_domain;
+    out->fp64_fallbacks = (int64_t)h.fallbacks;
+    out->overflow = (int64_t)h.overflow;
+    out->active_nodes = (int64_t)h.nodes;
+    double im = std::ldexp(s->m_max, -s->prm.mass_bits), ip = std::ldexp(s->m_max, -s->prm.momentum_bits);
+    out->total_mass = (double)(long long)h.mass * im;
+    for (int a = 0; a < 3; ++a) out->total_momentum[a] = (double)(long long)h.mom[a] * ip;
+    return AEP_OK;
+}
+
+aep_status aep_set_stream(aep_solver* s, void* cuda_stream) {
+    if (!s) return AEP_INVALID_ARG;
+    CK(cudaStreamSynchronize(s->stream));
+    s->stream = cuda_stream ? (cudaStream_t)cuda_stream : s->own_stream;
+    return AEP_OK;
+}
+
+aep_status aep_set_profiling(aep_solver* s, int32_t on) {
+    if (!s) return AEP_INVALID_ARG;
+    CK(cudaStreamSynchronize(s->stream));
+    if (on && !s->ev[0][0]) {
+        for (int r = 0; r < aep_solver::kRing; ++r)
+            for (int p = 0; p <= AEP_NUM_PHASES; ++p) CK(cudaEventCreate(&s->ev[r][p]));
+    }
+    for (int r = 0; r < aep_solver::kRing; ++r) s->ev_pending[r] = false;
+    for (int p = 0; p < AEP_NUM_PHASES; ++p) s->phase_ms[p] = 0.0;
+    s->timed_steps = 0;
+    s->ev_slot = 0;
+    s->profiling = on != 0;
+    return AEP_OK;
+}
+
+aep_status aep_get_phase_times(aep_solver* s, double* ms, int64_t* steps) {
+    if (!s || !ms) return AEP_INVALID_ARG;
+    CK(cudaStreamSynchronize(s->stream));
+    for (int r = 0; r < aep_solver::kRing; ++r) {
+        aep_status st = fold_slot(s, r);
+        if (st) return st;
+    }
+    for (int p = 0; p < AEP_NUM_PHASES; ++p) ms[p] = s->phase_ms[p];
+    if (steps) *steps = s->timed_steps;
+    return AEP_OK;
+}
+
+const char* aep_last_error(aep_solver* s) {
+    if (!s) return "null solver";
+    return s->err.c_str();
+}
+
+}  // extern "C"

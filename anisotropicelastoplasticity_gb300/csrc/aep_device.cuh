@@ -1,0 +1,387 @@
+// aep_device.cuh -- device-side building blocks of the sm_103a MPM step.
+//
+// Layout conventions used by every kernel:
+//   * particles: structure of arrays in FP32, one array per component; 3x3
+//     matrices are nine arrays, component (a,b) in array [3a+b] (row-major).
+//   * grid: padded, blocked.  The reference node (i,j,k) (RegularGrid.cpp:
+//     164-168) becomes padded node (i+4, j+4, k+4); padded nodes are grouped
+//     in 4x4x4 blocks stored contiguously (64 nodes), blocks in x-fastest
+//     order.  The padding lets every particle's 4x4x4 cubic stencil be
+//     addressed without bounds checks; nodes outside the reference grid get
+//     weight 0 exactly as HybridSolver.cpp:44-46 drops them.
+//   * a particle's cell is floor((x - min)/h), its stencil base node is
+//     cell - 1 and its stencil is base + {0..3}^3 (the nodes with nonzero
+//     cubic weight among the 5^3 candidates of HybridSolver.cpp:38-47).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace aep {
+
+constexpr int kMaxShapes = 8;
+constexpr uint32_t kInvalidKey = 0xFFFFFFFFu;
+
+enum : int { kSnow = 0, kSand = 1 };
+enum : int { kSdfPlane = 0, kSdfSphere = 1, kSdfWall2Ground = 2 };
+
+struct DevShape {
+    int type;
+    float p[6];
+};
+
+// Per-launch constants (kernel parameter space).
+struct KParams {
+    float min[3], h[3], inv_h[3];
+    int res[3];
+    int nb[3];            // padded node blocks per axis
+    float apic[3];        // (3 / hmin^2) * h_a: APIC D^-1 scaled to stencil offsets (HS:175-177)
+    float mass_scale, inv_mass_scale;
+    float mom_scale, inv_mom_scale;
+    float snow_mu, snow_lambda, snow_xi, snow_lo, snow_hi;
+    float sand_mu, sand_lambda, sand_h0, sand_h1, sand_h2, sand_h3, sand_k;  // k = (3l+2m)/(2m)
+    float gravity[3];
+    float friction;
+    int friction_bug;
+    float particle_damp;
+    int track_fp;
+    int nshapes;
+    DevShape shapes[kMaxShapes];
+    float cell_volume;
+};
+
+// Particle state, structure of arrays.
+struct PArrays {
+    float* x[3];
+    float* v[3];
+    float* B[9];
+    float* F[9];
+    float* Fp[9];   // only when track_fp
+    float* m;
+    float* vol;
+    float* plastic;  // sand: plasticAmount q; snow: J_P = det F_P
+    uint8_t* mat;
+    int32_t* id;     // caller's particle index
+};
+
+struct GArrays {
+    unsigned long long* acc;  // 4 per node: mass, momentum/impulse x, y, z (fixed point)
+    float4* vel;              // (v, m) after normalisation / after grid update
+    float4* vbf;              // before-friction velocity (w unused)
+    uint32_t* flag;           // per node block: touched this step
+    int32_t* active;          // list of touched node blocks
+    int32_t* nactive;         // its length
+};
+
+struct DevStats {
+    unsigned long long out_of_domain;
+    unsigned long long fallbacks;
+    unsigned long long overflow;
+    unsigned long long mass;       // int64 sums, exact
+    unsigned long long mom[3];
+    unsigned long long nodes;      // nodes with mass after P2G
+};
+
+// ---------------------------------------------------------------------------------
+// cubic B-spline weights on one axis for stencil offsets o = 0..3 (node cell-1+o):
+// w[o] = N(f + 1 - o), dw[o] = N'(f + 1 - o) / h, with N, N' of interpolation.cpp:9-33.
+__device__ __forceinline__ void bspline(float f, float inv_h, float w[4], float dw[4]) {
+    float g = 1.0f - f;
+    float f2 = f * f, g2 = g * g;
+    w[0] = g2 * g * (1.0f / 6.0f);
+    w[1] = 0.5f * f2 * f - f2 + (2.0f / 3.0f);
+    w[2] = 0.5f * g2 * g - g2 + (2.0f / 3.0f);
+    w[3] = f2 * f * (1.0f / 6.0f);
+    dw[0] = -0.5f * g2 * inv_h;
+    dw[1] = (1.5f * f2 - 2.0f * f) * inv_h;
+    dw[2] = (2.0f * g - 1.5f * g2) * inv_h;
+    dw[3] = 0.5f * f2 * inv_h;
+}
+
+// Particle location: reference cell (clamped into the grid), fraction in [0,1].
+// Returns true if the particle had to be clamped (it left the grid).
+__device__ __forceinline__ bool locate(const KParams& P, float px, float py, float pz, int cell[3],
+                                       float f[3]) {
+    float p[3] = {px, py, pz};
+    bool clamped = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float u = (p[a] - P.min[a]) * P.inv_h[a];
+        float c = floorf(u);
+        int ci = (int)c;
+        if (!(u >= 0.0f) || ci > P.res[a] - 1) {  // also catches NaN
+            clamped = true;
+            ci = !(u >= 0.0f) ? 0 : P.res[a] - 1;
+        }
+        float fr = u - (float)ci;
+        fr = fminf(fmaxf(fr, 0.0f), 1.0f);
+        cell[a] = ci;
+        f[a] = fr;
+    }
+    return clamped;
+}
+
+// sort key: (padded base-node block, base position inside the block)
+__device__ __forceinline__ uint32_t make_key(const KParams& P, const int cell[3]) {
+    int bx = (cell[0] + 3) >> 2, by = (cell[1] + 3) >> 2, bz = (cell[2] + 3) >> 2;
+    int wx = (cell[0] + 3) & 3, wy = (cell[1] + 3) & 3, wz = (cell[2] + 3) & 3;
+    uint32_t blk = (uint32_t)((bz * P.nb[1] + by) * P.nb[0] + bx);
+    return (blk << 6) | (uint32_t)((wz << 4) | (wy << 2) | wx);
+}
+
+// padded base node of a key
+__device__ __forceinline__ void key_base(const KParams& P, uint32_t key, int base[3]) {
+    uint32_t blk = key >> 6;
+    int bx = (int)(blk % (uint32_t)P.nb[0]);
+    uint32_t r = blk / (uint32_t)P.nb[0];
+    int by = (int)(r % (uint32_t)P.nb[1]);
+    int bz = (int)(r / (uint32_t)P.nb[1]);
+    base[0] = 4 * bx + (int)(key & 3);
+    base[1] = 4 * by + (int)((key >> 2) & 3);
+    base[2] = 4 * bz + (int)((key >> 4) & 3);
+}
+
+// storage index of padded node (x, y, z)
+__device__ __forceinline__ uint32_t node_index(const KParams& P, int x, int y, int z) {
+    uint32_t blk = (uint32_t)(((z >> 2) * P.nb[1] + (y >> 2)) * P.nb[0] + (x >> 2));
+    return (blk << 6) | (uint32_t)(((z & 3) << 4) | ((y & 3) << 2) | (x & 3));
+}
+
+// per-axis partial node indices: idx(ox,oy,oz) = X[ox] + Y[oy] + Z[oz]
+__device__ __forceinline__ void stencil_offsets(const KParams& P, const int base[3], uint32_t X[4],
+                                                uint32_t Y[4], uint32_t Z[4]) {
+    uint32_t sy = (uint32_t)P.nb[0] * 64u, sz = (uint32_t)P.nb[0] * (uint32_t)P.nb[1] * 64u;
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        int x = base[0] + o, y = base[1] + o, z = base[2] + o;
+        X[o] = (uint32_t)(x >> 2) * 64u + (uint32_t)(x & 3);
+        Y[o] = (uint32_t)(y >> 2) * sy + (uint32_t)((y & 3) << 2);
+        Z[o] = (uint32_t)(z >> 2) * sz + (uint32_t)((z & 3) << 4);
+    }
+}
+
+// weights of one particle with the reference's out-of-grid node drop (HS:44-46)
+__device__ __forceinline__ bool particle_weights(const KParams& P, const int cell[3], const float f[3],
+                                                 float w[3][4], float dw[3][4]) {
+    bool truncated = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        bspline(f[a], P.inv_h[a], w[a], dw[a]);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            int node = cell[a] - 1 + o;
+            if (node < 0 || node >= P.res[a]) {
+                w[a][o] = 0.0f;
+                dw[a][o] = 0.0f;
+                truncated = true;
+            }
+        }
+    }
+    return truncated;
+}
+
+// ---------------------------------------------------------------------------------
+// small row-major 3x3 helpers
+template <typename T>
+__device__ __forceinline__ void mat_mul(const T A[9], const T B[9], T C[9]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) C[3 * a + b] = A[3 * a] * B[b] + A[3 * a + 1] * B[3 + b] + A[3 * a + 2] * B[6 + b];
+}
+// C = A * B^T
+template <typename T>
+__device__ __forceinline__ void mat_mul_bt(const T A[9], const T B[9], T C[9]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            C[3 * a + b] = A[3 * a] * B[3 * b] + A[3 * a + 1] * B[3 * b + 1] + A[3 * a + 2] * B[3 * b + 2];
+}
+template <typename T>
+__device__ __forceinline__ T mat_det(const T A[9]) {
+    return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+           A[2] * (A[3] * A[7] - A[4] * A[6]);
+}
+// cof(A) = det(A) A^-T
+template <typename T>
+__device__ __forceinline__ void mat_cofactor(const T A[9], T C[9]) {
+    C[0] = A[4] * A[8] - A[5] * A[7];
+    C[1] = A[5] * A[6] - A[3] * A[8];
+    C[2] = A[3] * A[7] - A[4] * A[6];
+    C[3] = A[2] * A[7] - A[1] * A[8];
+    C[4] = A[0] * A[8] - A[2] * A[6];
+    C[5] = A[1] * A[6] - A[0] * A[7];
+    C[6] = A[1] * A[5] - A[2] * A[4];
+    C[7] = A[2] * A[3] - A[0] * A[5];
+    C[8] = A[0] * A[4] - A[1] * A[3];
+}
+
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+__device__ __forceinline__ float sqrt_t(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_t(double x) { return sqrt(x); }
+__device__ __forceinline__ float exp_t(float x) { return expf(x); }
+__device__ __forceinline__ double exp_t(double x) { return exp(x); }
+__device__ __forceinline__ float log_t(float x) { return logf(x); }
+__device__ __forceinline__ double log_t(double x) { return log(x); }
+__device__ __forceinline__ float sin_t(float x) { return sinf(x); }
+__device__ __forceinline__ double sin_t(double x) { return sin(x); }
+__device__ __forceinline__ float abs_t(float x) { return fabsf(x); }
+__device__ __forceinline__ double abs_t(double x) { return fabs(x); }
+
+// 3x3 SVD by one-sided (Hestenes) Jacobi rotations on the columns of A:
+// A V = U diag(s), s >= 0 (unsorted).  Every quantity the step needs from an
+// SVD (U V^T, U f(s) V^T, V s^-1 U^T with f applied per singular value) is
+// invariant under ordering, so no sort is done.  Returns false if a singular
+// value is below `smin_rel` * the largest (caller falls back to FP64).
+template <typename T>
+__device__ __forceinline__ bool svd3(const T A[9], T U[9], T s[3], T V[9], int max_sweeps, T tol, T smin_rel) {
+    T W[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) W[k] = A[k];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) V[k] = (k % 4 == 0) ? T(1) : T(0);
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        bool rotated = false;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            T alpha = W[p] * W[p] + W[3 + p] * W[3 + p] + W[6 + p] * W[6 + p];
+            T beta = W[q] * W[q] + W[3 + q] * W[3 + q] + W[6 + q] * W[6 + q];
+            T gamma = W[p] * W[q] + W[3 + p] * W[3 + q] + W[6 + p] * W[6 + q];
+            if (abs_t(gamma) > tol * sqrt_t(alpha * beta)) {
+                rotated = true;
+                T zeta = (beta - alpha) / (T(2) * gamma);
+                T az = abs_t(zeta);
+                T t = az > T(1e15) ? T(0.5) / zeta
+                                   : (zeta >= T(0) ? T(1) : T(-1)) / (az + sqrt_t(T(1) + zeta * zeta));
+                T c = rsqrt_t(T(1) + t * t), sn = c * t;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    T wp = W[3 * r + p], wq = W[3 * r + q];
+                    W[3 * r + p] = c * wp - sn * wq;
+                    W[3 * r + q] = sn * wp + c * wq;
+                    T vp = V[3 * r + p], vq = V[3 * r + q];
+                    V[3 * r + p] = c * vp - sn * vq;
+                    V[3 * r + q] = sn * vp + c * vq;
+                }
+            }
+        }
+        if (!rotated) break;
+    }
+    T smax = T(0);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        s[b] = sqrt_t(W[b] * W[b] + W[3 + b] * W[3 + b] + W[6 + b] * W[6 + b]);
+        smax = s[b] > smax ? s[b] : smax;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        if (!(s[b] > smin_rel * smax) || !(s[b] > T(0))) ok = false;
+        T inv = s[b] > T(0) ? T(1) / s[b] : T(0);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) U[3 * r + b] = W[3 * r + b] * inv;
+    }
+    return ok;
+}
+
+// Complete U where a singular value vanished (FP64 path only).
+__device__ inline void svd3_complete(double U[9], const double s[3]) {
+    double smax = fmax(s[0], fmax(s[1], s[2]));
+    double tiny = 1e-300 + 1e-14 * smax;
+    int good[3], ng = 0, bad[3], nbd = 0;
+    for (int b = 0; b < 3; ++b) {
+        if (s[b] > tiny) good[ng++] = b;
+        else bad[nbd++] = b;
+    }
+    for (int k = 0; k < nbd; ++k) {
+        int b = bad[k];
+        double u[3];
+        if (ng == 2) {
+            int c0 = good[0], c1 = good[1];
+            u[0] = U[3 + c0] * U[6 + c1] - U[6 + c0] * U[3 + c1];
+            u[1] = U[6 + c0] * U[c1] - U[c0] * U[6 + c1];
+            u[2] = U[c0] * U[3 + c1] - U[3 + c0] * U[c1];
+        } else {
+            double best = -1;
+            for (int e = 0; e < 3; ++e) {
+                double t[3] = {e == 0 ? 1.0 : 0.0, e == 1 ? 1.0 : 0.0, e == 2 ? 1.0 : 0.0};
+                for (int g = 0; g < ng; ++g) {
+                    int c = good[g];
+                    double d = t[0] * U[c] + t[1] * U[3 + c] + t[2] * U[6 + c];
+                    for (int r = 0; r < 3; ++r) t[r] -= d * U[3 * r + c];
+                }
+                double nn = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+                if (nn > best) { best = nn; u[0] = t[0]; u[1] = t[1]; u[2] = t[2]; }
+            }
+        }
+        double nn = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        for (int r = 0; r < 3; ++r) U[3 * r + b] = u[r] / nn;
+        good[ng++] = b;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Drucker-Prager projection in log-strain space (HybridSolver.cpp:632-674).
+// ln: trial log singular values (in/out), q: plasticAmount (in/out).
+// Returns 0 elastic, 1 apex (s = 1), 2 projected.
+template <typename T>
+__device__ __forceinline__ int dp_project(T ln[3], T& q, T h0, T h1, T h2, T h3, T k) {
+    const T deg = T(3.14159265358979323846 / 180.0);
+    T phi = (h0 + (h1 * q - h3) * exp_t(-h2 * q)) * deg;
+    T sphi = sin_t(phi);
+    T alpha = T(0.81649658092772603273) * T(2) * sphi / (T(3) - sphi);  // sqrt(2/3)
+    T tr = ln[0] + ln[1] + ln[2];
+    T dev[3] = {ln[0] - tr / T(3), ln[1] - tr / T(3), ln[2] - tr / T(3)};
+    T nd = sqrt_t(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
+    T dg = nd + k * tr * alpha;
+    if (dg <= T(0)) return 0;
+    if (nd == T(0) || tr > T(0)) {
+        q += sqrt_t(ln[0] * ln[0] + ln[1] * ln[1] + ln[2] * ln[2]);
+        ln[0] = ln[1] = ln[2] = T(0);
+        return 1;
+    }
+    T sc = dg / nd;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ln[a] -= sc * dev[a];
+    q += dg;
+    return 2;
+}
+
+// ---------------------------------------------------------------------------------
+// level set union (LevelSet.cpp:8-42): phi = min over shapes, n of the minimiser
+__device__ __forceinline__ void eval_levelset(const KParams& P, float x, float y, float z, float& phi,
+                                              float n[3]) {
+    phi = 3.0e38f;
+    n[0] = 0.f; n[1] = 0.f; n[2] = 1.f;
+    for (int i = 0; i < P.nshapes; ++i) {
+        const DevShape& s = P.shapes[i];
+        float ph, nx, ny, nz;
+        if (s.type == kSdfPlane) {
+            ph = s.p[0] * x + s.p[1] * y + s.p[2] * z - s.p[3];
+            nx = s.p[0]; ny = s.p[1]; nz = s.p[2];
+        } else if (s.type == kSdfSphere) {
+            float dx = x - s.p[0], dy = y - s.p[1], dz = z - s.p[2];
+            float r = sqrtf(dx * dx + dy * dy + dz * dz);
+            ph = r - s.p[3];
+            if (r > 0.f) { nx = dx / r; ny = dy / r; nz = dz / r; }
+            else { nx = 0.f; ny = 0.f; nz = 1.f; }
+        } else {
+            float X = s.p[0], Y = s.p[1], G = s.p[2];
+            ph = fminf(fminf(z - G, X - x), Y - y);
+            float adz = fabsf(z - G), adx = fabsf(X - x), ady = fabsf(Y - y);
+            if (adz <= adx && adz <= ady) { nx = 0.f; ny = 0.f; nz = 1.f; }
+            else if (ady <= adx) { nx = 0.f; ny = -1.f; nz = 0.f; }
+            else { nx = -1.f; ny = 0.f; nz = 0.f; }
+        }
+        if (ph < phi) { phi = ph; n[0] = nx; n[1] = ny; n[2] = nz; }
+    }
+}
+
+__device__ __forceinline__ unsigned long long to_fixed(float v, float scale) {
+    return (unsigned long long)__float2ll_rn(v * scale);
+}
+
+}  // namespace aep

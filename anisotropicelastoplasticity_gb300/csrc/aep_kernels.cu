@@ -1,0 +1,852 @@
+// aep_kernels.cu -- the sm_103a kernels of one MPM step.
+//
+// Step dataflow (reference order HybridSolver.cpp:867-989, rotated so the
+// P2G of :987 comes first):
+//   sort (by padded base-node block, then base node)         -> perm
+//   k_p2g        mass + APIC momentum scatter  (HS:113-240)
+//   k_normalize  v_i = p_i / m_i               (HS:233-240)
+//   k_force      gather grad v, SVD, stress, impulse scatter (HS:252-366, 457)
+//   k_grid       v += impulse/m + dt g, level-set collision  (HS:725-737, 460-511)
+//   k_g2p        G2P velocity, APIC, advection, F update, return mapping
+//                (HS:739-825, 940-951, 553-577, 612-681)
+//
+// Scatter design (P2G and force): particles are sorted so that all particles
+// with the same stencil base node are contiguous.  A half-warp (16 lanes)
+// streams through a chunk of sorted particles; lane l owns the four stencil
+// nodes (l&3, l>>2, 0..3) and accumulates their contributions in FP32
+// registers in a fixed particle order.  When the base node changes, the lane
+// converts its sums to int64 fixed point and adds them to the grid with
+// 64-bit atomics.  Integer addition is associative, so the grid sums are
+// order-independent and the step repeats bit-for-bit.  Same-node
+// contributions of all particles that share a base node are merged in
+// registers before any atomic (one atomic per node per run instead of one per
+// particle); __match_any_sync + __ballot_sync find the run structure of each
+// batch of 16 particles.
+#include "aep_device.cuh"
+#include "aep_kernels.h"
+
+namespace aep {
+
+// ===================================================================================
+// keys of the current particle order (after an upload)
+__global__ void k_keys(KParams P, PArrays cur, int n, uint32_t* keys, DevStats* st) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int cell[3];
+    float f[3];
+    bool clamped = locate(P, cur.x[0][j], cur.x[1][j], cur.x[2][j], cell, f);
+    keys[j] = make_key(P, cell);
+    if (clamped) atomicAdd(&st->out_of_domain, 1ull);
+}
+
+// ===================================================================================
+// P2G: mass and APIC momentum (HybridSolver.cpp:113-231).
+// momentum contribution of particle p to node o:  w m (v + D^-1 B (x_i - x_p)),
+// D^-1 = 3/h^2 (:177), x_i - x_p = (o - 1 - f) h  =>  w (b + Mh o) with
+// Mh[:,a] = m D^-1 h_a B[:,a] and b = m v - Mh (1 + f).
+constexpr int kP2GThreads = 128;
+constexpr int kP2GChunk = 64;  // particles per half-warp
+struct alignas(16) P2GPrep {
+    float b[3];
+    float m;
+    float Mh[9];
+    float pad0[3];
+    float wx[4], wy[4], wz[4];
+    int base[3];
+    uint32_t key;
+};
+static_assert(sizeof(P2GPrep) == 128, "prep layout");
+
+__device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, uint32_t key) {
+    uint32_t blk = key >> 6;
+    int bx = (int)(blk % (uint32_t)P.nb[0]);
+    uint32_t r = blk / (uint32_t)P.nb[0];
+    int by = (int)(r % (uint32_t)P.nb[1]);
+    int bz = (int)(r / (uint32_t)P.nb[1]);
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {
+        int x = bx + (d & 1), y = by + ((d >> 1) & 1), z = bz + (d >> 2);
+        uint32_t nb = (uint32_t)((z * P.nb[1] + y) * P.nb[0] + x);
+        if (atomicExch(&G.flag[nb], 1u) == 0u) {
+            int slot = atomicAdd(G.nactive, 1);
+            G.active[slot] = (int32_t)nb;
+        }
+    }
+}
+
+// Run structure of a batch of 16 sorted particles held one per lane of a
+// half-warp: bit t of the result is set if particle t starts a new run of equal
+// keys (the first particle is compared with the run carried in from the
+// previous batch).  __match_any_sync groups the lanes by key; since keys are
+// sorted, a lane heads its group iff it is the lowest lane of the group.
+__device__ __forceinline__ unsigned run_heads(unsigned hmask, int l, uint32_t key, uint32_t carried) {
+    const unsigned peers = __match_any_sync(hmask, key) >> (threadIdx.x & 16);
+    const bool lowest = (peers & ((1u << l) - 1u)) == 0u;
+    const bool head = lowest && !(l == 0 && key == carried);
+    return __ballot_sync(hmask, head) >> (threadIdx.x & 16);
+}
+
+__global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
+                                                     const int32_t* __restrict__ perm, int n, GArrays G) {
+    __shared__ P2GPrep sm[kP2GThreads / 16][16];
+    const int hw = threadIdx.x >> 4, l = threadIdx.x & 15;
+    const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
+    const int ox = l & 3, oy = l >> 2;
+    const long chunk0 = ((long)blockIdx.x * (kP2GThreads / 16) + hw) * kP2GChunk;
+    if (chunk0 >= n) return;  // uniform per half-warp
+    const int cnt_total = (int)min((long)kP2GChunk, (long)n - chunk0);
+
+    float am[4] = {0, 0, 0, 0}, ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+    uint32_t run_key = kInvalidKey;
+    int rb[3] = {0, 0, 0};
+
+    auto flush = [&]() {
+        if (run_key == kInvalidKey) return;
+        int x = rb[0] + ox, y = rb[1] + oy;
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            if (am[oz] != 0.0f) {
+                unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + oz);
+                atomicAdd(a + 0, to_fixed(am[oz], P.mass_scale));
+                atomicAdd(a + 1, to_fixed(ax[oz], P.mom_scale));
+                atomicAdd(a + 2, to_fixed(ay[oz], P.mom_scale));
+                atomicAdd(a + 3, to_fixed(az[oz], P.mom_scale));
+            }
+            am[oz] = ax[oz] = ay[oz] = az[oz] = 0.0f;
+        }
+    };
+
+    for (int b0 = 0; b0 < cnt_total; b0 += 16) {
+        const long j = chunk0 + b0 + l;
+        if (b0 + l < cnt_total) {
+            P2GPrep& s = sm[hw][l];
+            const uint32_t key = keys[j];
+            if (j == 0 || (keys[j - 1] >> 6) != (key >> 6)) mark_blocks(P, G, key);
+            const int pj = perm[j];
+            float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
+            float m = cur.m[pj];
+            int cell[3];
+            float f[3], w[3][4], dw[3][4];
+            locate(P, xp[0], xp[1], xp[2], cell, f);
+            particle_weights(P, cell, f, w, dw);
+            float Bm[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Bm[k] = cur.B[k][pj];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                float vma = m * cur.v[a][pj];
+                float t = vma;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float mh = m * P.apic[c] * Bm[3 * a + c];
+                    s.Mh[3 * a + c] = mh;
+                    t -= mh * (1.0f + f[c]);
+                }
+                s.b[a] = t;
+            }
+            s.m = m;
+#pragma unroll
+            for (int o = 0; o < 4; ++o) { s.wx[o] = w[0][o]; s.wy[o] = w[1][o]; s.wz[o] = w[2][o]; }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) s.base[a] = cell[a] + 3;
+            s.key = key;
+        }
+        __syncwarp(hmask);
+        const int cnt = min(16, cnt_total - b0);
+        const unsigned heads = run_heads(hmask, l, b0 + l < cnt_total ? sm[hw][l].key : kInvalidKey, run_key);
+        for (int t = 0; t < cnt; ++t) {
+            const P2GPrep& s = sm[hw][t];
+            if ((heads >> t) & 1u) {
+                flush();
+                run_key = s.key;
+                rb[0] = s.base[0]; rb[1] = s.base[1]; rb[2] = s.base[2];
+            }
+            const float wxy = s.wx[ox] * s.wy[oy];
+            const float fx = (float)ox, fy = (float)oy;
+            float tx = s.b[0] + s.Mh[0] * fx + s.Mh[1] * fy;
+            float ty = s.b[1] + s.Mh[3] * fx + s.Mh[4] * fy;
+            float tz = s.b[2] + s.Mh[6] * fx + s.Mh[7] * fy;
+#pragma unroll
+            for (int oz = 0; oz < 4; ++oz) {
+                const float w = wxy * s.wz[oz];
+                am[oz] = fmaf(w, s.m, am[oz]);
+                ax[oz] = fmaf(w, tx, ax[oz]);
+                ay[oz] = fmaf(w, ty, ay[oz]);
+                az[oz] = fmaf(w, tz, az[oz]);
+                tx += s.Mh[2];
+                ty += s.Mh[5];
+                tz += s.Mh[8];
+            }
+        }
+        __syncwarp(hmask);
+    }
+    flush();
+}
+
+// ===================================================================================
+// v_i = p_i / m_i on touched nodes (HybridSolver.cpp:233-240); clears the accumulators
+// for the force impulse; exact int64 totals of mass and momentum.
+__global__ void k_normalize(KParams P, GArrays G, DevStats* st) {
+    const int nact = *G.nactive;
+    const long total = (long)nact * 64;
+    long long sm_ = 0, sx = 0, sy = 0, sz = 0;
+    unsigned long long cnt = 0;
+    bool ovf = false;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        uint32_t node = ((uint32_t)G.active[i >> 6] << 6) | (uint32_t)(i & 63);
+        longlong2* a2 = reinterpret_cast<longlong2*>(G.acc + 4ull * node);
+        longlong2 a = a2[0], b = a2[1];
+        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (a.x > 0) {
+            ++cnt;
+            float m = __ll2float_rn(a.x) * P.inv_mass_scale;
+            float inv = 1.0f / m;
+            out = make_float4(__ll2float_rn(a.y) * P.inv_mom_scale * inv, __ll2float_rn(b.x) * P.inv_mom_scale * inv,
+                              __ll2float_rn(b.y) * P.inv_mom_scale * inv, m);
+        }
+        const long long lim = 1ll << 61;
+        ovf |= (a.x > lim) | (a.y > lim) | (a.y < -lim) | (b.x > lim) | (b.x < -lim) | (b.y > lim) | (b.y < -lim);
+        G.vel[node] = out;
+        a2[0] = make_longlong2(0, 0);
+        a2[1] = make_longlong2(0, 0);
+        sm_ += a.x; sx += a.y; sy += b.x; sz += b.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sm_ += __shfl_xor_sync(0xffffffffu, sm_, o);
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (cnt) atomicAdd(&st->nodes, cnt);
+        if (sm_) atomicAdd(&st->mass, (unsigned long long)sm_);
+        if (sx) atomicAdd(&st->mom[0], (unsigned long long)sx);
+        if (sy) atomicAdd(&st->mom[1], (unsigned long long)sy);
+        if (sz) atomicAdd(&st->mom[2], (unsigned long long)sz);
+    }
+    if (ovf) atomicOr(&st->overflow, 1ull);
+}
+
+// ===================================================================================
+// per-particle stress of HybridSolver.cpp:277-352, times -dt (the impulse kernel)
+template <typename T>
+__device__ __forceinline__ void stress_from_svd(const KParams& P, int mat, const T Fh[9], const T F[9], const T U[9],
+                                                const T s[3], const T V[9], T Jp, T vol, T out[9]) {
+    T A[9];
+    if (mat == kSnow) {
+        T hard = exp_t(T(P.snow_xi) * (T(1) - Jp));
+        T mu = T(P.snow_mu) * hard, lambda = T(P.snow_lambda) * hard;
+        T R[9], C[9];
+        mat_mul_bt(U, V, R);  // U V^T
+        mat_cofactor(Fh, C);
+        T J = mat_det(Fh);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) A[k] = T(2) * mu * (Fh[k] - R[k]) + lambda * (J - T(1)) * C[k];
+    } else {
+        T mu = T(P.sand_mu), lambda = T(P.sand_lambda);
+        T ln[3] = {log_t(s[0]), log_t(s[1]), log_t(s[2])};
+        T tr = ln[0] + ln[1] + ln[2];
+        T d[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) d[a] = (T(2) * mu * ln[a] + lambda * tr) / s[a];
+        T UD[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) UD[3 * r + c] = U[3 * r + c] * d[c];
+        mat_mul_bt(UD, V, A);
+    }
+    T st[9];
+    mat_mul_bt(A, F, st);  // * F_E^T
+#pragma unroll
+    for (int k = 0; k < 9; ++k) out[k] = vol * st[k];
+}
+
+constexpr int kFrcThreads = 128;
+struct alignas(16) FrcPrep {
+    float S[9];       // -dt * vol * P * F^T
+    float pad0[3];
+    float wx[4], wy[4], wz[4];
+    float dwx[4], dwy[4], dwz[4];
+    int base[3];
+    uint32_t key;
+};
+static_assert(sizeof(FrcPrep) == 160, "prep layout");
+
+__device__ void particle_stress_impulse(const KParams& P, const GArrays& G, const PArrays& cur, int pj, float dt_force,
+                                        float S[9], float w[3][4], float dw[3][4], int cell[3], DevStats* st) {
+    float f[3];
+    locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
+    particle_weights(P, cell, f, w, dw);
+    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+    uint32_t X[4], Y[4], Z[4];
+    stencil_offsets(P, base, X, Y, Z);
+    // velocity gradient of the P2G velocity (the three SpMVs of HS:269-271)
+    float Gm[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int oz = 0; oz < 4; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 4; ++oy) {
+            const float wyz = w[1][oy] * w[2][oz], dyz = dw[1][oy] * w[2][oz], ydz = w[1][oy] * dw[2][oz];
+#pragma unroll
+            for (int ox = 0; ox < 4; ++ox) {
+                float4 v = __ldg(&G.vel[X[ox] + Y[oy] + Z[oz]]);
+                float g0 = dw[0][ox] * wyz, g1 = w[0][ox] * dyz, g2 = w[0][ox] * ydz;
+                Gm[0] += v.x * g0; Gm[1] += v.x * g1; Gm[2] += v.x * g2;
+                Gm[3] += v.y * g0; Gm[4] += v.y * g1; Gm[5] += v.y * g2;
+                Gm[6] += v.z * g0; Gm[7] += v.z * g1; Gm[8] += v.z * g2;
+            }
+        }
+    float F[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
+    float GF[9], Fh[9];
+    mat_mul(Gm, F, GF);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Fh[k] = F[k] + dt_force * GF[k];  // EDG + EDG_modifier * EDG (:306)
+    const int mat = cur.mat[pj];
+    const float vol = cur.vol[pj];
+    float Jp = 1.0f;
+    if (mat == kSnow) {
+        if (P.track_fp) {
+            float Fp[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
+            Jp = mat_det(Fp);
+        } else {
+            Jp = cur.plastic[pj];
+        }
+    }
+    float U[9], s[3], V[9];
+    bool ok = svd3<float>(Fh, U, s, V, 8, 1e-7f, 2e-2f);
+    float out[9];
+    if (ok) {
+        stress_from_svd<float>(P, mat, Fh, F, U, s, V, Jp, vol, out);
+    } else {
+        double Fd[9], Fhd[9], Ud[9], sd[3], Vd[9], od[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) { Fd[k] = F[k]; Fhd[k] = Fh[k]; }
+        svd3<double>(Fhd, Ud, sd, Vd, 40, 1e-15, 0.0);
+        svd3_complete(Ud, sd);
+        stress_from_svd<double>(P, mat, Fhd, Fd, Ud, sd, Vd, (double)Jp, (double)vol, od);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) out[k] = (float)od[k];
+        atomicAdd(&st->fallbacks, 1ull);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S[k] = -dt_force * out[k];
+}
+
+// impulse scatter: f_i -= sum_p stress_p grad w_ip (HS:356-366), stored as dt * f_i
+__global__ void __launch_bounds__(kFrcThreads) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
+                                                       const int32_t* __restrict__ perm, int n, GArrays G,
+                                                       float dt_force, DevStats* st) {
+    __shared__ FrcPrep sm[kFrcThreads / 32][32];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long chunk0 = ((long)blockIdx.x * (kFrcThreads / 32) + wid) * 32;
+    if (chunk0 >= n) return;
+    const long j = chunk0 + lane;
+    {
+        FrcPrep& s = sm[wid][lane];
+        if (j < n) {
+            const int pj = perm[j];
+            float w[3][4], dw[3][4];
+            int cell[3];
+            particle_stress_impulse(P, G, cur, pj, dt_force, s.S, w, dw, cell, st);
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                s.wx[o] = w[0][o]; s.wy[o] = w[1][o]; s.wz[o] = w[2][o];
+                s.dwx[o] = dw[0][o]; s.dwy[o] = dw[1][o]; s.dwz[o] = dw[2][o];
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) s.base[a] = cell[a] + 3;
+            s.key = keys[j];
+        } else {
+            s.key = kInvalidKey;
+        }
+    }
+    __syncwarp();
+    // stream: half h takes particles [16h, 16h+16)
+    const int h = lane >> 4, l = lane & 15, ox = l & 3, oy = l >> 2;
+    const unsigned hmask = 0xFFFFu << (lane & 16);
+    float fx[4] = {0, 0, 0, 0}, fy[4] = {0, 0, 0, 0}, fz[4] = {0, 0, 0, 0};
+    uint32_t run_key = kInvalidKey;
+    int rb[3] = {0, 0, 0};
+    auto flush = [&]() {
+        if (run_key == kInvalidKey) return;
+        int x = rb[0] + ox, y = rb[1] + oy;
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            if (fx[oz] != 0.0f || fy[oz] != 0.0f || fz[oz] != 0.0f) {
+                unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + oz);
+                atomicAdd(a + 1, to_fixed(fx[oz], P.mom_scale));
+                atomicAdd(a + 2, to_fixed(fy[oz], P.mom_scale));
+                atomicAdd(a + 3, to_fixed(fz[oz], P.mom_scale));
+            }
+            fx[oz] = fy[oz] = fz[oz] = 0.0f;
+        }
+    };
+    const unsigned heads = run_heads(hmask, l, sm[wid][16 * h + l].key, kInvalidKey);
+    for (int t = 16 * h; t < 16 * h + 16; ++t) {
+        const FrcPrep& s = sm[wid][t];
+        if (s.key == kInvalidKey) break;
+        if ((heads >> (t - 16 * h)) & 1u) {
+            flush();
+            run_key = s.key;
+            rb[0] = s.base[0]; rb[1] = s.base[1]; rb[2] = s.base[2];
+        }
+        // grad w = (dwx wy wz, wx dwy wz, wx wy dwz); S g = wz (p1 S0 + p2 S1) + dwz p3 S2
+        const float p1 = s.dwx[ox] * s.wy[oy], p2 = s.wx[ox] * s.dwy[oy], p3 = s.wx[ox] * s.wy[oy];
+        const float ax_ = p1 * s.S[0] + p2 * s.S[1], ay_ = p1 * s.S[3] + p2 * s.S[4], az_ = p1 * s.S[6] + p2 * s.S[7];
+        const float cx = p3 * s.S[2], cy = p3 * s.S[5], cz = p3 * s.S[8];
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            const float wz = s.wz[oz], dz = s.dwz[oz];
+            fx[oz] = fmaf(wz, ax_, fmaf(dz, cx, fx[oz]));
+            fy[oz] = fmaf(wz, ay_, fmaf(dz, cy, fy[oz]));
+            fz[oz] = fmaf(wz, az_, fmaf(dz, cz, fz[oz]));
+        }
+    }
+    flush();
+}
+
+// ===================================================================================
+// grid velocity update + gravity (HS:725-737, 457) and level-set collision with
+// friction (HS:460-511), fused; clears the accumulators and block flags.
+__global__ void k_grid(KParams P, GArrays G, float dt_force, int write_force, double* force_out) {
+    const int nact = *G.nactive;
+    const long total = (long)nact * 64;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const uint32_t blk = (uint32_t)G.active[i >> 6];
+        const uint32_t node = (blk << 6) | (uint32_t)(i & 63);
+        longlong2* a2 = reinterpret_cast<longlong2*>(G.acc + 4ull * node);
+        longlong2 a = a2[0], b = a2[1];
+        float4 v4 = G.vel[node];
+        float4 bf = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float m = v4.w;
+        if (m > 0.0f) {
+            const float inv = P.inv_mom_scale / m;
+            float vx = v4.x + __ll2float_rn(a.y) * inv + dt_force * P.gravity[0];
+            float vy = v4.y + __ll2float_rn(b.x) * inv + dt_force * P.gravity[1];
+            float vz = v4.z + __ll2float_rn(b.y) * inv + dt_force * P.gravity[2];
+            bf = make_float4(vx, vy, vz, 0.f);
+            // node position (unpadded coordinates)
+            uint32_t bx = blk % (uint32_t)P.nb[0], r = blk / (uint32_t)P.nb[0];
+            uint32_t by = r % (uint32_t)P.nb[1], bz = r / (uint32_t)P.nb[1];
+            int ix = (int)(4 * bx + (i & 3)) - 4, iy = (int)(4 * by + ((i >> 2) & 3)) - 4,
+                iz = (int)(4 * bz + ((i >> 4) & 3)) - 4;
+            float px = P.min[0] + ix * P.h[0], py = P.min[1] + iy * P.h[1], pz = P.min[2] + iz * P.h[2];
+            float phi, nn[3];
+            eval_levelset(P, px, py, pz, phi, nn);
+            if (phi <= 0.0f) {
+                float vn = vx * nn[0] + vy * nn[1] + vz * nn[2];
+                if (vn < 0.0f) {
+                    float tx = vx - vn * nn[0], ty = vy - vn * nn[1], tz = vz - vn * nn[2];
+                    bf = make_float4(tx, ty, tz, 0.f);
+                    float nt = sqrtf(tx * tx + ty * ty + tz * tz);
+                    if (nt < -P.friction * vn) {
+                        vx = vy = vz = 0.0f;
+                    } else if (P.friction_bug) {
+                        vx = tx; vy = ty; vz = tz;
+                    } else {
+                        float sc = 1.0f + P.friction * vn / nt;
+                        vx = tx * sc; vy = ty * sc; vz = tz * sc;
+                    }
+                }
+            }
+            v4 = make_float4(vx, vy, vz, m);
+        }
+        if (write_force) {  // f_i without gravity, for parity tests (reference dense order)
+            int ix, iy, iz;
+            uint32_t bx = blk % (uint32_t)P.nb[0], r = blk / (uint32_t)P.nb[0];
+            uint32_t by = r % (uint32_t)P.nb[1], bz = r / (uint32_t)P.nb[1];
+            ix = (int)(4 * bx + (i & 3)) - 4; iy = (int)(4 * by + ((i >> 2) & 3)) - 4; iz = (int)(4 * bz + ((i >> 4) & 3)) - 4;
+            if (ix >= 0 && iy >= 0 && iz >= 0 && ix < P.res[0] && iy < P.res[1] && iz < P.res[2]) {
+                long ng = (long)P.res[0] * P.res[1] * P.res[2];
+                long idx = ((long)iz * P.res[1] + iy) * P.res[0] + ix;
+                double s = (double)P.inv_mom_scale / (double)dt_force;
+                force_out[idx] = (double)a.y * s;
+                force_out[ng + idx] = (double)b.x * s;
+                force_out[2 * ng + idx] = (double)b.y * s;
+            }
+            continue;  // force stage: leave velocities and accumulators untouched
+        }
+        G.vel[node] = v4;
+        G.vbf[node] = bf;
+        a2[0] = make_longlong2(0, 0);
+        a2[1] = make_longlong2(0, 0);
+        if ((i & 63) == 0) G.flag[blk] = 0u;
+    }
+}
+
+// clear accumulators and flags of the touched blocks (after a partial step)
+__global__ void k_grid_clear(GArrays G) {
+    const int nact = *G.nactive;
+    const long total = (long)nact * 64;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const uint32_t blk = (uint32_t)G.active[i >> 6];
+        const uint32_t node = (blk << 6) | (uint32_t)(i & 63);
+        longlong2* a2 = reinterpret_cast<longlong2*>(G.acc + 4ull * node);
+        a2[0] = make_longlong2(0, 0);
+        a2[1] = make_longlong2(0, 0);
+        if ((i & 63) == 0) G.flag[blk] = 0u;
+    }
+}
+
+// ===================================================================================
+// return mapping for snow / sand (HybridSolver.cpp:612-677) from the SVD of F_tr.
+// Returns the new singular values in s (in place); updates plastic.
+template <typename T>
+__device__ __forceinline__ void return_map(const KParams& P, int mat, T s[3], T& q) {
+    if (mat == kSnow) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) s[a] = fmin(fmax(s[a], T(P.snow_lo)), T(P.snow_hi));
+    } else {
+        T ln[3] = {log_t(s[0]), log_t(s[1]), log_t(s[2])};
+        int r = dp_project<T>(ln, q, T(P.sand_h0), T(P.sand_h1), T(P.sand_h2), T(P.sand_h3), T(P.sand_k));
+        if (r == 1) { s[0] = s[1] = s[2] = T(1); }
+        else if (r == 2) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) s[a] = exp_t(ln[a]);
+        }
+    }
+}
+
+// G2P + APIC + advection + F update + return mapping, one thread per particle
+__global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
+                                             int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
+                                             DevStats* st) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int pj = perm[j];
+    float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
+    int cell[3];
+    float f[3], w[3][4], dw[3][4];
+    locate(P, xp[0], xp[1], xp[2], cell, f);
+    const bool truncated = particle_weights(P, cell, f, w, dw);
+    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+    uint32_t X[4], Y[4], Z[4];
+    stencil_offsets(P, base, X, Y, Z);
+    float xi[3][4];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
+
+    float vp[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
+    float C[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Gb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int oz = 0; oz < 4; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 4; ++oy) {
+            const float wyz = w[1][oy] * w[2][oz], dyz = dw[1][oy] * w[2][oz], ydz = w[1][oy] * dw[2][oz];
+#pragma unroll
+            for (int ox = 0; ox < 4; ++ox) {
+                const uint32_t idx = X[ox] + Y[oy] + Z[oz];
+                const float4 v = __ldg(&G.vel[idx]);
+                const float4 b = __ldg(&G.vbf[idx]);
+                const float wt = w[0][ox] * wyz;
+                const float g0 = dw[0][ox] * wyz, g1 = w[0][ox] * dyz, g2 = w[0][ox] * ydz;
+                const float wvx = wt * v.x, wvy = wt * v.y, wvz = wt * v.z;
+                vp[0] += wvx; vp[1] += wvy; vp[2] += wvz;
+                const float e0 = xi[0][ox], e1 = xi[1][oy], e2 = xi[2][oz];
+                C[0] += wvx * e0; C[1] += wvx * e1; C[2] += wvx * e2;
+                C[3] += wvy * e0; C[4] += wvy * e1; C[5] += wvy * e2;
+                C[6] += wvz * e0; C[7] += wvz * e1; C[8] += wvz * e2;
+                xs[0] += wt * b.x; xs[1] += wt * b.y; xs[2] += wt * b.z;
+                Gb[0] += b.x * g0; Gb[1] += b.x * g1; Gb[2] += b.x * g2;
+                Gb[3] += b.y * g0; Gb[4] += b.y * g1; Gb[5] += b.y * g2;
+                Gb[6] += b.z * g0; Gb[7] += b.z * g1; Gb[8] += b.z * g2;
+            }
+        }
+    // advection x = sum w (x_i + dt v^bf_i) (HS:944): exact linear reproduction for a
+    // full stencil; a stencil cut by the grid boundary keeps its lost weight.
+    float xn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) xn[a] = xp[a] + dt * xs[a];
+    if (truncated) {
+        float s0[3], s1[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s0[a] = w[a][0] + w[a][1] + w[a][2] + w[a][3];
+            s1[a] = w[a][0] * xi[a][0] + w[a][1] * xi[a][1] + w[a][2] * xi[a][2] + w[a][3] * xi[a][3];
+        }
+        float sw = s0[0] * s0[1] * s0[2];
+        float swx[3] = {s1[0] * s0[1] * s0[2], s0[0] * s1[1] * s0[2], s0[0] * s0[1] * s1[2]};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) xn[a] += xp[a] * (sw - 1.0f) + swx[a];
+    }
+    // APIC damping (HS:808-824)
+    float Bn[9];
+    const float keep = 1.0f - P.particle_damp;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            float sym = 0.5f * (C[3 * a + b] + C[3 * b + a]);
+            Bn[3 * a + b] = (C[3 * a + b] - sym) + keep * sym;
+        }
+    // F update (HS:560-576)
+    float F[9], GF[9], Ftr[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
+    mat_mul(Gb, F, GF);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
+    // return mapping (HS:612-677)
+    const int mat = cur.mat[pj];
+    float q = cur.plastic[pj];
+    float U[9], s[3], V[9];
+    float Fe[9], sn[3];
+    float sprod = 1.0f;  // prod(s_trial / s_new) for J_P
+    bool used_fp64 = false;
+    double Ud[9], sd[3], Vd[9];
+    bool ok = svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
+    if (ok) {
+        sn[0] = s[0]; sn[1] = s[1]; sn[2] = s[2];
+        return_map<float>(P, mat, sn, q);
+        sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
+        float US[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) US[3 * r + c] = U[3 * r + c] * sn[c];
+        mat_mul_bt(US, V, Fe);
+    } else {
+        used_fp64 = true;
+        double Fd[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fd[k] = Ftr[k];
+        svd3<double>(Fd, Ud, sd, Vd, 40, 1e-15, 0.0);
+        svd3_complete(Ud, sd);
+        double s0[3] = {sd[0], sd[1], sd[2]};
+        double qd = q;
+        return_map<double>(P, mat, sd, qd);
+        q = (float)qd;
+        sprod = (float)((s0[0] / sd[0]) * (s0[1] / sd[1]) * (s0[2] / sd[2]));
+        double US[9], Fed[9];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) US[3 * r + c] = Ud[3 * r + c] * sd[c];
+        mat_mul_bt(US, Vd, Fed);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fe[k] = (float)Fed[k];
+        atomicAdd(&st->fallbacks, 1ull);
+    }
+    if (P.track_fp) {
+        // F_P = V S^-1 U^T F_tr F_P (HS:676)
+        float Fp[9], Ft[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
+        mat_mul(Ftr, Fp, Ft);
+        float VS[9], M[9], Fpn[9];
+        if (!used_fp64) {
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) VS[3 * r + c] = V[3 * r + c] / sn[c];
+            mat_mul_bt(VS, U, M);
+        } else {
+            double VSd[9], Md[9];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) VSd[3 * r + c] = Vd[3 * r + c] / sd[c];
+            mat_mul_bt(VSd, Ud, Md);
+            for (int k = 0; k < 9; ++k) M[k] = (float)Md[k];
+        }
+        mat_mul(M, Ft, Fpn);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = Fpn[k];
+        if (mat == kSnow) q = mat_det(Fpn);
+    } else if (mat == kSnow) {
+        q *= sprod;  // J_P = det F_P = det(F_tr) det(F_P) / det(S_new)
+    }
+    // store in the new order
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        nxt.x[a][j] = xn[a];
+        nxt.v[a][j] = vp[a];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        nxt.B[k][j] = Bn[k];
+        nxt.F[k][j] = Fe[k];
+    }
+    nxt.plastic[j] = q;
+    nxt.mat[j] = (uint8_t)mat;
+    nxt.m[j] = cur.m[pj];
+    nxt.vol[j] = cur.vol[pj];
+    nxt.id[j] = cur.id[pj];
+    int ncell[3];
+    float nf[3];
+    bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nf);
+    keys_next[j] = make_key(P, ncell);
+    if (clamped) atomicAdd(&st->out_of_domain, 1ull);
+}
+
+// ===================================================================================
+// first-P2G densities and volumes (HybridSolver.cpp:242-249):
+// rho_p = sum_i w_ip m_i / h^3, vol_p = m_p / rho_p; written in the current order.
+__global__ void k_volumes(KParams P, PArrays cur, const int32_t* __restrict__ perm, int n, GArrays G) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int pj = perm[j];
+    int cell[3];
+    float f[3], w[3][4], dw[3][4];
+    locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
+    particle_weights(P, cell, f, w, dw);
+    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+    uint32_t X[4], Y[4], Z[4];
+    stencil_offsets(P, base, X, Y, Z);
+    float s = 0.0f;
+    for (int oz = 0; oz < 4; ++oz)
+        for (int oy = 0; oy < 4; ++oy)
+            for (int ox = 0; ox < 4; ++ox) s += w[0][ox] * w[1][oy] * w[2][oz] * G.vel[X[ox] + Y[oy] + Z[oz]].w;
+    float rho = s / P.cell_volume;
+    cur.vol[pj] = cur.m[pj] / rho;
+}
+
+// ===================================================================================
+// layout conversion: reference FP64 layouts <-> device FP32 structure of arrays
+// mode: 0 = N x 3 column-major vector field into dst[3], 1 = 9N B rows (see aep.h),
+// 2 = 9N per-particle column-major 3x3 into row-major dst[9], 3 = N scalars
+__global__ void k_upload(int n, int mode, const double* __restrict__ src, float* d0, float* d1, float* d2,
+                         float* d3, float* d4, float* d5, float* d6, float* d7, float* d8) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float* d[9] = {d0, d1, d2, d3, d4, d5, d6, d7, d8};
+    if (mode == 0) {
+        for (int a = 0; a < 3; ++a) d[a][p] = (float)src[(long)a * n + p];
+    } else if (mode == 1) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[(long)a * 3 * n + (long)b * n + p];
+    } else if (mode == 2) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[9l * p + a + 3 * b];
+    } else {
+        d[0][p] = (float)src[p];
+    }
+}
+
+__global__ void k_download(int n, int mode, const int32_t* __restrict__ id, double* __restrict__ dst,
+                           const float* s0, const float* s1, const float* s2, const float* s3, const float* s4,
+                           const float* s5, const float* s6, const float* s7, const float* s8) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const float* s[9] = {s0, s1, s2, s3, s4, s5, s6, s7, s8};
+    const long p = id[j];
+    if (mode == 0) {
+        for (int a = 0; a < 3; ++a) dst[(long)a * n + p] = s[a][j];
+    } else if (mode == 1) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) dst[(long)a * 3 * n + (long)b * n + p] = s[3 * a + b][j];
+    } else if (mode == 2) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) dst[9 * p + a + 3 * b] = s[3 * a + b][j];
+    } else {
+        dst[p] = s[0][j];
+    }
+}
+
+__global__ void k_init_particles(int n, PArrays cur, const uint8_t* __restrict__ mat_in, int has_fp, int track_fp) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    cur.id[p] = p;
+    int mat = mat_in ? mat_in[p] : kSand;
+    cur.mat[p] = (uint8_t)mat;
+    if (!has_fp && track_fp)
+        for (int k = 0; k < 9; ++k) cur.Fp[k][p] = (k % 4 == 0) ? 1.0f : 0.0f;
+}
+
+// snow particles carry J_P = det F_P in `plastic` when F_P is not tracked
+__global__ void k_snow_jp(int n, PArrays cur, const double* __restrict__ Fp) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    if (cur.mat[p] != kSnow) return;
+    double A[9];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) A[3 * a + b] = Fp ? Fp[9l * p + a + 3 * b] : (a == b ? 1.0 : 0.0);
+    cur.plastic[p] = (float)mat_det(A);
+}
+
+// dense grid readback in reference order (mode 0: P2G state; 1: after grid update)
+__global__ void k_grid_dense(KParams P, GArrays G, double* mass, double* vel, double* vbf) {
+    const int nact = *G.nactive;
+    const long total = (long)nact * 64;
+    const long ng = (long)P.res[0] * P.res[1] * P.res[2];
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const uint32_t blk = (uint32_t)G.active[i >> 6];
+        const uint32_t node = (blk << 6) | (uint32_t)(i & 63);
+        uint32_t bx = blk % (uint32_t)P.nb[0], r = blk / (uint32_t)P.nb[0];
+        uint32_t by = r % (uint32_t)P.nb[1], bz = r / (uint32_t)P.nb[1];
+        int ix = (int)(4 * bx + (i & 3)) - 4, iy = (int)(4 * by + ((i >> 2) & 3)) - 4,
+            iz = (int)(4 * bz + ((i >> 4) & 3)) - 4;
+        if (ix < 0 || iy < 0 || iz < 0 || ix >= P.res[0] || iy >= P.res[1] || iz >= P.res[2]) continue;
+        long idx = ((long)iz * P.res[1] + iy) * P.res[0] + ix;
+        float4 v = G.vel[node];
+        if (mass) mass[idx] = v.w;
+        if (vel) { vel[idx] = v.x; vel[ng + idx] = v.y; vel[2 * ng + idx] = v.z; }
+        if (vbf) {
+            float4 b = G.vbf[node];
+            vbf[idx] = b.x; vbf[ng + idx] = b.y; vbf[2 * ng + idx] = b.z;
+        }
+    }
+}
+
+// ===================================================================================
+// host launchers
+static inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
+
+void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, DevStats* st, cudaStream_t s) {
+    if (n > 0) k_keys<<<blocks_for(n, 256), 256, 0, s>>>(P, cur, n, keys, st);
+}
+void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
+                const GArrays& G, cudaStream_t s) {
+    long hw = (n + kP2GChunk - 1) / kP2GChunk;
+    if (n > 0) k_p2g<<<blocks_for(hw, kP2GThreads / 16), kP2GThreads, 0, s>>>(P, cur, keys, perm, n, G);
+}
+void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s) {
+    k_normalize<<<grid_blocks, 256, 0, s>>>(P, G, st);
+}
+void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
+                  const GArrays& G, float dt_force, DevStats* st, cudaStream_t s) {
+    long warps = (n + 31) / 32;
+    if (n > 0) k_force<<<blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s>>>(P, cur, keys, perm, n, G, dt_force, st);
+}
+void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
+                 int grid_blocks, cudaStream_t s) {
+    k_grid<<<grid_blocks, 256, 0, s>>>(P, G, dt_force, write_force, force_out);
+}
+void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s) {
+    k_grid_clear<<<grid_blocks, 256, 0, s>>>(G);
+}
+void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, cudaStream_t s) {
+    if (n > 0) k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st);
+}
+void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
+                    cudaStream_t s) {
+    if (n > 0) k_volumes<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, perm, n, G);
+}
+void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s) {
+    if (n > 0)
+        k_upload<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, src, dst[0], dst[1], dst[2], dst[3], dst[4], dst[5],
+                                                    dst[6], dst[7], dst[8]);
+}
+void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s) {
+    if (n > 0)
+        k_download<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, id, dst, src[0], src[1], src[2], src[3], src[4],
+                                                      src[5], src[6], src[7], src[8]);
+}
+void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp, cudaStream_t s) {
+    if (n > 0) k_init_particles<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, mat, has_fp, track_fp);
+}
+void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s) {
+    if (n > 0) k_snow_jp<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, Fp);
+}
+void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double* vel, double* vbf, int grid_blocks,
+                       cudaStream_t s) {
+    k_grid_dense<<<grid_blocks, 256, 0, s>>>(P, G, mass, vel, vbf);
+}
+
+}  // namespace aep

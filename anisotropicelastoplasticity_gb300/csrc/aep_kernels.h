@@ -1,0 +1,34 @@
+// aep_kernels.h -- host launchers of the kernels in aep_kernels.cu.
+#pragma once
+
+#include "aep_device.cuh"
+
+namespace aep {
+
+void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, DevStats* st, cudaStream_t s);
+void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
+                const GArrays& G, cudaStream_t s);
+void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s);
+void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
+                  const GArrays& G, float dt_force, DevStats* st, cudaStream_t s);
+void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
+                 int grid_blocks, cudaStream_t s);
+void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s);
+void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, cudaStream_t s);
+void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
+                    cudaStream_t s);
+void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s);
+void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s);
+void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp,
+                           cudaStream_t s);
+void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s);
+void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double* vel, double* vbf,
+                       int grid_blocks, cudaStream_t s);
+
+// radix sort of (key, index) pairs; implemented with CUB in aep_sort.cu
+size_t sort_temp_bytes(int n, int key_bits);
+cudaError_t sort_pairs(void* temp, size_t temp_bytes, const uint32_t* keys_in, uint32_t* keys_out,
+                       const int32_t* vals_in, int32_t* vals_out, int n, int key_bits, cudaStream_t s);
+
+}  // namespace aep

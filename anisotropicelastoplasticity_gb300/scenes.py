@@ -1,0 +1,101 @@
+"""Seeded synthetic scenes for the benchmark configurations.
+
+The reference builds its scenes with unseeded rand()/time(0) generators
+(ParticleSystem.cpp:119-401); these generators are new and seeded (numpy PCG64).
+All scenes use the reference's frame: gravity along -z and the ground level
+set on x[2] (HybridSolver.cpp:457, LevelSet.cpp:8-16).  A configuration stated
+with y up is rotated to z up (the solids are isotropic and gravity and the
+ground plane rotate together, so the dynamics are the same).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+from .solver import LevelSet, ParticleSystem, RegularGrid, make_params
+
+
+@dataclass
+class Scene:
+    name: str
+    grid: RegularGrid
+    particles: ParticleSystem
+    levelset: LevelSet
+    params: capi.aep_params
+    dt: float
+    steps: int
+    note: str = ""
+
+
+def _block(rng, n, lo, hi):
+    lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+    return lo + rng.random((n, 3)) * (hi - lo)
+
+
+def _particles(x, v, m, vol, mat):
+    n = len(x)
+    return ParticleSystem(positions=x, velocities=v, masses=m, volumes=vol,
+                          elastic_deformation_gradients=np.tile(np.eye(3), (n, 1, 1)),
+                          plastic_deformation_gradients=np.tile(np.eye(3), (n, 1, 1)),
+                          affine_momenta=np.zeros((n, 3, 3)), plastic_amount=np.zeros(n),
+                          material=np.full(n, mat, dtype=np.uint8) if np.isscalar(mat) else mat)
+
+
+def snow_block(n: int = 32768, res: int = 64, seed: int = 0, track_plastic_F: bool = False) -> Scene:
+    """Plain snow block drop: 32,768 particles in [0.375, 0.625]^3 of a 64^3 grid over
+    [0,1]^3, 8 per cell, velocity 1 m/s towards the ground, snow E=1.4e5, nu=0.2,
+    theta_c=2.5e-2, theta_s=7.5e-3, xi=10, density 400, ground at 0.05 with mu=0.2,
+    dt=1e-4, 200 steps."""
+    rng = np.random.default_rng(seed)
+    x = _block(rng, n, [0.375] * 3, [0.625] * 3)
+    side = 0.25
+    m = np.full(n, 400.0 * side ** 3 / n)
+    v = np.tile([0.0, 0.0, -1.0], (n, 1))
+    ps = _particles(x, v, m, m / 400.0, capi.AEP_SNOW)
+    prm = make_params(friction=0.2, track_plastic_F=int(track_plastic_F))
+    return Scene("snow_block", RegularGrid([0, 0, 0], [1, 1, 1], [res] * 3), ps, LevelSet.ground(0.05), prm,
+                 1e-4, 200, "quadratic stencil in the configuration text; the reference is cubic (interpolation.cpp:9-33)")
+
+
+def sand_column(n: int = 524288, res: int = 128, seed: int = 1) -> Scene:
+    """Sand column collapse: 524,288 particles in a cylinder r=0.1, height 0.4 on the
+    ground at 0.05, axis at x=y=0.5, grid 128^3, Drucker-Prager sand E=3.537e5,
+    nu=0.3, friction angle 35 deg (h0), density 2200, ground mu=0.5, dt=5e-5, 1000 steps."""
+    rng = np.random.default_rng(seed)
+    r = 0.1 * np.sqrt(rng.random(n))
+    th = 2.0 * np.pi * rng.random(n)
+    z = 0.05 + 0.4 * rng.random(n)
+    x = np.stack([0.5 + r * np.cos(th), 0.5 + r * np.sin(th), z], axis=1)
+    vol_total = np.pi * 0.1 ** 2 * 0.4
+    m = np.full(n, 2200.0 * vol_total / n)
+    ps = _particles(x, np.zeros((n, 3)), m, m / 2200.0, capi.AEP_SAND)
+    prm = make_params(friction=0.5, sand_h0=35.0)
+    return Scene("sand_column", RegularGrid([0, 0, 0], [1, 1, 1], [res] * 3), ps, LevelSet.ground(0.05), prm,
+                 5e-5, 1000, f"{n / (vol_total * res ** 3):.1f} particles per cell at this N")
+
+
+def snow_sand_collision(n: int = 2097152, res: int = 256, seed: int = 3) -> Scene:
+    """Mixed snow and sand at scale: half snow (snow-block material, density 400), half
+    sand (sand-column material, density 2200) in two cubes of 8 particles per cell,
+    placed at random (seed 3) and colliding at relative speed 2; grid 256^3."""
+    rng = np.random.default_rng(seed)
+    nh = n // 2
+    side = (nh / 8.0) ** (1.0 / 3.0) / res
+    c_snow = np.array([0.30, 0.50, 0.30]) + 0.04 * (rng.random(3) - 0.5)
+    c_sand = np.array([0.70, 0.50, 0.30]) + 0.04 * (rng.random(3) - 0.5)
+    xs = _block(rng, nh, c_snow - side / 2, c_snow + side / 2)
+    xd = _block(rng, n - nh, c_sand - side / 2, c_sand + side / 2)
+    x = np.concatenate([xs, xd])
+    v = np.concatenate([np.tile([1.0, 0, 0], (nh, 1)), np.tile([-1.0, 0, 0], (n - nh, 1))])
+    m = np.concatenate([np.full(nh, 400.0 * side ** 3 / nh), np.full(n - nh, 2200.0 * side ** 3 / (n - nh))])
+    vol = np.concatenate([np.full(nh, side ** 3 / nh), np.full(n - nh, side ** 3 / (n - nh))])
+    mat = np.concatenate([np.full(nh, capi.AEP_SNOW, np.uint8), np.full(n - nh, capi.AEP_SAND, np.uint8)])
+    ps = _particles(x, v, m, vol, mat)
+    prm = make_params(friction=0.5)
+    return Scene("snow_sand_collision", RegularGrid([0, 0, 0], [1, 1, 1], [res] * 3), ps, LevelSet.ground(0.05),
+                 prm, 5e-5, 500)
+
+
+CONFIGS = {0: snow_block, 1: sand_column, 3: snow_sand_collision}

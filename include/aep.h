@@ -1,0 +1,245 @@
+/*
+ * aep.h -- C-ABI of the GB300 MPM step (APIC transfers, cubic B-spline weights,
+ * snow / Drucker-Prager sand / anisotropic cloth elastoplasticity, level-set
+ * collision).  Plain pointers and sizes only; no CUDA or C++ types cross it.
+ *
+ * The reference has no C API: its boundary is the C++ class surface of
+ * HybridSolver / ParticleSystem / RegularGrid / LagrangianMesh (public Eigen
+ * members, read and written in place).  Each entry point below names the
+ * reference interface it replaces.  All host arrays use the reference's memory
+ * layouts so that a caller can pass Eigen's data() pointers unchanged:
+ *
+ *   "N x 3 column-major"  = Eigen::MatrixX3d: all x, then all y, then all z.
+ *   "3x3 column-major"    = Eigen::Matrix3d: M(a,b) at [a + 3*b]; a
+ *                           std::vector<Matrix3d> of N is 9*N doubles.
+ *   affine momenta B      = affineMomenta_1 | affineMomenta_2 | affineMomenta_3
+ *                           (each N x 3 column-major; row p of affineMomenta_a
+ *                           is row a of the particle's 3x3 B), 9*N doubles.
+ *   grid node index       = k*Rx*Ry + j*Rx + i (RegularGrid.cpp:164-168).
+ *
+ * Errors: every function returns an aep_status; the reference instead spins
+ * in while(1) or calls exit() (RegularGrid.cpp:134, LagrangianMesh.cpp:213,360,474).
+ * Threading: one host thread per handle; work is ordered on the handle's stream.
+ */
+#ifndef AEP_H
+#define AEP_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AEP_ABI_VERSION 1
+
+/* Opaque solver handle: device state of one particle system on one grid. */
+typedef struct aep_solver aep_solver;
+
+typedef enum aep_status {
+    AEP_OK = 0,
+    AEP_INVALID_ARG = 1,     /* bad size, null pointer, bad enum value            */
+    AEP_CUDA_ERROR = 2,      /* a CUDA runtime call failed                        */
+    AEP_OVERFLOW = 3,        /* a fixed-point grid accumulator left its range     */
+    AEP_OUT_OF_DOMAIN = 4,   /* reserved: particles are clamped and counted       */
+    AEP_NOT_READY = 5,       /* call order violated (e.g. step before particles)  */
+    AEP_OUT_OF_MEMORY = 6,   /* device allocation failed                          */
+    AEP_NO_DEVICE = 7        /* no CUDA device visible                            */
+} aep_status;
+
+/* Particle material tags (the reference hard-codes one MaterialType for the
+ * whole system, HybridSolver.h:21-25 and HybridSolver.cpp:873,955,959; here
+ * the tag is per particle). */
+enum { AEP_SNOW = 0, AEP_SAND = 1 };
+
+/* Level-set shapes (replaces the LevelSet/DLevelSet std::function pair,
+ * HybridSolver.h:18-19, LevelSet.cpp:8-42).  Several shapes are unioned:
+ * phi = min over shapes, normal = the normal of the minimising shape. */
+enum {
+    AEP_SDF_PLANE = 0,       /* p[0..2] = unit normal n, p[3] = offset: phi = n.x - p[3]
+                                (groundLevelSet(x, g) is n=(0,0,1), offset g)        */
+    AEP_SDF_SPHERE = 1,      /* p[0..2] = centre, p[3] = radius: phi = |x-c| - r    */
+    AEP_SDF_WALL2GROUND = 2  /* p[0] = wallX, p[1] = wallY, p[2] = groundZ
+                                (wall2groundLevelSet / Dwall2groundLevelSet)        */
+};
+
+typedef struct aep_sdf {
+    int32_t type;
+    int32_t reserved;
+    double p[6];
+} aep_sdf;
+
+/* RegularGrid(minBound, maxBound, resolution), RegularGrid.cpp:117-162:
+ * h = (max - min) / res per axis; node (i,j,k) sits at min + (i,j,k)*h. */
+typedef struct aep_grid_desc {
+    double min[3];
+    double max[3];
+    int32_t res[3];
+    int32_t reserved;
+} aep_grid_desc;
+
+/* Fixed-corotated snow with hardening (HybridSolver.cpp:281-287,314-325,626-631). */
+typedef struct aep_snow_params {
+    double E, nu;            /* Young's modulus, Poisson ratio (ParticleSystem.cpp:173-174) */
+    double theta_c;          /* critical compression (clamp 1 - theta_c)               */
+    double theta_s;          /* critical stretch     (clamp 1 + theta_s)               */
+    double xi;               /* hardening coefficient, reference literal 10 (HS:267)    */
+} aep_snow_params;
+
+/* Drucker-Prager sand (HybridSolver.cpp:326-339,632-674). */
+typedef struct aep_sand_params {
+    double E, nu;
+    double h0, h1, h2, h3;   /* friction-angle hardening, reference 35, 9, 0.2, 10 (HS:641-644) */
+} aep_sand_params;
+
+typedef struct aep_params {
+    aep_snow_params snow;
+    aep_sand_params sand;
+    double gravity[3];       /* reference: (0, 0, -9.8), HybridSolver.cpp:457          */
+    double friction;         /* grid friction mu, reference literal 0.2 (HS:465)        */
+    int32_t friction_bug;    /* 1: reproduce the dropped Coulomb term of HS:500-501
+                                (sliding nodes keep the full tangential velocity);
+                                0: Coulomb friction v_t + mu v_n v_t/|v_t|             */
+    int32_t track_plastic_F; /* 1: keep the full 3x3 plastic gradient F_P per particle
+                                (HS:676); 0: keep only J_P = det F_P, which is all the
+                                step reads (HS:283)                                    */
+    double particle_damp;    /* APIC symmetric-part damping, reference 0 (HS:916)      */
+    int32_t mass_bits;       /* fixed-point fraction bits of the grid mass accumulator,
+                                relative to the heaviest particle (default 34)         */
+    int32_t momentum_bits;   /* same for momentum and force impulse, relative to
+                                (heaviest particle mass) x (1 m/s)   (default 40)      */
+    int64_t reserved[8];
+} aep_params;
+
+/* Counters of the last step (all zero until a step ran). */
+typedef struct aep_stats {
+    int64_t steps;              /* steps taken by this handle                            */
+    int64_t num_particles;
+    int64_t active_blocks;      /* 4x4x4 node blocks touched by the last P2G             */
+    int64_t out_of_domain;      /* particles clamped into the grid in the last step     */
+    int64_t fp64_fallbacks;     /* particles whose SVD / projection ran in FP64          */
+    int64_t overflow;           /* nonzero if a fixed-point accumulator overflowed       */
+    int64_t active_nodes;       /* grid nodes with mass after the last P2G               */
+    double total_mass;          /* grid mass after the last P2G (exact fixed-point sum)  */
+    double total_momentum[3];   /* grid momentum after the last P2G                      */
+    double reserved[7];
+} aep_stats;
+
+/* ---- version / defaults ------------------------------------------------------- */
+
+int32_t aep_abi_version(void);
+
+/* Reference literal values (see field comments above). */
+void aep_default_params(aep_params* params);
+
+/* ---- lifetime ------------------------------------------------------------------ */
+
+/* Replaces HybridSolver(ParticleSystem*, RegularGrid*) + RegularGrid(min,max,res)
+ * (HybridSolver.h:83-87, RegularGrid.cpp:117-162).  Picks the current CUDA device. */
+aep_status aep_solver_create(const aep_grid_desc* grid, const aep_params* params,
+                             aep_solver** out);
+aep_status aep_solver_destroy(aep_solver* s);
+
+/* ---- state upload (by copy, reference layouts) ------------------------------------ */
+
+/* Replaces the ParticleSystem constructor / HybridSolver::setParticleSystem
+ * (ParticleSystem.cpp:81-117, HybridSolver.h:86).  x, v: N x 3 column-major;
+ * B: 9N (see top), may be NULL (zero); Fe, Fp: 9N (3x3 column-major per
+ * particle), Fp may be NULL (identity); m, vol: N; plastic: N, the sand
+ * plasticAmount (ParticleSystem.h:31), may be NULL (zero); material: N tags.
+ * For snow particles the scalar J_P = det(Fp) is derived from Fp.             */
+aep_status aep_set_particles(aep_solver* s, int64_t n,
+                             const double* x, const double* v, const double* B,
+                             const double* Fe, const double* Fp,
+                             const double* m, const double* vol,
+                             const double* plastic, const uint8_t* material);
+
+/* Replaces HybridSolver::setLevelSet(phi, dphi) (HybridSolver.h:89). */
+aep_status aep_set_levelset(aep_solver* s, const aep_sdf* shapes, int32_t n);
+
+/* ---- stepping -------------------------------------------------------------------- */
+
+/* The first P2G of HybridSolver::solve with evaluateVolumesAndDensities = true
+ * (HybridSolver.cpp:242-249, called at :854): rho_p = sum_i w_ip m_i / h^3,
+ * vol_p = m_p / rho_p.  Overwrites the uploaded volumes.                       */
+aep_status aep_init_volumes(aep_solver* s);
+
+/* One MPM time step: the body of the while loop of HybridSolver::solve
+ * (HybridSolver.cpp:867-989) with a fixed dt, rotated so that the P2G that
+ * the reference runs last (:987) runs first: P2G -> grid forces -> grid
+ * velocity update + gravity -> collision/friction -> G2P (velocity, APIC
+ * affine, advection) -> F update -> return mapping.  Stream-ordered, returns
+ * without waiting for the GPU.                                                 */
+aep_status aep_step(aep_solver* s, double dt);
+
+/* Wait for all work of the handle; returns the status of the work (overflow). */
+aep_status aep_synchronize(aep_solver* s);
+
+/* ---- readback ------------------------------------------------------------------- */
+
+/* Replaces reading ParticleSystem's public members (ParticleSystem.h:28-41).
+ * Arrays in the layout of aep_set_particles, in the caller's original particle
+ * order; any pointer may be NULL.  Fp is only available with track_plastic_F.
+ * plastic returns the sand plasticAmount for sand particles and J_P for snow. */
+aep_status aep_get_particles(aep_solver* s, int64_t n,
+                             double* x, double* v, double* B,
+                             double* Fe, double* Fp, double* vol, double* plastic);
+
+/* Replaces reading RegularGrid::masses / velocities (RegularGrid.h:49-55).
+ * Dense arrays in reference node order; mass: Ng, vel: Ng x 3 column-major
+ * (the grid velocity after the last grid update and collision, or after the
+ * last P2G when stage == AEP_STAGE_P2G), vbf: the before-friction velocity
+ * (HybridSolver.cpp:460-511), force: f_i without gravity after the force
+ * stage.  Any pointer may be NULL.                                             */
+aep_status aep_get_grid(aep_solver* s, double* mass, double* vel, double* vbf,
+                        double* force);
+
+aep_status aep_get_stats(aep_solver* s, aep_stats* out);
+
+/* ---- staged stepping for parity tests ----------------------------------------------- */
+
+enum {
+    AEP_STAGE_P2G = 1,       /* stop after P2G + velocity normalisation          */
+    AEP_STAGE_FORCES = 2,    /* stop after the force scatter                      */
+    AEP_STAGE_GRID = 3,      /* stop after grid update + collision                */
+    AEP_STAGE_FULL = 4       /* the whole step (same as aep_step)                 */
+};
+
+/* Run one step up to `stage` (inclusive).  A partial step leaves the particle
+ * state untouched; the next call starts a fresh step.                          */
+aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage);
+
+/* ---- streams and timing ----------------------------------------------------------- */
+
+/* Order all later work of the handle on `cuda_stream` (a cudaStream_t of the
+ * handle's device; NULL restores the handle's own stream).  The reference has
+ * no counterpart (it is single-threaded CPU code).                            */
+aep_status aep_set_stream(aep_solver* s, void* cuda_stream);
+
+/* Kernel phases of one step, in launch order. */
+enum {
+    AEP_PHASE_SORT = 0,      /* radix sort of the particle keys                  */
+    AEP_PHASE_P2G = 1,       /* mass + APIC momentum scatter                     */
+    AEP_PHASE_NORMALIZE = 2, /* v = p / m on touched nodes                       */
+    AEP_PHASE_FORCE = 3,     /* grad v gather, SVD, stress, impulse scatter      */
+    AEP_PHASE_GRID = 4,      /* grid update, gravity, collision                  */
+    AEP_PHASE_G2P = 5,       /* G2P, APIC, advection, F update, return mapping   */
+    AEP_NUM_PHASES = 6
+};
+
+/* Enable (1) or disable (0) CUDA-event timing of every phase on the handle's
+ * stream.  Enabling resets the accumulated times.                             */
+aep_status aep_set_profiling(aep_solver* s, int32_t on);
+
+/* Accumulated milliseconds per phase since profiling was enabled, and the
+ * number of timed steps.  Synchronises the handle's stream.                  */
+aep_status aep_get_phase_times(aep_solver* s, double ms[AEP_NUM_PHASES], int64_t* steps);
+
+/* Human-readable text of the last error on this handle (static storage). */
+const char* aep_last_error(aep_solver* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AEP_H */

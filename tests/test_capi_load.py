@@ -1,0 +1,68 @@
+"""The C-ABI library builds, loads and exports every symbol include/aep.h declares;
+the ctypes structures match the C layout (checked against gcc's sizeof/offsetof)."""
+import ctypes as C
+import re
+import subprocess
+
+import pytest
+
+from anisotropicelastoplasticity_gb300 import _build, capi
+
+from .conftest import ROOT
+
+HEADER = ROOT / "include" / "aep.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(aep_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_build_and_load():
+    lib = _build.build()
+    assert lib.exists()
+    capi.load()
+
+
+def test_exports_every_declared_symbol():
+    lib = capi.load()
+    names = declared_functions()
+    assert len(names) >= 14
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) <= set(capi.SIGNATURES), set(names) - set(capi.SIGNATURES)
+
+
+def test_no_device_calls_without_gpu_are_safe():
+    lib = capi.load()
+    assert lib.aep_abi_version() == 1
+    p = capi.default_params()
+    assert p.gravity[2] == -9.8 and p.friction == 0.2 and p.friction_bug == 1
+    assert p.sand.h0 == 35.0 and p.snow.xi == 10.0
+
+
+def test_null_arguments_rejected():
+    lib = capi.load()
+    h = C.c_void_p()
+    assert lib.aep_solver_create(None, None, C.byref(h)) == capi.AEP_INVALID_ARG
+    g = capi.aep_grid_desc()
+    g.res[0] = g.res[1] = g.res[2] = 0
+    assert lib.aep_solver_create(C.byref(g), None, C.byref(h)) == capi.AEP_INVALID_ARG
+    assert lib.aep_step(None, 1e-4) == capi.AEP_INVALID_ARG
+    assert lib.aep_solver_destroy(None) == capi.AEP_INVALID_ARG
+
+
+def test_struct_layout_matches_header(tmp_path):
+    src = tmp_path / "sz.c"
+    src.write_text(f'#include "{HEADER}"\n#include <stdio.h>\n#include <stddef.h>\n'
+                   "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(aep_sdf), sizeof(aep_grid_desc),"
+                   " sizeof(aep_params), sizeof(aep_stats), offsetof(aep_params, friction_bug),"
+                   " offsetof(aep_params, mass_bits), offsetof(aep_stats, total_mass)); return 0;}\n")
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", str(src), "-o", str(exe)], check=True)
+    got = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
+    want = [C.sizeof(capi.aep_sdf), C.sizeof(capi.aep_grid_desc), C.sizeof(capi.aep_params),
+            C.sizeof(capi.aep_stats), capi.aep_params.friction_bug.offset, capi.aep_params.mass_bits.offset,
+            capi.aep_stats.total_mass.offset]
+    assert got == want

@@ -1,0 +1,169 @@
+"""GPU step (libaep.so through the C-ABI) against the FP64 oracle on identical
+seeded inputs: grid state after P2G, after the force scatter and after the grid
+update + collision, particle state after 1 and 10 steps, first-P2G volumes,
+bit-for-bit repeatability, exact mass conservation, and edge cases.
+
+Tolerances are FP32-vs-FP64: the bulk arithmetic is FP32 with int64
+fixed-point grid sums; each bound is stated at its assertion."""
+import numpy as np
+import pytest
+
+from anisotropicelastoplasticity_gb300 import AepError, HybridSolver, capi, scenes
+
+from .parity_util import make_pair, mass_weighted_rel, max_rel, perturbed, small_scene
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["snow", "sand", "mixed", "boundary"]
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_p2g_grid_matches_oracle(kind):
+    sc = perturbed(small_scene(kind), seed=11)
+    gpu, orc = make_pair(sc)
+    gpu.step_stage(sc.dt, capi.AEP_STAGE_P2G)
+    g = gpu.get_grid()
+    orc.init(volumes=False)
+    o = orc.get_grid()
+    # node masses: FP32 contributions summed exactly in fixed point -> ~1e-7 relative
+    assert max_rel(g["masses"], o["masses"]) < 2e-6
+    assert abs(g["masses"].sum() - sc.particles.masses.sum()) / sc.particles.masses.sum() < 1e-6
+    # APIC momentum / mass: mass-weighted relative error
+    assert mass_weighted_rel(g["velocities"], o["velocities"], o["masses"]) < 2e-5
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_force_scatter_matches_oracle(kind):
+    sc = perturbed(small_scene(kind), seed=12)
+    gpu, orc = make_pair(sc)
+    gpu.step_stage(sc.dt, capi.AEP_STAGE_FORCES)
+    g = gpu.get_grid()
+    orc.init(volumes=False)
+    orc.step(sc.dt, stage=capi.AEP_STAGE_FORCES)
+    o = orc.get_grid()
+    grav = np.array(list(sc.params.gravity))
+    f_orc = o["forces"] - o["masses"][:, None] * grav  # the GPU reports f without gravity
+    # FP32 SVD + stress relative to the largest nodal force
+    assert max_rel(g["forces"], f_orc) < 2e-4
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_grid_update_collision_matches_oracle(kind):
+    sc = perturbed(small_scene(kind), seed=13)
+    gpu, orc = make_pair(sc)
+    gpu.step_stage(sc.dt, capi.AEP_STAGE_GRID)
+    g = gpu.get_grid()
+    orc.init(volumes=False)
+    orc.step(sc.dt, stage=capi.AEP_STAGE_GRID)
+    o = orc.get_grid()
+    assert mass_weighted_rel(g["velocities"], o["velocities"], o["masses"]) < 1e-4
+    assert mass_weighted_rel(g["velocities_before_friction"], o["velocities_before_friction"], o["masses"]) < 1e-4
+
+
+def _compare_particles(gp, op, pos_tol, vel_tol, F_tol, B_tol, q_tol):
+    assert np.abs(gp["positions"] - op["positions"]).max() < pos_tol
+    assert max_rel(gp["velocities"], op["velocities"]) < vel_tol
+    assert np.abs(gp["elastic_deformation_gradients"] - op["elastic_deformation_gradients"]).max() < F_tol
+    assert max_rel(gp["affine_momenta"], op["affine_momenta"]) < B_tol
+    assert np.abs(gp["plastic"] - op["plastic"]).max() < q_tol
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_one_step_matches_oracle(kind):
+    sc = perturbed(small_scene(kind), seed=14)
+    gpu, orc = make_pair(sc)
+    gpu.step(sc.dt)
+    orc.init(volumes=False)
+    orc.step(sc.dt)
+    _compare_particles(gpu.get_particles(), orc.get_particles(), pos_tol=2e-7, vel_tol=1e-4, F_tol=2e-6,
+                       B_tol=1e-3, q_tol=2e-6)
+
+
+@pytest.mark.parametrize("kind", ["snow", "sand", "mixed"])
+def test_ten_steps_match_oracle(kind):
+    sc = small_scene(kind, seed=3)
+    gpu, orc = make_pair(sc)
+    gpu.init_volumes()
+    orc.init(volumes=True)
+    for _ in range(10):
+        gpu.step(sc.dt)
+        orc.step(sc.dt)
+    _compare_particles(gpu.get_particles(), orc.get_particles(), pos_tol=1e-6, vel_tol=2e-4, F_tol=1e-5,
+                       B_tol=2e-3, q_tol=1e-5)
+
+
+@pytest.mark.parametrize("kind", ["snow", "sand"])
+def test_init_volumes_match_oracle(kind):
+    sc = small_scene(kind)
+    gpu, orc = make_pair(sc)
+    gpu.init_volumes()
+    orc.init(volumes=True)
+    assert max_rel(gpu.get_particles()["volumes"], orc.get_particles()["volumes"]) < 1e-5
+
+
+def test_repeatable_bit_for_bit():
+    sc = perturbed(small_scene("mixed"), seed=21)
+    outs = []
+    for _ in range(2):
+        gpu = HybridSolver(sc.particles, sc.grid, sc.params)
+        gpu.set_level_set(sc.levelset)
+        for _ in range(5):
+            gpu.step(sc.dt)
+        outs.append((gpu.get_particles(), gpu.get_grid()))
+    for k in ("positions", "velocities", "affine_momenta", "elastic_deformation_gradients", "plastic"):
+        assert np.array_equal(outs[0][0][k], outs[1][0][k]), k
+    assert np.array_equal(outs[0][1]["velocities"], outs[1][1]["velocities"])
+
+
+def test_mass_conserved_exactly_over_run():
+    sc = small_scene("sand")
+    gpu = HybridSolver(sc.particles, sc.grid, sc.params)
+    gpu.set_level_set(sc.levelset)
+    gpu.init_volumes()
+    m0 = None
+    for _ in range(30):
+        gpu.step(sc.dt)
+        s = gpu.stats()
+        m0 = s["total_mass"] if m0 is None else m0
+        assert s["total_mass"] == m0  # integer grid sum of the same particle masses
+        assert s["overflow"] == 0
+    assert abs(m0 - sc.particles.masses.sum()) / sc.particles.masses.sum() < 1e-6
+
+
+def test_plastic_F_tracking_matches_oracle():
+    sc = perturbed(small_scene("snow"), seed=15)
+    sc.params.track_plastic_F = 1
+    gpu, orc = make_pair(sc)
+    for _ in range(3):
+        gpu.step(sc.dt)
+    orc.init(volumes=False)
+    for _ in range(3):
+        orc.step(sc.dt)
+    gp = gpu.get_particles(want_fp=True)
+    op = orc.get_particles()
+    assert np.abs(gp["plastic_deformation_gradients"] - op["plastic_deformation_gradients"]).max() < 1e-5
+
+
+def test_invalid_arguments():
+    sc = small_scene("snow")
+    gpu = HybridSolver(None, sc.grid, sc.params)
+    with pytest.raises(AepError):
+        gpu.step(1e-4)  # no particles yet
+    gpu.set_particle_system(sc.particles)
+    with pytest.raises(AepError):
+        gpu.step(-1.0)
+    bad = sc.particles.copy()
+    bad.masses[0] = np.nan
+    with pytest.raises(AepError):
+        gpu.set_particle_system(bad)
+
+
+def test_out_of_domain_particles_are_counted_not_fatal():
+    sc = small_scene("snow")
+    ps = sc.particles.copy()
+    ps.positions[:10] = [1.5, 0.5, 0.5]
+    gpu = HybridSolver(ps, sc.grid, sc.params)
+    gpu.set_level_set(sc.levelset)
+    gpu.step(sc.dt)
+    assert gpu.stats()["out_of_domain"] == 10
+    assert np.all(np.isfinite(gpu.get_particles()["positions"]))
