@@ -50,7 +50,8 @@ struct alignas(16) P2GPrep {
     float b[3];
     float m;
     float Mh[9];
-    float pad0[3];
+    float pad0;
+    long long T;  // the particle's exact fixed-point grid mass (see k_p2g)
     float wx[4], wy[4], wz[4];
     int base[3];
     uint32_t key;
@@ -100,14 +101,30 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
     uint32_t run_key = kInvalidKey;
     int rb[3] = {0, 0, 0};
 
+    // Exact mass: the run's node masses are rounded to fixed point one by one;
+    // their sum S differs from the run's exact fixed-point mass T = sum_p T_p by
+    // the FP32 weight-sum error and the roundings.  The residual T - S is added
+    // to stencil node (1,1,1), which always exists, so the grid mass equals
+    // sum_p T_p exactly and is conserved bit-for-bit from step to step.
+    long long run_T = 0;
     auto flush = [&]() {
         if (run_key == kInvalidKey) return;
+        long long mf[4], S = 0;
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            mf[oz] = __float2ll_rn(am[oz] * P.mass_scale);
+            S += mf[oz];
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) S += __shfl_xor_sync(hmask, S, o, 16);
+        if (l == 5) mf[1] += run_T - S;
+        run_T = 0;
         int x = rb[0] + ox, y = rb[1] + oy;
 #pragma unroll
         for (int oz = 0; oz < 4; ++oz) {
-            if (am[oz] != 0.0f) {
+            if (mf[oz] != 0) {
                 unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + oz);
-                atomicAdd(a + 0, to_fixed(am[oz], P.mass_scale));
+                atomicAdd(a + 0, (unsigned long long)mf[oz]);
                 atomicAdd(a + 1, to_fixed(ax[oz], P.mom_scale));
                 atomicAdd(a + 2, to_fixed(ay[oz], P.mom_scale));
                 atomicAdd(a + 3, to_fixed(az[oz], P.mom_scale));
@@ -128,7 +145,14 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
             int cell[3];
             float f[3], w[3][4], dw[3][4];
             locate(P, xp[0], xp[1], xp[2], cell, f);
-            particle_weights(P, cell, f, w, dw);
+            const bool trunc = particle_weights(P, cell, f, w, dw);
+            // exact fixed-point mass; a stencil cut by the grid boundary keeps only
+            // the weight inside the grid (HS:44-46), as the reference does
+            float wsum = 1.0f;
+            if (trunc)
+                wsum = (w[0][0] + w[0][1] + w[0][2] + w[0][3]) * (w[1][0] + w[1][1] + w[1][2] + w[1][3]) *
+                       (w[2][0] + w[2][1] + w[2][2] + w[2][3]);
+            s.T = __float2ll_rn(m * wsum * P.mass_scale);
             float Bm[9];
 #pragma unroll
             for (int k = 0; k < 9; ++k) Bm[k] = cur.B[k][pj];
@@ -161,6 +185,7 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
                 run_key = s.key;
                 rb[0] = s.base[0]; rb[1] = s.base[1]; rb[2] = s.base[2];
             }
+            run_T += s.T;
             const float wxy = s.wx[ox] * s.wy[oy];
             const float fx = (float)ox, fy = (float)oy;
             float tx = s.b[0] + s.Mh[0] * fx + s.Mh[1] * fy;

