@@ -20,10 +20,12 @@ AEP_OUT_OF_DOMAIN = 4
 AEP_NOT_READY = 5
 AEP_OUT_OF_MEMORY = 6
 AEP_NO_DEVICE = 7
+AEP_CAPACITY = 8
 STATUS_NAMES = {
     0: "AEP_OK", 1: "AEP_INVALID_ARG", 2: "AEP_CUDA_ERROR", 3: "AEP_OVERFLOW", 4: "AEP_OUT_OF_DOMAIN",
-    5: "AEP_NOT_READY", 6: "AEP_OUT_OF_MEMORY", 7: "AEP_NO_DEVICE",
+    5: "AEP_NOT_READY", 6: "AEP_OUT_OF_MEMORY", 7: "AEP_NO_DEVICE", 8: "AEP_CAPACITY",
 }
+AEP_NOALLOC_MAX_NODES = 373248
 
 AEP_SNOW = 0
 AEP_SAND = 1
@@ -108,6 +110,8 @@ SIGNATURES = {
     "aep_set_stream": (C.c_int, [_solver_p, C.c_void_p]),
     "aep_set_profiling": (C.c_int, [_solver_p, C.c_int32]),
     "aep_get_phase_times": (C.c_int, [_solver_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "aep_p2g_noalloc": (C.c_int, [C.POINTER(aep_grid_desc), C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
     "aep_last_error": (C.c_char_p, [_solver_p]),
 }
 

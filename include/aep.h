@@ -44,7 +44,8 @@ typedef enum aep_status {
     AEP_OUT_OF_DOMAIN = 4,   /* reserved: particles are clamped and counted       */
     AEP_NOT_READY = 5,       /* call order violated (e.g. step before particles)  */
     AEP_OUT_OF_MEMORY = 6,   /* device allocation failed                          */
-    AEP_NO_DEVICE = 7        /* no CUDA device visible                            */
+    AEP_NO_DEVICE = 7,       /* no CUDA device visible                            */
+    AEP_CAPACITY = 8         /* request exceeds the fixed scratch of aep_p2g_noalloc */
 } aep_status;
 
 /* Particle material tags (the reference hard-codes one MaterialType for the
@@ -234,6 +235,37 @@ aep_status aep_set_profiling(aep_solver* s, int32_t on);
 /* Accumulated milliseconds per phase since profiling was enabled, and the
  * number of timed steps.  Synchronises the handle's stream.                  */
 aep_status aep_get_phase_times(aep_solver* s, double ms[AEP_NUM_PHASES], int64_t* steps);
+
+/* ---- particle-to-grid without allocation --------------------------------------------- */
+
+/* No counterpart in the reference.  For callers that must not allocate GPU memory:
+ * code running inside a host application that owns all device memory through its
+ * own pool, code running while a CUDA graph is being captured, or real-time loops
+ * that cannot afford the synchronisation of cudaMalloc/cudaFree.  It performs the
+ * step's particle-to-grid transfer (mass and APIC momentum, then v = p / m) from
+ * the caller's device arrays into the caller's device output arrays, and allocates
+ * nothing: its only working memory is a fixed array compiled into the library
+ * (AEP_NOALLOC_MAX_NODES * 32 bytes, about 12 MB, held on every GPU that loads the
+ * library until the process exits).
+ *
+ * Inputs (device pointers, FP32, the C-ABI layouts above): x, v are N x 3
+ * column-major; B is 9N (affineMomenta_1 | _2 | _3); m is N.  mass_ref > 0 sets the
+ * fixed-point unit and should be the largest particle mass.  Outputs (device
+ * pointers, FP32, reference node order): mass_out (Ng), vel_out (Ng x 3
+ * column-major); nodes without mass get 0.  Work is queued on cuda_stream (NULL =
+ * the default stream) and the call returns without waiting.
+ *
+ * Limits: the padded grid, ((res+2)/4 + 2)^3 * 64 nodes, must not exceed
+ * AEP_NOALLOC_MAX_NODES (a 64^3 grid fits); larger grids return AEP_CAPACITY.
+ * The first call on a device looks up the device address of the fixed array
+ * (cudaGetSymbolAddress); make that first call before any stream capture begins.
+ * Every call shares the one array and clears the part it uses at its start, so
+ * calls that can overlap on the GPU (different streams, or different host
+ * threads) race and must be serialised by the caller.                          */
+#define AEP_NOALLOC_MAX_NODES 373248
+aep_status aep_p2g_noalloc(const aep_grid_desc* grid, int64_t n,
+                           const float* x, const float* v, const float* B, const float* m,
+                           double mass_ref, float* mass_out, float* vel_out, void* cuda_stream);
 
 /* Human-readable text of the last error on this handle (static storage). */
 const char* aep_last_error(aep_solver* s);
