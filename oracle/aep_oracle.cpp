@@ -683,6 +683,32 @@ void g2p_set(Oracle& o, const Weights& W, std::vector<V3>& x, std::vector<V3>& v
     }
 }
 
+// singular-value return mapping, HybridSolver.cpp:626-674 (snow clamp, sand
+// Drucker-Prager projection with hardening of the plastic amount q)
+void return_map(const aep_params& P, int mat, V3& S, double& q) {
+    if (mat == AEP_SNOW) {
+        for (int a = 0; a < 3; ++a) S[a] = std::min(std::max(S[a], 1.0 - P.snow.theta_c), 1.0 + P.snow.theta_s);
+        return;
+    }
+    double lambda, mu;
+    lame(P.sand.E, P.sand.nu, lambda, mu);
+    double phiF = (P.sand.h0 + (P.sand.h1 * q - P.sand.h3) * std::exp(-P.sand.h2 * q)) * kPi / 180.0;
+    double alpha = std::sqrt(2.0 / 3.0) * 2.0 * std::sin(phiF) / (3.0 - std::sin(phiF));
+    V3 ln{std::log(S[0]), std::log(S[1]), std::log(S[2])};
+    double tr = ln[0] + ln[1] + ln[2];
+    V3 dev{ln[0] - tr / 3.0, ln[1] - tr / 3.0, ln[2] - tr / 3.0};
+    double nd = norm(dev);
+    double dg = nd + (3.0 * lambda + 2.0 * mu) / 2.0 / mu * tr * alpha;
+    if (dg <= 0.0) {
+    } else if (nd == 0.0 || tr > 0.0) {
+        S = V3{1, 1, 1};
+        q += norm(ln);
+    } else {
+        for (int a = 0; a < 3; ++a) S[a] = std::exp(ln[a] - dg * dev[a] / nd);
+        q += dg;
+    }
+}
+
 // HybridSolver.cpp:553-609 + :612-723 for the particles; fused per particle
 void plasticity_particles(Oracle& o, double dt) {
     const aep_params& P = o.prm;
@@ -696,28 +722,7 @@ void plasticity_particles(Oracle& o, double dt) {
         M3 U, V;
         V3 S;
         svd3(Ftr, U, S, V);
-        if (o.mat[p] == AEP_SNOW) {
-            for (int a = 0; a < 3; ++a) S[a] = std::min(std::max(S[a], 1.0 - P.snow.theta_c), 1.0 + P.snow.theta_s);
-        } else {
-            double lambda, mu;
-            lame(P.sand.E, P.sand.nu, lambda, mu);
-            double q = o.plastic[p];
-            double phiF = (P.sand.h0 + (P.sand.h1 * q - P.sand.h3) * std::exp(-P.sand.h2 * q)) * kPi / 180.0;
-            double alpha = std::sqrt(2.0 / 3.0) * 2.0 * std::sin(phiF) / (3.0 - std::sin(phiF));
-            V3 ln{std::log(S[0]), std::log(S[1]), std::log(S[2])};
-            double tr = ln[0] + ln[1] + ln[2];
-            V3 dev{ln[0] - tr / 3.0, ln[1] - tr / 3.0, ln[2] - tr / 3.0};
-            double nd = norm(dev);
-            double dg = nd + (3.0 * lambda + 2.0 * mu) / 2.0 / mu * tr * alpha;
-            if (dg <= 0.0) {
-            } else if (nd == 0.0 || tr > 0.0) {
-                S = V3{1, 1, 1};
-                o.plastic[p] += norm(ln);
-            } else {
-                for (int a = 0; a < 3; ++a) S[a] = std::exp(ln[a] - dg * dev[a] / nd);
-                o.plastic[p] += dg;
-            }
-        }
+        return_map(P, o.mat[p], S, o.plastic[p]);
         M3 Ds{}, Dinv{};
         for (int a = 0; a < 3; ++a) { E(Ds, a, a) = S[a]; E(Dinv, a, a) = 1.0 / S[a]; }
         M3 Ftot = mul(Ftr, o.Fp[p]);  // totalDeformationGradient, :618-619
@@ -1005,6 +1010,12 @@ void orc_svd3(const double* A, double* U, double* s, double* V) {
     svd3(a, u, sv, v);
     for (int k = 0; k < 9; ++k) { U[k] = u[k]; V[k] = v[k]; }
     for (int k = 0; k < 3; ++k) s[k] = sv[k];
+}
+// singular-value return map of one particle (mat: AEP_SNOW / AEP_SAND); s in/out, q in/out
+void orc_return_map(const aep_params* prm, int mat, double* s, double* q) {
+    V3 S{s[0], s[1], s[2]};
+    return_map(*prm, mat, S, *q);
+    for (int a = 0; a < 3; ++a) s[a] = S[a];
 }
 double orc_cubic(double x) { return cubic_B_spline(x); }
 double orc_dcubic(double x) { return Dcubic_B_spline(x); }

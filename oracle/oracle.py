@@ -43,6 +43,7 @@ def load() -> C.CDLL:
         lib.orc_get_grid.argtypes = [vp] + [_dp] * 4
         lib.orc_get_stress.argtypes = [vp, C.c_int64, _dp]
         lib.orc_svd3.argtypes = [_dp, _dp, _dp, _dp]
+        lib.orc_return_map.argtypes = [C.POINTER(capi.aep_params), C.c_int, _dp, _dp]
         lib.orc_cubic.restype = C.c_double
         lib.orc_cubic.argtypes = [C.c_double]
         lib.orc_dcubic.restype = C.c_double
@@ -131,6 +132,25 @@ def svd3(A: np.ndarray):
     U, s, V = np.empty(9), np.empty(3), np.empty(9)
     lib.orc_svd3(_p(a), _p(U), _p(s), _p(V))
     return U.reshape(3, 3).T, s, V.reshape(3, 3).T
+
+
+def return_map(params, mat: int, s, q: float):
+    """Singular-value return mapping of one particle (HybridSolver.cpp:626-674)."""
+    sv = np.ascontiguousarray(np.asarray(s, float).copy())
+    qq = C.c_double(q)
+    load().orc_return_map(C.byref(params), int(mat), _p(sv), C.byref(qq))
+    return sv, qq.value
+
+
+def particle_weights(grid, params, pos):
+    """Weights of one particle: (node ids, w, grad w) as built at HybridSolver.cpp:30-79."""
+    orc = Oracle(grid, params)
+    node = np.zeros(125, np.int64)
+    w = np.zeros(125)
+    g = np.zeros(375)
+    p = np.ascontiguousarray(np.asarray(pos, float))
+    c = orc.lib.orc_particle_weights(orc.h, _p(p), node.ctypes.data_as(C.POINTER(C.c_int64)), _p(w), _p(g))
+    return node[:c], w[:c], g[:3 * c].reshape(c, 3)
 
 
 def cubic(x: float) -> float:
