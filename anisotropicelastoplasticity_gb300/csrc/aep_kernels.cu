@@ -46,18 +46,15 @@ __global__ void k_keys(KParams P, PArrays cur, int n, uint32_t* keys, DevStats* 
 // Mh[:,a] = m D^-1 h_a B[:,a] and b = m v - Mh (1 + f).
 constexpr int kP2GThreads = 128;
 constexpr int kP2GChunk = 64;  // particles per half-warp
-struct alignas(16) P2GPrep {
-    float b[3];
-    float m;
-    float Mh[9];
-    float pad0;
-    long long T;  // the particle's exact fixed-point grid mass (see k_p2g)
-    float wx[4], wy[4], wz[4];
-    int base[3];
-    uint32_t key;
-};
-static_assert(sizeof(P2GPrep) == 128, "prep layout");
-
+// Prep record of one particle, 9 float4 (36 words, 16-byte aligned):
+//   q0 = (b, m)  q1 = Mh[0..3]  q2 = Mh[4..7]  q3 = (Mh[8], T lo, T hi, -)
+//   q4 = wx  q5 = wy  q6 = wz  q7 = (base, key)
+// A lane writes its own record with 128-bit stores; a stride of 36 words puts
+// the 8 lanes of each store wavefront on distinct banks.  Each half-warp's 16
+// records are skewed by one float4 so the two halves of a warp reading the
+// same slot do not collide either.
+constexpr int kP2GRec = 9;
+constexpr int kP2GRegion = 16 * kP2GRec + 1;  // float4 per half-warp region
 __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, uint32_t key) {
     uint32_t blk = key >> 6;
     int bx = (int)(blk % (uint32_t)P.nb[0]);
@@ -89,8 +86,9 @@ __device__ __forceinline__ unsigned run_heads(unsigned hmask, int l, uint32_t ke
 
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                      const int32_t* __restrict__ perm, int n, GArrays G) {
-    __shared__ P2GPrep sm[kP2GThreads / 16][16];
+    __shared__ float4 sm4[(kP2GThreads / 16) * kP2GRegion];
     const int hw = threadIdx.x >> 4, l = threadIdx.x & 15;
+    float4* const region = sm4 + hw * kP2GRegion;
     const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
     const int ox = l & 3, oy = l >> 2;
     const long chunk0 = ((long)blockIdx.x * (kP2GThreads / 16) + hw) * kP2GChunk;
@@ -135,8 +133,8 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
 
     for (int b0 = 0; b0 < cnt_total; b0 += 16) {
         const long j = chunk0 + b0 + l;
+        uint32_t my_key = kInvalidKey;
         if (b0 + l < cnt_total) {
-            P2GPrep& s = sm[hw][l];
             const uint32_t key = keys[j];
             if (j == 0 || (keys[j - 1] >> 6) != (key >> 6)) mark_blocks(P, G, key);
             const int pj = perm[j];
@@ -152,55 +150,66 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
             if (trunc)
                 wsum = (w[0][0] + w[0][1] + w[0][2] + w[0][3]) * (w[1][0] + w[1][1] + w[1][2] + w[1][3]) *
                        (w[2][0] + w[2][1] + w[2][2] + w[2][3]);
-            s.T = __float2ll_rn(m * wsum * P.mass_scale);
-            float Bm[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) Bm[k] = cur.B[k][pj];
+            const long long T = __float2ll_rn(m * wsum * P.mass_scale);
+            float Mh[9], b[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                float vma = m * cur.v[a][pj];
-                float t = vma;
+                float t = m * cur.v[a][pj];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    float mh = m * P.apic[c] * Bm[3 * a + c];
-                    s.Mh[3 * a + c] = mh;
+                    const float mh = m * P.apic[c] * cur.B[3 * a + c][pj];
+                    Mh[3 * a + c] = mh;
                     t -= mh * (1.0f + f[c]);
                 }
-                s.b[a] = t;
+                b[a] = t;
             }
-            s.m = m;
-#pragma unroll
-            for (int o = 0; o < 4; ++o) { s.wx[o] = w[0][o]; s.wy[o] = w[1][o]; s.wz[o] = w[2][o]; }
-#pragma unroll
-            for (int a = 0; a < 3; ++a) s.base[a] = cell[a] + 3;
-            s.key = key;
+            float4* r = region + l * kP2GRec;
+            r[0] = make_float4(b[0], b[1], b[2], m);
+            r[1] = make_float4(Mh[0], Mh[1], Mh[2], Mh[3]);
+            r[2] = make_float4(Mh[4], Mh[5], Mh[6], Mh[7]);
+            r[3] = make_float4(Mh[8], __int_as_float((int)(unsigned)(T & 0xffffffffll)), __int_as_float((int)(T >> 32)),
+                               0.0f);
+            r[4] = make_float4(w[0][0], w[0][1], w[0][2], w[0][3]);
+            r[5] = make_float4(w[1][0], w[1][1], w[1][2], w[1][3]);
+            r[6] = make_float4(w[2][0], w[2][1], w[2][2], w[2][3]);
+            r[7] = make_float4(__int_as_float(cell[0] + 3), __int_as_float(cell[1] + 3), __int_as_float(cell[2] + 3),
+                               __uint_as_float(key));
+            my_key = key;
         }
         __syncwarp(hmask);
         const int cnt = min(16, cnt_total - b0);
-        const unsigned heads = run_heads(hmask, l, b0 + l < cnt_total ? sm[hw][l].key : kInvalidKey, run_key);
+        const unsigned heads = run_heads(hmask, l, my_key, run_key);
         for (int t = 0; t < cnt; ++t) {
-            const P2GPrep& s = sm[hw][t];
+            const float4* r = region + t * kP2GRec;
             if ((heads >> t) & 1u) {
                 flush();
-                run_key = s.key;
-                rb[0] = s.base[0]; rb[1] = s.base[1]; rb[2] = s.base[2];
+                const float4 q7 = r[7];
+                run_key = __float_as_uint(q7.w);
+                rb[0] = __float_as_int(q7.x); rb[1] = __float_as_int(q7.y); rb[2] = __float_as_int(q7.z);
             }
-            run_T += s.T;
-            const float wxy = s.wx[ox] * s.wy[oy];
+            const float4 q0 = r[0], q1 = r[1], q2 = r[2], q3 = r[3], q6 = r[6];
+            const float wxo = reinterpret_cast<const float*>(r + 4)[ox];
+            const float wyo = reinterpret_cast<const float*>(r + 5)[oy];
+            run_T += (long long)(((unsigned long long)(unsigned)__float_as_int(q3.z) << 32) |
+                                 (unsigned long long)(unsigned)__float_as_int(q3.y));
+            const float wxy = wxo * wyo;
             const float fx = (float)ox, fy = (float)oy;
-            float tx = s.b[0] + s.Mh[0] * fx + s.Mh[1] * fy;
-            float ty = s.b[1] + s.Mh[3] * fx + s.Mh[4] * fy;
-            float tz = s.b[2] + s.Mh[6] * fx + s.Mh[7] * fy;
+            // Mh row-major: row a = (Mh[3a], Mh[3a+1], Mh[3a+2])
+            float tx = q0.x + q1.x * fx + q1.y * fy;
+            float ty = q0.y + q1.w * fx + q2.x * fy;
+            float tz = q0.z + q2.z * fx + q2.w * fy;
+            const float mz0 = q1.z, mz1 = q2.y, mz2 = q3.x;
+            const float wz4[4] = {q6.x, q6.y, q6.z, q6.w};
 #pragma unroll
             for (int oz = 0; oz < 4; ++oz) {
-                const float w = wxy * s.wz[oz];
-                am[oz] = fmaf(w, s.m, am[oz]);
+                const float w = wxy * wz4[oz];
+                am[oz] = fmaf(w, q0.w, am[oz]);
                 ax[oz] = fmaf(w, tx, ax[oz]);
                 ay[oz] = fmaf(w, ty, ay[oz]);
                 az[oz] = fmaf(w, tz, az[oz]);
-                tx += s.Mh[2];
-                ty += s.Mh[5];
-                tz += s.Mh[8];
+                tx += mz0;
+                ty += mz1;
+                tz += mz2;
             }
         }
         __syncwarp(hmask);
@@ -290,15 +299,14 @@ __device__ __forceinline__ void stress_from_svd(const KParams& P, int mat, const
 }
 
 constexpr int kFrcThreads = 128;
-struct alignas(16) FrcPrep {
-    float S[9];       // -dt * vol * P * F^T
-    float pad0[3];
-    float wx[4], wy[4], wz[4];
-    float dwx[4], dwy[4], dwz[4];
-    int base[3];
-    uint32_t key;
-};
-static_assert(sizeof(FrcPrep) == 160, "prep layout");
+// Force prep record of one particle, 11 float4 (44 words):
+//   q0..q2 = S[0..8] (-dt vol P F^T, row-major) + pad   q3 = wx  q4 = wy  q5 = wz
+//   q6 = dwx  q7 = dwy  q8 = dwz  q9 = (base, key)  q10 unused
+// 44-word stride: conflict-free 128-bit stores; the second half-warp's records are
+// skewed by one float4 so both halves reading slot i hit different banks.
+constexpr int kFrcRec = 11;
+constexpr int kFrcWarpBuf = 32 * kFrcRec + 1;
+__device__ __forceinline__ int frc_slot(int p) { return p * kFrcRec + (p >= 16 ? 1 : 0); }
 
 __device__ void particle_stress_impulse(const KParams& P, const GArrays& G, const PArrays& cur, int pj, float dt_force,
                                         float S[9], float w[3][4], float dw[3][4], int cell[3], DevStats* st) {
@@ -308,22 +316,40 @@ __device__ void particle_stress_impulse(const KParams& P, const GArrays& G, cons
     int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
     uint32_t X[4], Y[4], Z[4];
     stencil_offsets(P, base, X, Y, Z);
-    // velocity gradient of the P2G velocity (the three SpMVs of HS:269-271)
+    // velocity gradient of the P2G velocity (the three SpMVs of HS:269-271),
+    // contracted one axis at a time: Gm = sum v (grad w)^T with
+    // grad w = (dwx wy wz, wx dwy wz, wx wy dwz)
     float Gm[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-    for (int oz = 0; oz < 4; ++oz)
+    for (int oy = 0; oy < 4; ++oy) {
+        float Bd[3] = {0, 0, 0}, Bw[3] = {0, 0, 0}, Bz[3] = {0, 0, 0};
 #pragma unroll
-        for (int oy = 0; oy < 4; ++oy) {
-            const float wyz = w[1][oy] * w[2][oz], dyz = dw[1][oy] * w[2][oz], ydz = w[1][oy] * dw[2][oz];
+        for (int oz = 0; oz < 4; ++oz) {
+            const uint32_t yz = Y[oy] + Z[oz];
+            float Ad[3] = {0, 0, 0}, Aw[3] = {0, 0, 0};
 #pragma unroll
             for (int ox = 0; ox < 4; ++ox) {
-                float4 v = __ldg(&G.vel[X[ox] + Y[oy] + Z[oz]]);
-                float g0 = dw[0][ox] * wyz, g1 = w[0][ox] * dyz, g2 = w[0][ox] * ydz;
-                Gm[0] += v.x * g0; Gm[1] += v.x * g1; Gm[2] += v.x * g2;
-                Gm[3] += v.y * g0; Gm[4] += v.y * g1; Gm[5] += v.y * g2;
-                Gm[6] += v.z * g0; Gm[7] += v.z * g1; Gm[8] += v.z * g2;
+                const float4 v = __ldg(&G.vel[yz + X[ox]]);
+                const float a = w[0][ox], d = dw[0][ox];
+                Ad[0] = fmaf(d, v.x, Ad[0]); Ad[1] = fmaf(d, v.y, Ad[1]); Ad[2] = fmaf(d, v.z, Ad[2]);
+                Aw[0] = fmaf(a, v.x, Aw[0]); Aw[1] = fmaf(a, v.y, Aw[1]); Aw[2] = fmaf(a, v.z, Aw[2]);
+            }
+            const float cz = w[2][oz], dz = dw[2][oz];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                Bd[c] = fmaf(cz, Ad[c], Bd[c]);
+                Bw[c] = fmaf(cz, Aw[c], Bw[c]);
+                Bz[c] = fmaf(dz, Aw[c], Bz[c]);
             }
         }
+        const float cy = w[1][oy], dy = dw[1][oy];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            Gm[3 * c + 0] = fmaf(cy, Bd[c], Gm[3 * c + 0]);
+            Gm[3 * c + 1] = fmaf(dy, Bw[c], Gm[3 * c + 1]);
+            Gm[3 * c + 2] = fmaf(cy, Bz[c], Gm[3 * c + 2]);
+        }
+    }
     float F[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
@@ -365,37 +391,40 @@ __device__ void particle_stress_impulse(const KParams& P, const GArrays& G, cons
 }
 
 // impulse scatter: f_i -= sum_p stress_p grad w_ip (HS:356-366), stored as dt * f_i
-__global__ void __launch_bounds__(kFrcThreads) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                        const int32_t* __restrict__ perm, int n, GArrays G,
                                                        float dt_force, DevStats* st) {
-    __shared__ FrcPrep sm[kFrcThreads / 32][32];
+    __shared__ float4 sm4[(kFrcThreads / 32) * kFrcWarpBuf];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* const buf = sm4 + wid * kFrcWarpBuf;
     const long chunk0 = ((long)blockIdx.x * (kFrcThreads / 32) + wid) * 32;
     if (chunk0 >= n) return;
     const long j = chunk0 + lane;
-    {
-        FrcPrep& s = sm[wid][lane];
-        if (j < n) {
-            const int pj = perm[j];
-            float w[3][4], dw[3][4];
-            int cell[3];
-            particle_stress_impulse(P, G, cur, pj, dt_force, s.S, w, dw, cell, st);
-#pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                s.wx[o] = w[0][o]; s.wy[o] = w[1][o]; s.wz[o] = w[2][o];
-                s.dwx[o] = dw[0][o]; s.dwy[o] = dw[1][o]; s.dwz[o] = dw[2][o];
-            }
-#pragma unroll
-            for (int a = 0; a < 3; ++a) s.base[a] = cell[a] + 3;
-            s.key = keys[j];
-        } else {
-            s.key = kInvalidKey;
-        }
+    uint32_t my_key = kInvalidKey;
+    if (j < n) {
+        const int pj = perm[j];
+        float w[3][4], dw[3][4], S[9];
+        int cell[3];
+        particle_stress_impulse(P, G, cur, pj, dt_force, S, w, dw, cell, st);
+        float4* r = buf + frc_slot(lane);
+        r[0] = make_float4(S[0], S[1], S[2], S[3]);
+        r[1] = make_float4(S[4], S[5], S[6], S[7]);
+        r[2] = make_float4(S[8], 0.f, 0.f, 0.f);
+        r[3] = make_float4(w[0][0], w[0][1], w[0][2], w[0][3]);
+        r[4] = make_float4(w[1][0], w[1][1], w[1][2], w[1][3]);
+        r[5] = make_float4(w[2][0], w[2][1], w[2][2], w[2][3]);
+        r[6] = make_float4(dw[0][0], dw[0][1], dw[0][2], dw[0][3]);
+        r[7] = make_float4(dw[1][0], dw[1][1], dw[1][2], dw[1][3]);
+        r[8] = make_float4(dw[2][0], dw[2][1], dw[2][2], dw[2][3]);
+        my_key = keys[j];
+        r[9] = make_float4(__int_as_float(cell[0] + 3), __int_as_float(cell[1] + 3), __int_as_float(cell[2] + 3),
+                           __uint_as_float(my_key));
     }
     __syncwarp();
     // stream: half h takes particles [16h, 16h+16)
     const int h = lane >> 4, l = lane & 15, ox = l & 3, oy = l >> 2;
     const unsigned hmask = 0xFFFFu << (lane & 16);
+    const int cnt = (int)max(0l, min(16l, (long)n - (chunk0 + 16 * h)));
     float fx[4] = {0, 0, 0, 0}, fy[4] = {0, 0, 0, 0}, fz[4] = {0, 0, 0, 0};
     uint32_t run_key = kInvalidKey;
     int rb[3] = {0, 0, 0};
@@ -413,25 +442,31 @@ __global__ void __launch_bounds__(kFrcThreads) k_force(KParams P, PArrays cur, c
             fx[oz] = fy[oz] = fz[oz] = 0.0f;
         }
     };
-    const unsigned heads = run_heads(hmask, l, sm[wid][16 * h + l].key, kInvalidKey);
-    for (int t = 16 * h; t < 16 * h + 16; ++t) {
-        const FrcPrep& s = sm[wid][t];
-        if (s.key == kInvalidKey) break;
-        if ((heads >> (t - 16 * h)) & 1u) {
+    const unsigned heads = run_heads(hmask, l, my_key, kInvalidKey);
+    for (int i = 0; i < cnt; ++i) {
+        const float4* r = buf + frc_slot(16 * h + i);
+        if ((heads >> i) & 1u) {
             flush();
-            run_key = s.key;
-            rb[0] = s.base[0]; rb[1] = s.base[1]; rb[2] = s.base[2];
+            const float4 q9 = r[9];
+            run_key = __float_as_uint(q9.w);
+            rb[0] = __float_as_int(q9.x); rb[1] = __float_as_int(q9.y); rb[2] = __float_as_int(q9.z);
         }
-        // grad w = (dwx wy wz, wx dwy wz, wx wy dwz); S g = wz (p1 S0 + p2 S1) + dwz p3 S2
-        const float p1 = s.dwx[ox] * s.wy[oy], p2 = s.wx[ox] * s.dwy[oy], p3 = s.wx[ox] * s.wy[oy];
-        const float ax_ = p1 * s.S[0] + p2 * s.S[1], ay_ = p1 * s.S[3] + p2 * s.S[4], az_ = p1 * s.S[6] + p2 * s.S[7];
-        const float cx = p3 * s.S[2], cy = p3 * s.S[5], cz = p3 * s.S[8];
+        const float4 q0 = r[0], q1 = r[1], q2 = r[2], q5 = r[5], q8 = r[8];
+        const float wxo = reinterpret_cast<const float*>(r + 3)[ox];
+        const float wyo = reinterpret_cast<const float*>(r + 4)[oy];
+        const float dxo = reinterpret_cast<const float*>(r + 6)[ox];
+        const float dyo = reinterpret_cast<const float*>(r + 7)[oy];
+        // grad w = (dwx wy wz, wx dwy wz, wx wy dwz); S g = wz (p1 S[:,0] + p2 S[:,1]) + dwz p3 S[:,2]
+        // S row-major: S[3a+b] -> q0=(S0,S1,S2,S3) q1=(S4,S5,S6,S7) q2.x=S8
+        const float p1 = dxo * wyo, p2 = wxo * dyo, p3 = wxo * wyo;
+        const float ax_ = p1 * q0.x + p2 * q0.y, ay_ = p1 * q0.w + p2 * q1.x, az_ = p1 * q1.z + p2 * q1.w;
+        const float cx = p3 * q0.z, cy = p3 * q1.y, cz = p3 * q2.x;
+        const float wz4[4] = {q5.x, q5.y, q5.z, q5.w}, dz4[4] = {q8.x, q8.y, q8.z, q8.w};
 #pragma unroll
         for (int oz = 0; oz < 4; ++oz) {
-            const float wz = s.wz[oz], dz = s.dwz[oz];
-            fx[oz] = fmaf(wz, ax_, fmaf(dz, cx, fx[oz]));
-            fy[oz] = fmaf(wz, ay_, fmaf(dz, cy, fy[oz]));
-            fz[oz] = fmaf(wz, az_, fmaf(dz, cz, fz[oz]));
+            fx[oz] = fmaf(wz4[oz], ax_, fmaf(dz4[oz], cx, fx[oz]));
+            fy[oz] = fmaf(wz4[oz], ay_, fmaf(dz4[oz], cy, fy[oz]));
+            fz[oz] = fmaf(wz4[oz], az_, fmaf(dz4[oz], cz, fz[oz]));
         }
     }
     flush();
@@ -560,32 +595,58 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
 #pragma unroll
         for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
 
+    // Gather of v (G2P velocity + APIC) and v^bf (advection + velocity gradient)
+    // over the 4x4x4 stencil, contracted one axis at a time because the weights
+    // are tensor products: x first (A), then z (Bq), then y.
+    //   A0 = sum_x wx v      A1 = sum_x wx xi_x v   A2 = sum_x dwx vbf   A3 = sum_x wx vbf
+    //   vp = sum w v,  C = sum w v xi^T,  xs = sum w vbf,  Gb = sum vbf (grad w)^T
     float vp[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
     float C[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Gb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float wxi[4];
 #pragma unroll
-    for (int oz = 0; oz < 4; ++oz)
+    for (int o = 0; o < 4; ++o) wxi[o] = w[0][o] * xi[0][o];
 #pragma unroll
-        for (int oy = 0; oy < 4; ++oy) {
-            const float wyz = w[1][oy] * w[2][oz], dyz = dw[1][oy] * w[2][oz], ydz = w[1][oy] * dw[2][oz];
+    for (int oy = 0; oy < 4; ++oy) {
+        float B0[3] = {0, 0, 0}, B1[3] = {0, 0, 0}, B2[3] = {0, 0, 0};
+        float B3[3] = {0, 0, 0}, B4[3] = {0, 0, 0}, B5[3] = {0, 0, 0};
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            const uint32_t yz = Y[oy] + Z[oz];
+            float A0[3] = {0, 0, 0}, A1[3] = {0, 0, 0}, A2[3] = {0, 0, 0}, A3[3] = {0, 0, 0};
 #pragma unroll
             for (int ox = 0; ox < 4; ++ox) {
-                const uint32_t idx = X[ox] + Y[oy] + Z[oz];
-                const float4 v = __ldg(&G.vel[idx]);
-                const float4 b = __ldg(&G.vbf[idx]);
-                const float wt = w[0][ox] * wyz;
-                const float g0 = dw[0][ox] * wyz, g1 = w[0][ox] * dyz, g2 = w[0][ox] * ydz;
-                const float wvx = wt * v.x, wvy = wt * v.y, wvz = wt * v.z;
-                vp[0] += wvx; vp[1] += wvy; vp[2] += wvz;
-                const float e0 = xi[0][ox], e1 = xi[1][oy], e2 = xi[2][oz];
-                C[0] += wvx * e0; C[1] += wvx * e1; C[2] += wvx * e2;
-                C[3] += wvy * e0; C[4] += wvy * e1; C[5] += wvy * e2;
-                C[6] += wvz * e0; C[7] += wvz * e1; C[8] += wvz * e2;
-                xs[0] += wt * b.x; xs[1] += wt * b.y; xs[2] += wt * b.z;
-                Gb[0] += b.x * g0; Gb[1] += b.x * g1; Gb[2] += b.x * g2;
-                Gb[3] += b.y * g0; Gb[4] += b.y * g1; Gb[5] += b.y * g2;
-                Gb[6] += b.z * g0; Gb[7] += b.z * g1; Gb[8] += b.z * g2;
+                const float4 v = __ldg(&G.vel[yz + X[ox]]);
+                const float4 b = __ldg(&G.vbf[yz + X[ox]]);
+                const float a = w[0][ox], ax_ = wxi[ox], d = dw[0][ox];
+                A0[0] = fmaf(a, v.x, A0[0]); A0[1] = fmaf(a, v.y, A0[1]); A0[2] = fmaf(a, v.z, A0[2]);
+                A1[0] = fmaf(ax_, v.x, A1[0]); A1[1] = fmaf(ax_, v.y, A1[1]); A1[2] = fmaf(ax_, v.z, A1[2]);
+                A2[0] = fmaf(d, b.x, A2[0]); A2[1] = fmaf(d, b.y, A2[1]); A2[2] = fmaf(d, b.z, A2[2]);
+                A3[0] = fmaf(a, b.x, A3[0]); A3[1] = fmaf(a, b.y, A3[1]); A3[2] = fmaf(a, b.z, A3[2]);
+            }
+            const float cz = w[2][oz], czx = w[2][oz] * xi[2][oz], dz = dw[2][oz];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                B0[c] = fmaf(cz, A0[c], B0[c]);
+                B1[c] = fmaf(cz, A1[c], B1[c]);
+                B2[c] = fmaf(czx, A0[c], B2[c]);
+                B3[c] = fmaf(cz, A2[c], B3[c]);
+                B4[c] = fmaf(cz, A3[c], B4[c]);
+                B5[c] = fmaf(dz, A3[c], B5[c]);
             }
         }
+        const float cy = w[1][oy], cyx = w[1][oy] * xi[1][oy], dy = dw[1][oy];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            vp[c] = fmaf(cy, B0[c], vp[c]);
+            C[3 * c + 0] = fmaf(cy, B1[c], C[3 * c + 0]);
+            C[3 * c + 1] = fmaf(cyx, B0[c], C[3 * c + 1]);
+            C[3 * c + 2] = fmaf(cy, B2[c], C[3 * c + 2]);
+            xs[c] = fmaf(cy, B4[c], xs[c]);
+            Gb[3 * c + 0] = fmaf(cy, B3[c], Gb[3 * c + 0]);
+            Gb[3 * c + 1] = fmaf(dy, B4[c], Gb[3 * c + 1]);
+            Gb[3 * c + 2] = fmaf(cy, B5[c], Gb[3 * c + 2]);
+        }
+    }
     // advection x = sum w (x_i + dt v^bf_i) (HS:944): exact linear reproduction for a
     // full stencil; a stencil cut by the grid boundary keeps its lost weight.
     float xn[3];
