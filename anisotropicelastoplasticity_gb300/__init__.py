@@ -7,7 +7,7 @@ this package is its host-side binding and the reference-shaped classes.
 """
 from . import capi, scenes
 from .capi import AepError
-from .solver import HybridSolver, LevelSet, ParticleSystem, RegularGrid, make_params
+from .solver import HybridSolver, LagrangianMesh, LevelSet, ParticleSystem, RegularGrid, make_params
 
-__all__ = ["capi", "scenes", "AepError", "HybridSolver", "LevelSet", "ParticleSystem", "RegularGrid",
-           "make_params"]
+__all__ = ["capi", "scenes", "AepError", "HybridSolver", "LagrangianMesh", "LevelSet", "ParticleSystem",
+           "RegularGrid", "make_params"]

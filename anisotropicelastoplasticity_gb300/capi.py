@@ -29,6 +29,8 @@ AEP_NOALLOC_MAX_NODES = 373248
 
 AEP_SNOW = 0
 AEP_SAND = 1
+AEP_CLOTH_VERTEX = 2
+AEP_CLOTH_ELEMENT = 3
 
 AEP_SDF_PLANE = 0
 AEP_SDF_SPHERE = 1
@@ -69,7 +71,10 @@ class aep_params(C.Structure):
         ("particle_damp", C.c_double),
         ("mass_bits", C.c_int32),
         ("momentum_bits", C.c_int32),
-        ("reserved", C.c_int64 * 8),
+        ("mesh_damp", C.c_double),
+        ("cloth_volume_weighting", C.c_int32),
+        ("reserved_i", C.c_int32),
+        ("reserved", C.c_int64 * 6),
     ]
 
 
@@ -100,6 +105,9 @@ SIGNATURES = {
     "aep_solver_destroy": (C.c_int, [_solver_p]),
     "aep_set_particles": (C.c_int, [_solver_p, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _u8p]),
     "aep_set_levelset": (C.c_int, [_solver_p, C.POINTER(aep_sdf), C.c_int32]),
+    "aep_set_mesh": (C.c_int, [_solver_p, C.c_int64, C.c_int64, _dp, C.POINTER(C.c_int32), _dp, _dp, _dp, _dp, _dp,
+                               _dp, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
+    "aep_get_mesh": (C.c_int, [_solver_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "aep_init_volumes": (C.c_int, [_solver_p]),
     "aep_step": (C.c_int, [_solver_p, C.c_double]),
     "aep_synchronize": (C.c_int, [_solver_p]),

@@ -31,7 +31,17 @@ struct aep_solver {
     aep_grid_desc grid{};
     aep_params prm{};
     KParams kp{};
-    int64_t n = 0, cap = 0;
+    int64_t n = 0, cap = 0;   // n = np + nv + nf particle slots
+    int64_t np = 0, nv = 0, nf = 0;
+    bool stepped_since_upload = false;
+    // LagrangianMesh device state
+    int32_t* faces = nullptr;
+    float* rest = nullptr;
+    float* estress = nullptr;
+    unsigned long long* vforce = nullptr;
+    int32_t* slot_of = nullptr;
+    int32_t* curidx_of = nullptr;
+    double cloth[5] = {0, 0, 0, 0, 0};  // mu, lambda, shear, stiffness, friction
     ParticleSet set[2];
     PArrays P[2];
     int cur = 0;
@@ -129,7 +139,44 @@ void fill_kparams(aep_solver* s) {
     k.friction = (float)p.friction;
     k.friction_bug = p.friction_bug;
     k.particle_damp = (float)p.particle_damp;
+    k.mesh_damp = (float)p.mesh_damp;
     k.track_fp = p.track_plastic_F;
+}
+
+MeshArrays mesh_arrays(aep_solver* s) {
+    MeshArrays M{};
+    M.nv = (int)s->nv;
+    M.nf = (int)s->nf;
+    M.vbase = (int)s->np;
+    M.ebase = (int)(s->np + s->nv);
+    M.faces = s->faces;
+    M.rest = s->rest;
+    M.estress = s->estress;
+    M.vforce = s->vforce;
+    M.slot_of = s->slot_of;
+    M.curidx_of = s->curidx_of;
+    M.mu = (float)s->cloth[0];
+    M.lambda = (float)s->cloth[1];
+    M.shear = (float)s->cloth[2];
+    M.stiffness = (float)s->cloth[3];
+    M.friction = (float)s->cloth[4];
+    M.damp = (float)s->prm.mesh_damp;
+    M.volume_weighting = s->prm.cloth_volume_weighting;
+    return M;
+}
+
+void free_mesh(aep_solver* s) {
+    cudaFree(s->faces);
+    cudaFree(s->rest);
+    cudaFree(s->estress);
+    cudaFree(s->vforce);
+    cudaFree(s->slot_of);
+    cudaFree(s->curidx_of);
+    s->faces = nullptr;
+    s->rest = s->estress = nullptr;
+    s->vforce = nullptr;
+    s->slot_of = s->curidx_of = nullptr;
+    s->nv = s->nf = 0;
 }
 
 void build_parrays(aep_solver* s, int which) {
@@ -169,16 +216,31 @@ void free_particles(aep_solver* s) {
     s->cap = 0;
 }
 
-aep_status ensure_capacity(aep_solver* s, int64_t n) {
+// Grow the particle buffers to n slots.  The first `keep` slots of set 0 (in id
+// order, i.e. before any step) survive the reallocation.
+aep_status ensure_capacity(aep_solver* s, int64_t n, int64_t keep = 0) {
     if (n <= s->cap) return AEP_OK;
-    free_particles(s);
     size_t nf = kFloatArrays + (s->prm.track_plastic_F ? kFpArrays : 0);
+    ParticleSet old = s->set[0];
+    int64_t oldcap = s->cap;
+    s->set[0] = ParticleSet{};  // keep the old set 0 alive until copied
+    free_particles(s);
     s->cap = n;
     for (int i = 0; i < 2; ++i) {
         CK(cudaMalloc(&s->set[i].f, sizeof(float) * nf * (size_t)n));
         CK(cudaMalloc(&s->set[i].mat, (size_t)n));
         CK(cudaMalloc(&s->set[i].id, sizeof(int32_t) * (size_t)n));
     }
+    if (keep > 0 && old.f) {
+        for (size_t k = 0; k < nf; ++k)
+            CK(cudaMemcpy(s->set[0].f + k * (size_t)n, old.f + k * (size_t)oldcap, sizeof(float) * (size_t)keep,
+                          cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(s->set[0].mat, old.mat, (size_t)keep, cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(s->set[0].id, old.id, sizeof(int32_t) * (size_t)keep, cudaMemcpyDeviceToDevice));
+    }
+    cudaFree(old.f);
+    cudaFree(old.mat);
+    cudaFree(old.id);
     CK(cudaMalloc(&s->keys, sizeof(uint32_t) * (size_t)n));
     CK(cudaMalloc(&s->keys_sorted, sizeof(uint32_t) * (size_t)n));
     CK(cudaMalloc(&s->iota, sizeof(int32_t) * (size_t)n));
@@ -195,18 +257,28 @@ aep_status ensure_capacity(aep_solver* s, int64_t n) {
     return AEP_OK;
 }
 
-aep_status upload(aep_solver* s, const double* src, int count, int mode, float* const* dst) {
-    CK(cudaMemcpyAsync(s->staging, src, sizeof(double) * count * (size_t)s->n, cudaMemcpyHostToDevice, s->stream));
-    launch_upload((int)s->n, mode, s->staging, dst, s->stream);
+// upload `count` doubles per item for items [id0, id0 + n) of set 0
+aep_status upload(aep_solver* s, const double* src, int count, int mode, float* const* dst, int64_t n = -1,
+                  int64_t id0 = 0) {
+    if (n < 0) n = s->n;
+    CK(cudaMemcpyAsync(s->staging, src, sizeof(double) * count * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    float* d[9] = {};
+    int nd = mode == 3 ? 1 : (mode == 0 ? 3 : 9);
+    for (int k = 0; k < nd; ++k) d[k] = dst[k] + id0;
+    launch_upload((int)n, mode, s->staging, d, s->stream);
     CKLAUNCH();
     return AEP_OK;
 }
 
-aep_status download(aep_solver* s, double* dst, int count, int mode, float* const* src) {
+// download ids [id_lo, id_hi) in id order
+aep_status download(aep_solver* s, double* dst, int count, int mode, float* const* src, int64_t id_lo = 0,
+                    int64_t id_hi = -1) {
+    if (id_hi < 0) id_hi = s->n;
     const PArrays& P = s->P[s->cur];
-    launch_download((int)s->n, mode, P.id, s->staging, src, s->stream);
+    launch_download((int)s->n, mode, P.id, s->staging, src, s->stream, (int)id_lo, (int)id_hi);
     CKLAUNCH();
-    CK(cudaMemcpyAsync(dst, s->staging, sizeof(double) * count * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(dst, s->staging, sizeof(double) * count * (size_t)(id_hi - id_lo), cudaMemcpyDeviceToHost,
+                       s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return AEP_OK;
 }
@@ -254,7 +326,7 @@ aep_status run_p2g(aep_solver* s) {
                   s->stream));
     CK(cudaMemsetAsync(s->G.nactive, 0, sizeof(int32_t), s->stream));
     mark(s, AEP_PHASE_P2G);
-    launch_p2g(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, s->stream);
+    launch_p2g(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, s->slot_of, s->curidx_of, s->stream);
     CKLAUNCH();
     mark(s, AEP_PHASE_NORMALIZE);
     launch_normalize(s->kp, s->G, s->dstats, s->grid_blocks, s->stream);
@@ -291,6 +363,7 @@ void aep_default_params(aep_params* p) {
     p->friction_bug = 1;   // HybridSolver.cpp:500-501
     p->track_plastic_F = 0;
     p->particle_damp = 0.0;  // HybridSolver.cpp:916
+    p->mesh_damp = 1.0;      // HybridSolver.cpp:926,932
     p->mass_bits = 34;
     p->momentum_bits = 40;
 }
@@ -346,6 +419,7 @@ aep_status aep_solver_destroy(aep_solver* s) {
     if (!s) return AEP_INVALID_ARG;
     cudaStreamSynchronize(s->stream);
     free_particles(s);
+    free_mesh(s);
     cudaFree(s->G.acc);
     cudaFree(s->G.vel);
     cudaFree(s->G.vbf);
@@ -378,9 +452,10 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
             if (material[p] > AEP_SAND) return fail(s, AEP_INVALID_ARG, "aep_set_particles: unknown material tag");
     if (!(mm > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_particles: all masses are zero");
     CK(cudaStreamSynchronize(s->stream));
+    free_mesh(s);  // a mesh must be (re)attached after the particles
     aep_status st = ensure_capacity(s, n);
     if (st != AEP_OK) return st;
-    s->n = n;
+    s->n = s->np = n;
     s->cur = 0;
     s->m_max = mm;
     fill_kparams(s);
@@ -424,7 +499,160 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     CK(cudaStreamSynchronize(s->stream));
     s->have_particles = true;
     s->keys_valid = false;
+    s->stepped_since_upload = false;
     s->last_stage = 0;
+    return AEP_OK;
+}
+
+// LagrangianMesh(vertexPositions, faces, vertexVelocities, elementVelocities, vertexMasses,
+// vertexVolumes, elementMasses, elementVolumes, elementDirections_1..3, elementRestDirections_1..3,
+// mu, lambda, shearStiffness, stiffness, frictionCoeff)   (LagrangianMesh.cpp:127-195)
+aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv, const int32_t* faces,
+                        const double* vv, const double* ve, const double* mv, const double* volv, const double* me,
+                        const double* vole, const double* d, const double* drest, double mu, double lambda,
+                        double shear_stiffness, double stiffness, double friction_coeff) {
+    if (!s) return AEP_INVALID_ARG;
+    if (nv <= 0 || nf <= 0 || !xv || !faces || !mv || !me || !vole || !d || !drest)
+        return fail(s, AEP_INVALID_ARG, "aep_set_mesh: need nv, nf > 0 and non-null xv, faces, masses, "
+                                        "element volumes and directions");
+    if (s->have_particles && s->stepped_since_upload)
+        return fail(s, AEP_NOT_READY, "aep_set_mesh: attach the mesh before the first step");
+    if (s->np + nv + nf > (int64_t)INT32_MAX / 2) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: too many items");
+    for (int64_t e = 0; e < nf; ++e)
+        for (int c = 0; c < 3; ++c) {
+            int32_t v = faces[c * nf + e];
+            if (v < 0 || v >= nv) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: face index out of range");
+        }
+    double mm = s->have_particles ? s->m_max : 0.0;
+    for (int64_t i = 0; i < nv; ++i) {
+        if (!(mv[i] >= 0.0) || !std::isfinite(mv[i])) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: bad mass");
+        mm = std::max(mm, mv[i]);
+    }
+    for (int64_t e = 0; e < nf; ++e) {
+        if (!(me[e] >= 0.0) || !std::isfinite(me[e])) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: bad mass");
+        mm = std::max(mm, me[e]);
+    }
+    if (!(mm > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: all masses are zero");
+    // rest data per element: inverseR of the rest in-plane R (geometry.cpp:67-73, from the
+    // Gram-Schmidt QR of the rest directions, LagrangianMesh.cpp:421-429) and the third
+    // row of the rest direction matrix (HybridSolver.cpp:427)
+    std::vector<float> rest((size_t)6 * nf);
+    for (int64_t e = 0; e < nf; ++e) {
+        double D1[3], D2[3], D3[3];
+        for (int a = 0; a < 3; ++a) {
+            D1[a] = drest[0 * 3 * nf + a * nf + e];
+            D2[a] = drest[1 * 3 * nf + a * nf + e];
+            D3[a] = drest[2 * 3 * nf + a * nf + e];
+        }
+        double r11 = std::sqrt(D1[0] * D1[0] + D1[1] * D1[1] + D1[2] * D1[2]);
+        double r12 = (D2[0] * D1[0] + D2[1] * D1[1] + D2[2] * D1[2]) / r11;
+        double q2[3];
+        for (int a = 0; a < 3; ++a) q2[a] = D2[a] - r12 * D1[a] / r11;
+        double r22 = std::sqrt(q2[0] * q2[0] + q2[1] * q2[1] + q2[2] * q2[2]);
+        if (!(r11 > 0.0) || !(r22 > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: degenerate rest element");
+        rest[6 * e + 0] = (float)(1.0 / r11);
+        rest[6 * e + 1] = (float)(-r12 / r11 / r22);
+        rest[6 * e + 2] = (float)(1.0 / r22);
+        rest[6 * e + 3] = (float)D1[2];
+        rest[6 * e + 4] = (float)D2[2];
+        rest[6 * e + 5] = (float)D3[2];
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    const int64_t np = s->have_particles ? s->np : 0;
+    free_mesh(s);
+    const int64_t total = np + nv + nf;
+    aep_status st = ensure_capacity(s, total, np);
+    if (st != AEP_OK) return st;
+    s->np = np;
+    s->nv = nv;
+    s->nf = nf;
+    s->n = total;
+    s->cur = 0;
+    s->m_max = mm;
+    s->cloth[0] = mu;
+    s->cloth[1] = lambda;
+    s->cloth[2] = shear_stiffness;
+    s->cloth[3] = stiffness;
+    s->cloth[4] = friction_coeff;
+    fill_kparams(s);
+    PArrays& P = s->P[0];
+    const int64_t vb = np, eb = np + nv;
+    std::vector<double> tmp((size_t)9 * std::max(nv, nf), 0.0);
+    // vertices
+    st = upload(s, xv, 3, 0, P.x, nv, vb);
+    if (st) return st;
+    if (vv) { st = upload(s, vv, 3, 0, P.v, nv, vb); if (st) return st; }
+    else for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(P.v[a] + vb, 0, sizeof(float) * nv, s->stream));
+    for (int a = 0; a < 9; ++a) CK(cudaMemsetAsync(P.B[a] + vb, 0, sizeof(float) * (nv + nf), s->stream));
+    for (int64_t i = 0; i < nv; ++i)
+        for (int k = 0; k < 9; ++k) tmp[9 * i + k] = (k % 4 == 0) ? 1.0 : 0.0;
+    st = upload(s, tmp.data(), 9, 2, P.F, nv, vb);
+    if (st) return st;
+    st = upload(s, mv, 1, 3, &P.m, nv, vb);
+    if (st) return st;
+    if (volv) { st = upload(s, volv, 1, 3, &P.vol, nv, vb); if (st) return st; }
+    else CK(cudaMemsetAsync(P.vol + vb, 0, sizeof(float) * nv, s->stream));
+    CK(cudaMemsetAsync(P.plastic + vb, 0, sizeof(float) * (nv + nf), s->stream));
+    launch_init_particles((int)nv, P, nullptr, 0, 0, s->stream, (int)vb, AEP_CLOTH_VERTEX);
+    CKLAUNCH();
+    // elements: positions are the centroids of their vertices (LagrangianMesh.cpp:186-187)
+    for (int64_t e = 0; e < nf; ++e)
+        for (int a = 0; a < 3; ++a) {
+            double c = 0.0;
+            for (int k = 0; k < 3; ++k) c += xv[a * nv + faces[k * nf + e]];
+            tmp[a * nf + e] = c / 3.0;
+        }
+    CK(cudaStreamSynchronize(s->stream));
+    st = upload(s, tmp.data(), 3, 0, P.x, nf, eb);
+    if (st) return st;
+    if (ve) { st = upload(s, ve, 3, 0, P.v, nf, eb); if (st) return st; }
+    else for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(P.v[a] + eb, 0, sizeof(float) * nf, s->stream));
+    st = upload(s, d, 9, 4, P.F, nf, eb);
+    if (st) return st;
+    st = upload(s, me, 1, 3, &P.m, nf, eb);
+    if (st) return st;
+    st = upload(s, vole, 1, 3, &P.vol, nf, eb);
+    if (st) return st;
+    launch_init_particles((int)nf, P, nullptr, 0, 0, s->stream, (int)eb, AEP_CLOTH_ELEMENT);
+    CKLAUNCH();
+    // mesh buffers
+    std::vector<int32_t> fem((size_t)3 * nf);
+    for (int64_t e = 0; e < nf; ++e)
+        for (int c = 0; c < 3; ++c) fem[3 * e + c] = faces[c * nf + e];
+    CK(cudaMalloc(&s->faces, sizeof(int32_t) * 3 * nf));
+    CK(cudaMalloc(&s->rest, sizeof(float) * 6 * nf));
+    CK(cudaMalloc(&s->estress, sizeof(float) * 9 * nf));
+    CK(cudaMalloc(&s->vforce, sizeof(unsigned long long) * 3 * nv));
+    CK(cudaMalloc(&s->slot_of, sizeof(int32_t) * total));
+    CK(cudaMalloc(&s->curidx_of, sizeof(int32_t) * total));
+    CK(cudaMemcpy(s->faces, fem.data(), sizeof(int32_t) * 3 * nf, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->rest, rest.data(), sizeof(float) * 6 * nf, cudaMemcpyHostToDevice));
+    CK(cudaMemset(s->vforce, 0, sizeof(unsigned long long) * 3 * nv));
+    CK(cudaStreamSynchronize(s->stream));
+    s->have_particles = true;
+    s->keys_valid = false;
+    s->stepped_since_upload = false;
+    s->last_stage = 0;
+    return AEP_OK;
+}
+
+// LagrangianMesh public members (LagrangianMesh.h:37-61) in the layouts of aep_set_mesh;
+// any pointer may be NULL.
+aep_status aep_get_mesh(aep_solver* s, double* xv, double* vv, double* Bv, double* xe, double* ve, double* Be,
+                        double* d) {
+    if (!s) return AEP_INVALID_ARG;
+    if (s->nf == 0) return fail(s, AEP_NOT_READY, "aep_get_mesh: no mesh");
+    CK(cudaStreamSynchronize(s->stream));
+    PArrays& P = s->P[s->cur];
+    const int64_t vb = s->np, eb = s->np + s->nv, ee = s->n;
+    aep_status st;
+    if (xv && (st = download(s, xv, 3, 0, P.x, vb, eb))) return st;
+    if (vv && (st = download(s, vv, 3, 0, P.v, vb, eb))) return st;
+    if (Bv && (st = download(s, Bv, 9, 1, P.B, vb, eb))) return st;
+    if (xe && (st = download(s, xe, 3, 0, P.x, eb, ee))) return st;
+    if (ve && (st = download(s, ve, 3, 0, P.v, eb, ee))) return st;
+    if (Be && (st = download(s, Be, 9, 1, P.B, eb, ee))) return st;
+    if (d && (st = download(s, d, 9, 4, P.F, eb, ee))) return st;
     return AEP_OK;
 }
 
@@ -477,7 +705,8 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
     }
     const float dtf = (float)dt;
     const PArrays& P = s->P[s->cur];
-    launch_force(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, dtf, s->dstats, s->stream);
+    const MeshArrays M = mesh_arrays(s);
+    launch_force(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, dtf, s->dstats, M, s->stream);
     CKLAUNCH();
     if (timed) mark(s, AEP_PHASE_GRID);
     if (stage == AEP_STAGE_FORCES) {
@@ -494,7 +723,7 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
     if (stage == AEP_STAGE_GRID) return AEP_OK;
     if (timed) mark(s, AEP_PHASE_G2P);
     const int nx = 1 - s->cur;
-    launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, dtf, s->keys, s->dstats, s->stream);
+    launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, dtf, s->keys, s->dstats, M, s->stream);
     CKLAUNCH();
     if (timed) {
         mark(s, AEP_NUM_PHASES);
@@ -503,6 +732,7 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
     }
     s->cur = nx;
     s->keys_valid = true;
+    s->stepped_since_upload = true;
     s->steps++;
     return AEP_OK;
 }
@@ -519,18 +749,19 @@ aep_status aep_get_particles(aep_solver* s, int64_t n, double* x, double* v, dou
                              double* vol, double* plastic) {
     if (!s) return AEP_INVALID_ARG;
     if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_get_particles: no particles");
-    if (n != s->n) return fail(s, AEP_INVALID_ARG, "aep_get_particles: n mismatch");
+    if (n != s->np) return fail(s, AEP_INVALID_ARG, "aep_get_particles: n mismatch");
     if (Fp && !s->prm.track_plastic_F) return fail(s, AEP_INVALID_ARG, "aep_get_particles: Fp needs track_plastic_F");
     CK(cudaStreamSynchronize(s->stream));
     PArrays& P = s->P[s->cur];
     aep_status st;
-    if (x && (st = download(s, x, 3, 0, P.x))) return st;
-    if (v && (st = download(s, v, 3, 0, P.v))) return st;
-    if (B && (st = download(s, B, 9, 1, P.B))) return st;
-    if (Fe && (st = download(s, Fe, 9, 2, P.F))) return st;
-    if (Fp && (st = download(s, Fp, 9, 2, P.Fp))) return st;
-    if (vol && (st = download(s, vol, 1, 3, &P.vol))) return st;
-    if (plastic && (st = download(s, plastic, 1, 3, &P.plastic))) return st;
+    const int64_t np = s->np;
+    if (x && (st = download(s, x, 3, 0, P.x, 0, np))) return st;
+    if (v && (st = download(s, v, 3, 0, P.v, 0, np))) return st;
+    if (B && (st = download(s, B, 9, 1, P.B, 0, np))) return st;
+    if (Fe && (st = download(s, Fe, 9, 2, P.F, 0, np))) return st;
+    if (Fp && (st = download(s, Fp, 9, 2, P.Fp, 0, np))) return st;
+    if (vol && (st = download(s, vol, 1, 3, &P.vol, 0, np))) return st;
+    if (plastic && (st = download(s, plastic, 1, 3, &P.plastic, 0, np))) return st;
     return AEP_OK;
 }
 

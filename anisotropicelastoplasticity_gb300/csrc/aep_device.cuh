@@ -22,7 +22,7 @@ namespace aep {
 constexpr int kMaxShapes = 8;
 constexpr uint32_t kInvalidKey = 0xFFFFFFFFu;
 
-enum : int { kSnow = 0, kSand = 1 };
+enum : int { kSnow = 0, kSand = 1, kClothVertex = 2, kClothElement = 3 };
 enum : int { kSdfPlane = 0, kSdfSphere = 1, kSdfWall2Ground = 2 };
 
 struct DevShape {
@@ -44,6 +44,7 @@ struct KParams {
     float friction;
     int friction_bug;
     float particle_damp;
+    float mesh_damp;  // APIC damping of cloth vertices and elements, reference 1 (HS:926,932)
     int track_fp;
     int nshapes;
     DevShape shapes[kMaxShapes];
@@ -71,6 +72,23 @@ struct GArrays {
     uint32_t* flag;           // per node block: touched this step
     int32_t* active;          // list of touched node blocks
     int32_t* nactive;         // its length
+};
+
+// LagrangianMesh state on the device (LagrangianMesh.h:37-73).  Vertices and
+// elements live in the particle arrays with ids [vbase, vbase+nv) and
+// [ebase, ebase+nf); their element directions [d1 d2 d3] are stored as the
+// columns of the particle's F.
+struct MeshArrays {
+    int nv, nf, vbase, ebase;
+    const int32_t* faces;          // 3 per element: vertex indices 0..nv-1
+    const float* rest;             // 6 per element: inverseR of the rest in-plane R (i11, i12, i22)
+                                   // and the third row of the rest direction matrix (HS:427)
+    float* estress;                // 9 per element: -dt * (element normal stress), row-major
+    unsigned long long* vforce;    // 3 per vertex: dt * in-plane force, fixed point
+    int32_t* slot_of;              // per id: slot in this step's sorted order
+    int32_t* curidx_of;            // per id: index in the current particle arrays
+    float mu, lambda, shear, stiffness, friction, damp;
+    int volume_weighting;          // multiply the in-plane vertex forces by the element volume
 };
 
 struct DevStats {
@@ -378,6 +396,115 @@ __device__ __forceinline__ void eval_levelset(const KParams& P, float x, float y
         }
         if (ph < phi) { phi = ph; n[0] = nx; n[1] = ny; n[2] = nz; }
     }
+}
+
+// ---------------------------------------------------------------------------------
+// classical Gram-Schmidt QR of D = [d1 d2 d3] (geometry.cpp:31-62); row-major 3x3.
+__device__ __forceinline__ void gram_schmidt(const float D[9], float Q[9], float R[9]) {
+    float d1[3] = {D[0], D[3], D[6]}, d2[3] = {D[1], D[4], D[7]}, d3[3] = {D[2], D[5], D[8]};
+    const float r11 = sqrtf(d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2]);
+    float q1[3] = {d1[0] / r11, d1[1] / r11, d1[2] / r11};
+    const float r12 = d2[0] * q1[0] + d2[1] * q1[1] + d2[2] * q1[2];
+    float q2[3] = {d2[0] - r12 * q1[0], d2[1] - r12 * q1[1], d2[2] - r12 * q1[2]};
+    const float r22 = sqrtf(q2[0] * q2[0] + q2[1] * q2[1] + q2[2] * q2[2]);
+    q2[0] /= r22; q2[1] /= r22; q2[2] /= r22;
+    const float r13 = d3[0] * q1[0] + d3[1] * q1[1] + d3[2] * q1[2];
+    const float r23 = d3[0] * q2[0] + d3[1] * q2[1] + d3[2] * q2[2];
+    float q3[3] = {d3[0] - r13 * q1[0] - r23 * q2[0], d3[1] - r13 * q1[1] - r23 * q2[1],
+                   d3[2] - r13 * q1[2] - r23 * q2[2]};
+    const float r33 = sqrtf(q3[0] * q3[0] + q3[1] * q3[1] + q3[2] * q3[2]);
+    q3[0] /= r33; q3[1] /= r33; q3[2] /= r33;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        Q[3 * r + 0] = q1[r];
+        Q[3 * r + 1] = q2[r];
+        Q[3 * r + 2] = q3[r];
+    }
+    R[0] = r11; R[1] = r12; R[2] = r13;
+    R[3] = 0.f; R[4] = r22; R[5] = r23;
+    R[6] = 0.f; R[7] = 0.f; R[8] = r33;
+}
+
+// In-plane cloth forces of one element (LagrangianMesh.cpp:392-458): vertex forces
+// f1, f2, f3 and invRest * P (the in-plane part of the element stress, HS:406-409).
+// rest = (i11, i12, i22) of inverseR(rest in-plane R), geometry.cpp:67-73.
+__device__ __forceinline__ void cloth_inplane(const float Q[9], const float R[9], const float rest[3], float mu,
+                                              float lambda, float f[3][3], float ip[3]) {
+    const float i11 = rest[0], i12 = rest[1], i22 = rest[2];
+    const float t00 = i11 * R[0], t01 = i11 * R[1] + i12 * R[4], t11 = i22 * R[4];
+    // polar rotation of the upper-triangular [[t00, t01], [0, t11]] (positive diagonal, det > 0)
+    const float a = t00 + t11, c = -t01;
+    const float rn = rsqrtf(a * a + c * c);
+    const float cs = a * rn, sn = c * rn;
+    const float J = t00 * t11;
+    const float lj = lambda * (J - 1.0f);
+    // P = 2 mu (Rt - rot) + lambda (J - 1) cof(Rt); cof(Rt) = [[t11, 0], [-t01, t00]]
+    const float P00 = 2.0f * mu * (t00 - cs) + lj * t11;
+    const float P01 = 2.0f * mu * (t01 + sn);
+    const float P10 = 2.0f * mu * (-sn) - lj * t01;
+    const float P11 = 2.0f * mu * (t11 - cs) + lj * t00;
+    ip[0] = i11 * P00 + i12 * P10;  // (invRest P)(0,0)
+    ip[1] = i11 * P01 + i12 * P11;  // (0,1)
+    ip[2] = i22 * P11;              // (1,1)
+    const float c2 = -(P00 * i11 + P01 * i12), c3a = -P01 * i22, c3b = -P11 * i22;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float q1 = Q[3 * r], q2 = Q[3 * r + 1];
+        f[1][r] = c2 * q1;
+        f[2][r] = c3a * q1 + c3b * q2;
+        f[0][r] = -(f[1][r] + f[2][r]);
+    }
+}
+
+// Normal/shear stress of one element (HybridSolver.cpp:389-441): V dF3 d3^T.
+// w2 = third row of the rest direction matrix, (D_rest^T).col(2) at HS:427.
+__device__ __forceinline__ void cloth_normal_stress(const float D[9], const float Q[9], const float R[9],
+                                                    const float ip[3], const float w2[3], float shear, float stiffness,
+                                                    float vol, float S[9]) {
+    const float dr13 = shear * R[2], dr23 = shear * R[5];
+    const float r33 = R[8];
+    const float dr33 = r33 > 1.0f ? 0.0f : -stiffness * (1.0f - r33) * (1.0f - r33);
+    // dR = [[ip0, ip1, dr13], [0, ip2, dr23], [0, 0, dr33]];  K = dR R^T
+    const float dR[9] = {ip[0], ip[1], dr13, 0.f, ip[2], dr23, 0.f, 0.f, dr33};
+    float K[9];
+    mat_mul_bt(dR, R, K);
+    // upper triangle of K mirrored: M(a,b) = K(min(a,b), max(a,b))
+    const float M[9] = {K[0], K[1], K[2], K[1], K[4], K[5], K[2], K[5], K[8]};
+    // y = R^-T w2  (forward substitution with R^T lower-triangular)
+    const float y0 = w2[0] / R[0];
+    const float y1 = (w2[1] - R[1] * y0) / R[4];
+    const float y2 = (w2[2] - R[2] * y0 - R[5] * y1) / R[8];
+    float z[3], dF3[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) z[a] = M[3 * a] * y0 + M[3 * a + 1] * y1 + M[3 * a + 2] * y2;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dF3[a] = Q[3 * a] * z[0] + Q[3 * a + 1] * z[1] + Q[3 * a + 2] * z[2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) S[3 * a + b] = vol * dF3[a] * D[3 * b + 2];
+}
+
+// Cloth return mapping (HybridSolver.cpp:695-719): new d3 from the QR of [d1 d2 d3].
+__device__ __forceinline__ void cloth_return_map(const float D[9], float shear, float stiffness, float friction,
+                                                 float d3[3]) {
+    float Q[9], R[9];
+    gram_schmidt(D, Q, R);
+    float r13 = R[2], r23 = R[5], r33 = R[8];
+    if (r33 > 1.0f) {
+        r33 = 1.0f;
+        r13 = r23 = 0.0f;
+    } else {
+        const float nf = stiffness * (r33 - 1.0f) * (r33 - 1.0f);
+        const float sf = shear * sqrtf(r13 * r13 + r23 * r23);
+        if (sf > friction * nf) {
+            const float sc = friction * nf / sf;
+            r13 *= sc;
+            r23 *= sc;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) d3[a] = Q[3 * a] * r13 + Q[3 * a + 1] * r23 + Q[3 * a + 2] * r33;
 }
 
 __device__ __forceinline__ unsigned long long to_fixed(float v, float scale) {

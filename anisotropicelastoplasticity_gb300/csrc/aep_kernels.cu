@@ -85,7 +85,8 @@ __device__ __forceinline__ unsigned run_heads(unsigned hmask, int l, uint32_t ke
 }
 
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
-                                                     const int32_t* __restrict__ perm, int n, GArrays G) {
+                                                     const int32_t* __restrict__ perm, int n, GArrays G,
+                                                     int32_t* __restrict__ slot_of, int32_t* __restrict__ curidx_of) {
     __shared__ float4 sm4[(kP2GThreads / 16) * kP2GRegion];
     const int hw = threadIdx.x >> 4, l = threadIdx.x & 15;
     float4* const region = sm4 + hw * kP2GRegion;
@@ -138,6 +139,11 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
             const uint32_t key = keys[j];
             if (j == 0 || (keys[j - 1] >> 6) != (key >> 6)) mark_blocks(P, G, key);
             const int pj = perm[j];
+            if (slot_of) {  // a mesh is present: where each id sits in this step's order
+                const int id = cur.id[pj];
+                slot_of[id] = (int32_t)j;
+                curidx_of[id] = pj;
+            }
             float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
             float m = cur.m[pj];
             int cell[3];
@@ -393,7 +399,7 @@ __device__ void particle_stress_impulse(const KParams& P, const GArrays& G, cons
 // impulse scatter: f_i -= sum_p stress_p grad w_ip (HS:356-366), stored as dt * f_i
 __global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                        const int32_t* __restrict__ perm, int n, GArrays G,
-                                                       float dt_force, DevStats* st) {
+                                                       float dt_force, DevStats* st, MeshArrays M) {
     __shared__ float4 sm4[(kFrcThreads / 32) * kFrcWarpBuf];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const buf = sm4 + wid * kFrcWarpBuf;
@@ -404,8 +410,33 @@ __global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur
     if (j < n) {
         const int pj = perm[j];
         float w[3][4], dw[3][4], S[9];
+        float av[3] = {0.f, 0.f, 0.f};  // w-weighted impulse (cloth vertices)
         int cell[3];
-        particle_stress_impulse(P, G, cur, pj, dt_force, S, w, dw, cell, st);
+        const int mat = cur.mat[pj];
+        if (mat <= kSand) {
+            particle_stress_impulse(P, G, cur, pj, dt_force, S, w, dw, cell, st);
+        } else {
+            float f[3];
+            locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
+            particle_weights(P, cell, f, w, dw);
+            const int id = cur.id[pj];
+            if (mat == kClothVertex) {
+                // rg.forces += vertexOmegas^T vertexInPlaneForces (HS:376-378)
+                unsigned long long* vf = M.vforce + 3ull * (id - M.vbase);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    av[c] = __ll2float_rn((long long)vf[c]) * P.inv_mom_scale;
+                    vf[c] = 0ull;
+                }
+#pragma unroll
+                for (int k = 0; k < 9; ++k) S[k] = 0.f;
+            } else {
+                // element normal stress scattered with the element weight gradients (HS:444-454)
+                const float* es = M.estress + 9ull * (id - M.ebase);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) S[k] = es[k];
+            }
+        }
         float4* r = buf + frc_slot(lane);
         r[0] = make_float4(S[0], S[1], S[2], S[3]);
         r[1] = make_float4(S[4], S[5], S[6], S[7]);
@@ -419,6 +450,7 @@ __global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur
         my_key = keys[j];
         r[9] = make_float4(__int_as_float(cell[0] + 3), __int_as_float(cell[1] + 3), __int_as_float(cell[2] + 3),
                            __uint_as_float(my_key));
+        r[10] = make_float4(av[0], av[1], av[2], mat == kClothVertex ? 1.0f : 0.0f);
     }
     __syncwarp();
     // stream: half h takes particles [16h, 16h+16)
@@ -468,8 +500,48 @@ __global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur
             fy[oz] = fmaf(wz4[oz], ay_, fmaf(dz4[oz], cy, fy[oz]));
             fz[oz] = fmaf(wz4[oz], az_, fmaf(dz4[oz], cz, fz[oz]));
         }
+        const float4 q10 = r[10];
+        if (q10.w != 0.0f) {  // cloth vertex: + w f_v (uniform across the half-warp)
+            const float wx_ = p3 * q10.x, wy_ = p3 * q10.y, wz_ = p3 * q10.z;
+#pragma unroll
+            for (int oz = 0; oz < 4; ++oz) {
+                fx[oz] = fmaf(wz4[oz], wx_, fx[oz]);
+                fy[oz] = fmaf(wz4[oz], wy_, fy[oz]);
+                fz[oz] = fmaf(wz4[oz], wz_, fz[oz]);
+            }
+        }
     }
     flush();
+}
+
+// ===================================================================================
+// per-element cloth forces: in-plane vertex forces (LagrangianMesh.cpp:382-460)
+// accumulated per vertex in fixed point, and the element normal/shear stress
+// (HybridSolver.cpp:389-442) stored for the element's scatter in k_force.
+__global__ void k_cloth_force(KParams P, PArrays cur, MeshArrays M, float dt_force) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M.nf) return;
+    const int pc = M.curidx_of[M.ebase + e];
+    float D[9], Q[9], R[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) D[k] = cur.F[k][pc];
+    gram_schmidt(D, Q, R);
+    const float* rest = M.rest + 6ull * e;
+    const float rs[3] = {rest[0], rest[1], rest[2]}, w2[3] = {rest[3], rest[4], rest[5]};
+    float f[3][3], ip[3];
+    cloth_inplane(Q, R, rs, M.mu, M.lambda, f, ip);
+    const float fw = dt_force * (M.volume_weighting ? cur.vol[pc] : 1.0f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        unsigned long long* vf = M.vforce + 3ull * M.faces[3 * e + c];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) atomicAdd(vf + r, to_fixed(fw * f[c][r], P.mom_scale));
+    }
+    float S[9];
+    cloth_normal_stress(D, Q, R, ip, w2, M.shear, M.stiffness, cur.vol[pc], S);
+    float* es = M.estress + 9ull * e;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) es[k] = -dt_force * S[k];
 }
 
 // ===================================================================================
@@ -574,34 +646,18 @@ __device__ __forceinline__ void return_map(const KParams& P, int mat, T s[3], T&
     }
 }
 
-// G2P + APIC + advection + F update + return mapping, one thread per particle
-__global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
-                                             int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
-                                             DevStats* st) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const int pj = perm[j];
-    float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
-    int cell[3];
-    float f[3], w[3][4], dw[3][4];
-    locate(P, xp[0], xp[1], xp[2], cell, f);
-    const bool truncated = particle_weights(P, cell, f, w, dw);
-    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
-    uint32_t X[4], Y[4], Z[4];
-    stencil_offsets(P, base, X, Y, Z);
-    float xi[3][4];
+// Gather of v (G2P velocity + APIC) and v^bf (advection + velocity gradient) over
+// the 4x4x4 stencil, contracted one axis at a time because the weights are tensor
+// products: x first (A), then z (B), then y.
+//   A0 = sum_x wx v      A1 = sum_x wx xi_x v   A2 = sum_x dwx vbf   A3 = sum_x wx vbf
+//   vp = sum w v,  C = sum w v xi^T,  xs = sum w vbf,  Gb = sum vbf (grad w)^T
+__device__ __forceinline__ void g2p_gather(const GArrays& G, const float w[3][4], const float dw[3][4],
+                                           const float xi[3][4], const uint32_t X[4], const uint32_t Y[4],
+                                           const uint32_t Z[4], float vp[3], float C[9], float xs[3], float Gb[9]) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < 3; ++k) vp[k] = xs[k] = 0.f;
 #pragma unroll
-        for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
-
-    // Gather of v (G2P velocity + APIC) and v^bf (advection + velocity gradient)
-    // over the 4x4x4 stencil, contracted one axis at a time because the weights
-    // are tensor products: x first (A), then z (Bq), then y.
-    //   A0 = sum_x wx v      A1 = sum_x wx xi_x v   A2 = sum_x dwx vbf   A3 = sum_x wx vbf
-    //   vp = sum w v,  C = sum w v xi^T,  xs = sum w vbf,  Gb = sum vbf (grad w)^T
-    float vp[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
-    float C[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Gb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 9; ++k) C[k] = Gb[k] = 0.f;
     float wxi[4];
 #pragma unroll
     for (int o = 0; o < 4; ++o) wxi[o] = w[0][o] * xi[0][o];
@@ -647,6 +703,45 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
             Gb[3 * c + 2] = fmaf(cy, B5[c], Gb[3 * c + 2]);
         }
     }
+}
+
+// APIC symmetric-part damping (HybridSolver.cpp:808-824): B = skew(C) + (1 - damp) sym(C)
+__device__ __forceinline__ void apic_damp(const float C[9], float damp, float Bn[9]) {
+    const float keep = 1.0f - damp;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const float sym = 0.5f * (C[3 * a + b] + C[3 * b + a]);
+            Bn[3 * a + b] = (C[3 * a + b] - sym) + keep * sym;
+        }
+}
+
+// G2P + APIC + advection + F update + return mapping, one thread per particle
+__global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
+                                             int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
+                                             DevStats* st) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int pj = perm[j];
+    const int mat = cur.mat[pj];
+    if (mat == kClothElement) return;  // elements follow their vertices (k_cloth_g2p)
+    float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
+    int cell[3];
+    float f[3], w[3][4], dw[3][4];
+    locate(P, xp[0], xp[1], xp[2], cell, f);
+    const bool truncated = particle_weights(P, cell, f, w, dw);
+    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+    uint32_t X[4], Y[4], Z[4];
+    stencil_offsets(P, base, X, Y, Z);
+    float xi[3][4];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
+
+    float vp[3], xs[3], C[9], Gb[9];
+    g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
     // advection x = sum w (x_i + dt v^bf_i) (HS:944): exact linear reproduction for a
     // full stencil; a stencil cut by the grid boundary keeps its lost weight.
     float xn[3];
@@ -664,16 +759,32 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
 #pragma unroll
         for (int a = 0; a < 3; ++a) xn[a] += xp[a] * (sw - 1.0f) + swx[a];
     }
-    // APIC damping (HS:808-824)
+    // APIC damping (HS:916, 926)
     float Bn[9];
-    const float keep = 1.0f - P.particle_damp;
+    apic_damp(C, mat == kClothVertex ? P.mesh_damp : P.particle_damp, Bn);
+    if (mat == kClothVertex) {  // vertices carry no deformation gradient of their own
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            float sym = 0.5f * (C[3 * a + b] + C[3 * b + a]);
-            Bn[3 * a + b] = (C[3 * a + b] - sym) + keep * sym;
+        for (int a = 0; a < 3; ++a) {
+            nxt.x[a][j] = xn[a];
+            nxt.v[a][j] = vp[a];
         }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            nxt.B[k][j] = Bn[k];
+            nxt.F[k][j] = cur.F[k][pj];
+        }
+        nxt.plastic[j] = cur.plastic[pj];
+        nxt.mat[j] = (uint8_t)mat;
+        nxt.m[j] = cur.m[pj];
+        nxt.vol[j] = cur.vol[pj];
+        nxt.id[j] = cur.id[pj];
+        int vc[3];
+        float vf[3];
+        const bool vclamped = locate(P, xn[0], xn[1], xn[2], vc, vf);
+        keys_next[j] = make_key(P, vc);
+        if (vclamped) atomicAdd(&st->out_of_domain, 1ull);
+        return;
+    }
     // F update (HS:560-576)
     float F[9], GF[9], Ftr[9];
 #pragma unroll
@@ -682,7 +793,6 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
 #pragma unroll
     for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
     // return mapping (HS:612-677)
-    const int mat = cur.mat[pj];
     float q = cur.plastic[pj];
     float U[9], s[3], V[9];
     float Fe[9], sn[3];
@@ -771,12 +881,88 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
 }
 
 // ===================================================================================
+// cloth elements (one thread per element): APIC momenta from the element's own
+// G2P velocity at its old centroid (HS:927-933), velocity = mean of the new vertex
+// velocities (HS:749-756), position = centroid of the new vertex positions
+// (LagrangianMesh.cpp:371-380), directions d1, d2 from the vertices and
+// d3 += dt grad v^bf d3 (HS:584-607), then the QR return mapping (HS:686-720).
+__global__ void k_cloth_g2p(KParams P, PArrays cur, PArrays nxt, GArrays G, MeshArrays M, float dt,
+                            uint32_t* __restrict__ keys_next, DevStats* st) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M.nf) return;
+    const int id = M.ebase + e;
+    const int j = M.slot_of[id];
+    const int pc = M.curidx_of[id];
+    float xp[3] = {cur.x[0][pc], cur.x[1][pc], cur.x[2][pc]};
+    int cell[3];
+    float f[3], w[3][4], dw[3][4];
+    locate(P, xp[0], xp[1], xp[2], cell, f);
+    particle_weights(P, cell, f, w, dw);
+    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+    uint32_t X[4], Y[4], Z[4];
+    stencil_offsets(P, base, X, Y, Z);
+    float xi[3][4];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
+    float vp[3], xs[3], C[9], Gb[9];
+    g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+    float Bn[9];
+    apic_damp(C, P.mesh_damp, Bn);
+    float xv[3][3], vv[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int sv = M.slot_of[M.vbase + M.faces[3 * e + c]];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            xv[c][a] = nxt.x[a][sv];
+            vv[c][a] = nxt.v[a][sv];
+        }
+    }
+    float D[9];
+    float d3o[3] = {cur.F[2][pc], cur.F[5][pc], cur.F[8][pc]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        D[3 * a + 0] = xv[1][a] - xv[0][a];
+        D[3 * a + 1] = xv[2][a] - xv[0][a];
+        D[3 * a + 2] = dt * (Gb[3 * a] * d3o[0] + Gb[3 * a + 1] * d3o[1] + Gb[3 * a + 2] * d3o[2]) + d3o[a];
+    }
+    float d3[3];
+    cloth_return_map(D, M.shear, M.stiffness, M.friction, d3);
+    D[2] = d3[0]; D[5] = d3[1]; D[8] = d3[2];
+    float xn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        xn[a] = (xv[0][a] + xv[1][a] + xv[2][a]) / 3.0f;
+        nxt.x[a][j] = xn[a];
+        nxt.v[a][j] = (vv[0][a] + vv[1][a] + vv[2][a]) / 3.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        nxt.B[k][j] = Bn[k];
+        nxt.F[k][j] = D[k];
+    }
+    nxt.plastic[j] = cur.plastic[pc];
+    nxt.mat[j] = (uint8_t)kClothElement;
+    nxt.m[j] = cur.m[pc];
+    nxt.vol[j] = cur.vol[pc];
+    nxt.id[j] = id;
+    int nc[3];
+    float nf[3];
+    const bool clamped = locate(P, xn[0], xn[1], xn[2], nc, nf);
+    keys_next[j] = make_key(P, nc);
+    if (clamped) atomicAdd(&st->out_of_domain, 1ull);
+}
+
+// ===================================================================================
 // first-P2G densities and volumes (HybridSolver.cpp:242-249):
 // rho_p = sum_i w_ip m_i / h^3, vol_p = m_p / rho_p; written in the current order.
 __global__ void k_volumes(KParams P, PArrays cur, const int32_t* __restrict__ perm, int n, GArrays G) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const int pj = perm[j];
+    if (cur.mat[pj] > kSand) return;  // only the ParticleSystem gets volumes (HS:244-248)
     int cell[3];
     float f[3], w[3][4], dw[3][4];
     locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
@@ -795,7 +981,8 @@ __global__ void k_volumes(KParams P, PArrays cur, const int32_t* __restrict__ pe
 // ===================================================================================
 // layout conversion: reference FP64 layouts <-> device FP32 structure of arrays
 // mode: 0 = N x 3 column-major vector field into dst[3], 1 = 9N B rows (see aep.h),
-// 2 = 9N per-particle column-major 3x3 into row-major dst[9], 3 = N scalars
+// 2 = 9N per-particle column-major 3x3 into row-major dst[9], 3 = N scalars,
+// 4 = element directions d1 | d2 | d3 (each N x 3 column-major) into the columns of dst[9]
 __global__ void k_upload(int n, int mode, const double* __restrict__ src, float* d0, float* d1, float* d2,
                          float* d3, float* d4, float* d5, float* d6, float* d7, float* d8) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -809,18 +996,26 @@ __global__ void k_upload(int n, int mode, const double* __restrict__ src, float*
     } else if (mode == 2) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[9l * p + a + 3 * b];
+    } else if (mode == 4) {
+        for (int c = 0; c < 3; ++c)
+            for (int a = 0; a < 3; ++a) d[3 * a + c][p] = (float)src[(long)c * 3 * n + (long)a * n + p];
     } else {
         d[0][p] = (float)src[p];
     }
 }
 
+// j runs over all n particle slots; only ids in [id_lo, id_hi) are written, at id - id_lo
 __global__ void k_download(int n, int mode, const int32_t* __restrict__ id, double* __restrict__ dst,
                            const float* s0, const float* s1, const float* s2, const float* s3, const float* s4,
-                           const float* s5, const float* s6, const float* s7, const float* s8) {
+                           const float* s5, const float* s6, const float* s7, const float* s8, int id_lo,
+                           int id_hi) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const float* s[9] = {s0, s1, s2, s3, s4, s5, s6, s7, s8};
-    const long p = id[j];
+    const int pid = id[j];
+    if (pid < id_lo || pid >= id_hi) return;
+    const long p = pid - id_lo;
+    n = id_hi - id_lo;
     if (mode == 0) {
         for (int a = 0; a < 3; ++a) dst[(long)a * n + p] = s[a][j];
     } else if (mode == 1) {
@@ -829,16 +1024,21 @@ __global__ void k_download(int n, int mode, const int32_t* __restrict__ id, doub
     } else if (mode == 2) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) dst[9 * p + a + 3 * b] = s[3 * a + b][j];
+    } else if (mode == 4) {
+        for (int c = 0; c < 3; ++c)
+            for (int a = 0; a < 3; ++a) dst[(long)c * 3 * n + (long)a * n + p] = s[3 * a + c][j];
     } else {
         dst[p] = s[0][j];
     }
 }
 
-__global__ void k_init_particles(int n, PArrays cur, const uint8_t* __restrict__ mat_in, int has_fp, int track_fp) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
+__global__ void k_init_particles(int n, PArrays cur, const uint8_t* __restrict__ mat_in, int has_fp, int track_fp,
+                                 int id0, int fixed_mat) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int p = id0 + q;
     cur.id[p] = p;
-    int mat = mat_in ? mat_in[p] : kSand;
+    int mat = fixed_mat >= 0 ? fixed_mat : (mat_in ? mat_in[q] : kSand);
     cur.mat[p] = (uint8_t)mat;
     if (!has_fp && track_fp)
         for (int k = 0; k < 9; ++k) cur.Fp[k][p] = (k % 4 == 0) ? 1.0f : 0.0f;
@@ -887,17 +1087,20 @@ void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, De
     if (n > 0) k_keys<<<blocks_for(n, 256), 256, 0, s>>>(P, cur, n, keys, st);
 }
 void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
-                const GArrays& G, cudaStream_t s) {
+                const GArrays& G, int32_t* slot_of, int32_t* curidx_of, cudaStream_t s) {
     long hw = (n + kP2GChunk - 1) / kP2GChunk;
-    if (n > 0) k_p2g<<<blocks_for(hw, kP2GThreads / 16), kP2GThreads, 0, s>>>(P, cur, keys, perm, n, G);
+    if (n > 0)
+        k_p2g<<<blocks_for(hw, kP2GThreads / 16), kP2GThreads, 0, s>>>(P, cur, keys, perm, n, G, slot_of, curidx_of);
 }
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s) {
     k_normalize<<<grid_blocks, 256, 0, s>>>(P, G, st);
 }
 void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
-                  const GArrays& G, float dt_force, DevStats* st, cudaStream_t s) {
+                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s) {
     long warps = (n + 31) / 32;
-    if (n > 0) k_force<<<blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s>>>(P, cur, keys, perm, n, G, dt_force, st);
+    if (M.nf > 0) k_cloth_force<<<blocks_for(M.nf, 128), 128, 0, s>>>(P, cur, M, dt_force);
+    if (n > 0)
+        k_force<<<blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s>>>(P, cur, keys, perm, n, G, dt_force, st, M);
 }
 void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
                  int grid_blocks, cudaStream_t s) {
@@ -907,8 +1110,9 @@ void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s) {
     k_grid_clear<<<grid_blocks, 256, 0, s>>>(G);
 }
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
-                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, cudaStream_t s) {
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s) {
     if (n > 0) k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st);
+    if (M.nf > 0) k_cloth_g2p<<<blocks_for(M.nf, 128), 128, 0, s>>>(P, cur, nxt, G, M, dt, keys_next, st);
 }
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s) {
@@ -919,13 +1123,16 @@ void launch_upload(int n, int mode, const double* src, float* const* dst, cudaSt
         k_upload<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, src, dst[0], dst[1], dst[2], dst[3], dst[4], dst[5],
                                                     dst[6], dst[7], dst[8]);
 }
-void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s) {
+void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s, int id_lo,
+                     int id_hi) {
+    if (id_hi < 0) id_hi = n;
     if (n > 0)
         k_download<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, id, dst, src[0], src[1], src[2], src[3], src[4],
-                                                      src[5], src[6], src[7], src[8]);
+                                                      src[5], src[6], src[7], src[8], id_lo, id_hi);
 }
-void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp, cudaStream_t s) {
-    if (n > 0) k_init_particles<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, mat, has_fp, track_fp);
+void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp, cudaStream_t s,
+                           int id0, int fixed_mat) {
+    if (n > 0) k_init_particles<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, mat, has_fp, track_fp, id0, fixed_mat);
 }
 void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s) {
     if (n > 0) k_snow_jp<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, Fp);

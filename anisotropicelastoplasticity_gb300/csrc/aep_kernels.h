@@ -7,21 +7,22 @@ namespace aep {
 
 void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, DevStats* st, cudaStream_t s);
 void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
-                const GArrays& G, cudaStream_t s);
+                const GArrays& G, int32_t* slot_of, int32_t* curidx_of, cudaStream_t s);
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s);
 void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
-                  const GArrays& G, float dt_force, DevStats* st, cudaStream_t s);
+                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s);
 void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
                  int grid_blocks, cudaStream_t s);
 void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s);
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
-                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, cudaStream_t s);
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s);
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s);
 void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s);
-void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s);
+void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s,
+                     int id_lo = 0, int id_hi = -1);
 void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp,
-                           cudaStream_t s);
+                           cudaStream_t s, int id0 = 0, int fixed_mat = -1);
 void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s);
 void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double* vel, double* vbf,
                        int grid_blocks, cudaStream_t s);

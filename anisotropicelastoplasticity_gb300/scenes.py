@@ -14,19 +14,26 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import capi
-from .solver import LevelSet, ParticleSystem, RegularGrid, make_params
+from .solver import LagrangianMesh, LevelSet, ParticleSystem, RegularGrid, make_params
 
 
 @dataclass
 class Scene:
     name: str
     grid: RegularGrid
-    particles: ParticleSystem
+    particles: ParticleSystem | None
     levelset: LevelSet
     params: capi.aep_params
     dt: float
     steps: int
     note: str = ""
+    mesh: LagrangianMesh | None = None
+
+    def num_items(self) -> int:
+        n = len(self.particles) if self.particles is not None else 0
+        if self.mesh is not None:
+            n += len(self.mesh.vertex_positions) + len(self.mesh.faces)
+        return n
 
 
 def _block(rng, n, lo, hi):
@@ -98,4 +105,38 @@ def snow_sand_collision(n: int = 2097152, res: int = 256, seed: int = 3) -> Scen
                  prm, 5e-5, 500)
 
 
-CONFIGS = {0: snow_block, 1: sand_column, 3: snow_sand_collision}
+def sheet(nside: int, side: float, center_xy, height: float, jitter: float, rng):
+    """nside x nside vertex square sheet in the plane z = height, two triangles per quad."""
+    t = np.linspace(-side / 2, side / 2, nside)
+    X, Y = np.meshgrid(center_xy[0] + t, center_xy[1] + t, indexing="ij")
+    V = np.stack([X.ravel(), Y.ravel(), np.full(X.size, height)], axis=1)
+    V += rng.uniform(-jitter, jitter, V.shape)
+    idx = np.arange(nside * nside).reshape(nside, nside)
+    a, b, c, d = idx[:-1, :-1].ravel(), idx[1:, :-1].ravel(), idx[1:, 1:].ravel(), idx[:-1, 1:].ravel()
+    F = np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)]).astype(np.int32)
+    return V, F
+
+
+def cloth_drape(nside: int = 256, res: int = 128, seed: int = 2, shear_stiffness: float = 1e3) -> Scene:
+    """Cloth drape: a 256x256-vertex square sheet (65,536 vertices, 130,050 triangles) of
+    side 0.6, flat at height 0.7, vertex positions jittered +-1e-4 (seed 2); in-plane
+    E=1e4, nu=0.3, normal stiffness 1e3, frictional cap 0.3, mass 0.2 per unit area;
+    sphere r=0.2 at (0.5, 0.5, 0.4) plus the ground; grid 128^3, dt=2e-5, 2000 steps."""
+    rng = np.random.default_rng(seed)
+    V, F = sheet(nside, 0.6, (0.5, 0.5), 0.7, 1e-4, rng)
+    thickness = 1.0 / res
+    mesh = LagrangianMesh.from_triangles(V, F, density=0.2 / thickness, thickness=thickness, youngs_modulus=1e4,
+                                         poisson_ratio=0.3, shear_stiffness=shear_stiffness, stiffness=1e3,
+                                         friction_coeff=0.3)
+    ls = LevelSet.sphere([0.5, 0.5, 0.4], 0.2) | LevelSet.ground(0.05)
+    # The reference's in-plane vertex forces carry no element volume
+    # (LagrangianMesh.cpp:452-458); with E = 1e4 on this mesh they would be ~1e6 times
+    # too stiff for dt = 2e-5, so this scene weights them by the element volume.
+    prm = make_params(cloth_volume_weighting=1)
+    return Scene("cloth_drape", RegularGrid([0, 0, 0], [1, 1, 1], [res] * 3), None, ls, prm, 2e-5, 2000,
+                 f"thickness {thickness:g} (density x thickness = 0.2 per area); shear stiffness "
+                 f"{shear_stiffness:g} (not given by the configuration); in-plane forces weighted by the "
+                 f"element volume", mesh)
+
+
+CONFIGS = {0: snow_block, 1: sand_column, 2: cloth_drape, 3: snow_sand_collision}

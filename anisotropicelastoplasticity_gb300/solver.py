@@ -135,6 +135,80 @@ class ParticleSystem:
                                  for k, v in self.__dict__.items()})
 
 
+def dirs_to_ref(D: np.ndarray) -> np.ndarray:
+    """(Nf, 3, 3) with columns d1 d2 d3 -> elementDirections_1 | _2 | _3 memory."""
+    return np.ascontiguousarray(np.asarray(D, dtype=np.float64).transpose(2, 1, 0))
+
+
+def dirs_from_ref(buf: np.ndarray, nf: int) -> np.ndarray:
+    return buf.reshape(3, 3, nf).transpose(2, 1, 0).copy()
+
+
+@dataclass
+class LagrangianMesh:
+    """Public members of LagrangianMesh (LagrangianMesh.h:37-73): one MPM particle per
+    vertex and one per triangle; element directions as (Nf, 3, 3) with columns d1 d2 d3."""
+
+    vertex_positions: np.ndarray
+    faces: np.ndarray
+    vertex_masses: np.ndarray
+    vertex_volumes: np.ndarray
+    element_masses: np.ndarray
+    element_volumes: np.ndarray
+    element_directions: np.ndarray
+    element_rest_directions: np.ndarray
+    mu: float
+    lambda_: float
+    shear_stiffness: float
+    stiffness: float
+    friction_coeff: float
+    vertex_velocities: np.ndarray | None = None
+    element_velocities: np.ndarray | None = None
+
+    def __post_init__(self):
+        nv, nf = len(self.vertex_positions), len(self.faces)
+        self.vertex_positions = np.asarray(self.vertex_positions, np.float64).reshape(nv, 3)
+        self.faces = np.asarray(self.faces, np.int32).reshape(nf, 3)
+        if self.vertex_velocities is None:
+            self.vertex_velocities = np.zeros((nv, 3))
+        if self.element_velocities is None:
+            self.element_velocities = np.zeros((nf, 3))
+
+    @property
+    def element_positions(self) -> np.ndarray:  # updateElementPositions (LagrangianMesh.cpp:371-380)
+        return self.vertex_positions[self.faces].mean(axis=1)
+
+    @staticmethod
+    def from_triangles(V, F, density, thickness, youngs_modulus, poisson_ratio, shear_stiffness, stiffness,
+                       friction_coeff) -> "LagrangianMesh":
+        """Mass, volume and rest-direction rules of LagrangianMesh::ObjMesh
+        (LagrangianMesh.cpp:306-351) for an in-memory triangle mesh with int32 indices;
+        friction_coeff is the cap coefficient itself (ObjMesh takes tan of an angle)."""
+        V = np.asarray(V, np.float64)
+        F = np.asarray(F, np.int32)
+        v1, v2, v3 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+        a = np.linalg.norm(v2 - v1, axis=1)
+        b = np.linalg.norm(v3 - v2, axis=1)
+        c = np.linalg.norm(v1 - v3, axis=1)
+        p = 0.5 * (a + b + c)
+        area = np.sqrt(p * (p - a) * (p - b) * (p - c))  # triangleArea (geometry.cpp:13-23)
+        evol = 0.25 * area * thickness
+        vvol = np.zeros(len(V))
+        for k in range(3):
+            np.add.at(vvol, F[:, k], evol)
+        nrm = np.cross(v2 - v1, v3 - v1)
+        nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+        D = np.stack([v2 - v1, v3 - v1, nrm], axis=2)
+        lam = youngs_modulus * poisson_ratio / (1 + poisson_ratio) / (1 - 2 * poisson_ratio)
+        mu = youngs_modulus / 2 / (1 + poisson_ratio)
+        return LagrangianMesh(V, F, density * vvol, vvol, density * evol, evol, D.copy(), D.copy(), mu, lam,
+                              shear_stiffness, stiffness, friction_coeff)
+
+    def copy(self) -> "LagrangianMesh":
+        import copy as _c
+        return _c.deepcopy(self)
+
+
 @dataclass
 class LevelSet:
     """Union of analytic level sets (LevelSet.cpp:8-42): phi = min over shapes."""
@@ -202,6 +276,7 @@ class HybridSolver:
         self._lib = capi.load()
         self._h = C.c_void_p()
         self.ps = None
+        self.mesh = None
         self.rg = rg
         self.params = params if params is not None else capi.default_params()
         if rg is not None:
@@ -254,6 +329,31 @@ class HybridSolver:
         self._check(self._lib.aep_set_particles(self._h, n, _dp(x), _dp(v), _dp(B), _dp(Fe), _dp(Fp), _dp(m),
                                                 _dp(vol), _dp(q), mat.ctypes.data_as(C.POINTER(C.c_uint8))))
 
+    def set_lagrangian_mesh(self, mesh: LagrangianMesh):
+        """setLagrangianMesh (HybridSolver.h:88); call after set_particle_system, before stepping."""
+        self.mesh = mesh
+        nv, nf = len(mesh.vertex_positions), len(mesh.faces)
+        xv = vec_to_ref(mesh.vertex_positions)
+        faces = np.ascontiguousarray(mesh.faces.T, dtype=np.int32)
+        vv, ve = vec_to_ref(mesh.vertex_velocities), vec_to_ref(mesh.element_velocities)
+        mv, volv = (np.ascontiguousarray(a, np.float64) for a in (mesh.vertex_masses, mesh.vertex_volumes))
+        me, vole = (np.ascontiguousarray(a, np.float64) for a in (mesh.element_masses, mesh.element_volumes))
+        d, dr = dirs_to_ref(mesh.element_directions), dirs_to_ref(mesh.element_rest_directions)
+        self._check(self._lib.aep_set_mesh(self._h, nv, nf, _dp(xv), faces.ctypes.data_as(C.POINTER(C.c_int32)),
+                                           _dp(vv), _dp(ve), _dp(mv), _dp(volv), _dp(me), _dp(vole), _dp(d),
+                                           _dp(dr), mesh.mu, mesh.lambda_, mesh.shear_stiffness, mesh.stiffness,
+                                           mesh.friction_coeff))
+
+    def get_mesh(self) -> dict:
+        nv, nf = len(self.mesh.vertex_positions), len(self.mesh.faces)
+        xv, vv, xe, ve = np.empty(3 * nv), np.empty(3 * nv), np.empty(3 * nf), np.empty(3 * nf)
+        Bv, Be, d = np.empty(9 * nv), np.empty(9 * nf), np.empty(9 * nf)
+        self._check(self._lib.aep_get_mesh(self._h, _dp(xv), _dp(vv), _dp(Bv), _dp(xe), _dp(ve), _dp(Be), _dp(d)))
+        return dict(vertex_positions=vec_from_ref(xv, nv), vertex_velocities=vec_from_ref(vv, nv),
+                    vertex_affine_momenta=rows_from_ref(Bv, nv), element_positions=vec_from_ref(xe, nf),
+                    element_velocities=vec_from_ref(ve, nf), element_affine_momenta=rows_from_ref(Be, nf),
+                    element_directions=dirs_from_ref(d, nf))
+
     def set_level_set(self, ls: LevelSet):
         arr, n = ls.to_c()
         self._check(self._lib.aep_set_levelset(self._h, arr, n))
@@ -274,7 +374,7 @@ class HybridSolver:
 
     # --- readback -----------------------------------------------------------------
     def get_particles(self, want_fp: bool = False) -> dict:
-        n = len(self.ps)
+        n = len(self.ps) if self.ps is not None else 0
         x, v = np.empty(3 * n), np.empty(3 * n)
         B, Fe = np.empty(9 * n), np.empty(9 * n)
         Fp = np.empty(9 * n) if want_fp else None

@@ -52,6 +52,9 @@ typedef enum aep_status {
  * whole system, HybridSolver.h:21-25 and HybridSolver.cpp:873,955,959; here
  * the tag is per particle). */
 enum { AEP_SNOW = 0, AEP_SAND = 1 };
+/* Tags of the LagrangianMesh vertices and elements inside the solver (set by
+ * aep_set_mesh; not accepted by aep_set_particles). */
+enum { AEP_CLOTH_VERTEX = 2, AEP_CLOTH_ELEMENT = 3 };
 
 /* Level-set shapes (replaces the LevelSet/DLevelSet std::function pair,
  * HybridSolver.h:18-19, LevelSet.cpp:8-42).  Several shapes are unioned:
@@ -109,7 +112,12 @@ typedef struct aep_params {
                                 relative to the heaviest particle (default 34)         */
     int32_t momentum_bits;   /* same for momentum and force impulse, relative to
                                 (heaviest particle mass) x (1 m/s)   (default 40)      */
-    int64_t reserved[8];
+    double mesh_damp;        /* APIC damping of cloth vertices/elements, reference 1 (HS:926,932) */
+    int32_t cloth_volume_weighting; /* 0: in-plane vertex forces as the reference computes
+                                       them, without the element volume (LagrangianMesh.cpp:
+                                       452-458); 1: multiplied by the element volume        */
+    int32_t reserved_i;
+    int64_t reserved[6];
 } aep_params;
 
 /* Counters of the last step (all zero until a step ran). */
@@ -154,6 +162,30 @@ aep_status aep_set_particles(aep_solver* s, int64_t n,
                              const double* Fe, const double* Fp,
                              const double* m, const double* vol,
                              const double* plastic, const uint8_t* material);
+
+/* Replaces the LagrangianMesh constructor + HybridSolver::setLagrangianMesh
+ * (LagrangianMesh.cpp:127-195, HybridSolver.h:88).  Vertices and elements (one
+ * per triangle) become MPM particles.  xv: Nv x 3 column-major; faces: Nf x 3
+ * column-major int32 (0-based vertex indices); vv (Nv x 3), ve (Nf x 3) may be
+ * NULL; mv, volv (Nv); me, vole (Nf), volv may be NULL; d, drest: element
+ * directions d1 | d2 | d3 and rest directions, each Nf x 3 column-major (9Nf);
+ * mu, lambda: in-plane Lame parameters; shear_stiffness, stiffness: the shear
+ * and normal stiffness of the normal-direction response; friction_coeff: the
+ * frictional cap of the cloth return mapping.  Element positions start at the
+ * centroids of their vertices.  Call after aep_set_particles (or without
+ * particles) and before the first step; aep_set_particles removes the mesh.    */
+aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv, const int32_t* faces,
+                        const double* vv, const double* ve, const double* mv, const double* volv,
+                        const double* me, const double* vole, const double* d, const double* drest,
+                        double mu, double lambda, double shear_stiffness, double stiffness,
+                        double friction_coeff);
+
+/* Replaces reading LagrangianMesh's public members (LagrangianMesh.h:37-61):
+ * vertex positions/velocities/affine momenta, element positions/velocities/
+ * affine momenta and element directions, in the layouts of aep_set_mesh; any
+ * pointer may be NULL.                                                          */
+aep_status aep_get_mesh(aep_solver* s, double* xv, double* vv, double* Bv, double* xe,
+                        double* ve, double* Be, double* d);
 
 /* Replaces HybridSolver::setLevelSet(phi, dphi) (HybridSolver.h:89). */
 aep_status aep_set_levelset(aep_solver* s, const aep_sdf* shapes, int32_t n);

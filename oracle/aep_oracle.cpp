@@ -522,9 +522,12 @@ void vertex_inplane_forces(Oracle& o, std::vector<V3>& fv) {
         double dr11 = Pk[0], dr12 = Pk[2], dr22 = Pk[3];
         V3 q1{E(Q, 0, 0), E(Q, 1, 0), E(Q, 2, 0)}, q2{E(Q, 0, 1), E(Q, 1, 1), E(Q, 2, 1)};
         V3 f2, f3, f1;
+        // the reference does not weight these forces by the element volume; the
+        // cloth_volume_weighting parameter (off by default) does
+        double fw = o.prm.cloth_volume_weighting ? me.vole[f] : 1.0;
         for (int r = 0; r < 3; ++r) {
-            f2[r] = -(dr11 * i11 + dr12 * i12) * q1[r];
-            f3[r] = -dr12 * i22 * q1[r] - dr22 * i22 * q2[r];
+            f2[r] = -(dr11 * i11 + dr12 * i12) * q1[r] * fw;
+            f3[r] = (-dr12 * i22 * q1[r] - dr22 * i22 * q2[r]) * fw;
             f1[r] = -(f2[r] + f3[r]);
         }
         fe[f] = {f1, f2, f3};

@@ -14,8 +14,8 @@ import ctypes as C
 import numpy as np
 
 from anisotropicelastoplasticity_gb300 import capi
-from anisotropicelastoplasticity_gb300.solver import (mats_from_ref, mats_to_ref, rows_from_ref, rows_to_ref,
-                                                      vec_from_ref, vec_to_ref)
+from anisotropicelastoplasticity_gb300.solver import (dirs_from_ref, dirs_to_ref, mats_from_ref, mats_to_ref,
+                                                      rows_from_ref, rows_to_ref, vec_from_ref, vec_to_ref)
 
 from . import build as _build
 
@@ -94,6 +94,29 @@ class Oracle:
     def set_level_set(self, ls):
         arr, n = ls.to_c()
         self.lib.orc_set_levelset(self.h, arr, n)
+
+    def set_lagrangian_mesh(self, mesh):
+        self.mesh = mesh
+        nv, nf = len(mesh.vertex_positions), len(mesh.faces)
+        arrs = [vec_to_ref(mesh.vertex_positions), np.ascontiguousarray(mesh.faces.T, np.int32),
+                vec_to_ref(mesh.vertex_velocities), vec_to_ref(mesh.element_velocities),
+                np.ascontiguousarray(mesh.vertex_masses, float), np.ascontiguousarray(mesh.vertex_volumes, float),
+                np.ascontiguousarray(mesh.element_masses, float), np.ascontiguousarray(mesh.element_volumes, float),
+                dirs_to_ref(mesh.element_directions), dirs_to_ref(mesh.element_rest_directions)]
+        self._keep_mesh = arrs
+        self.lib.orc_set_mesh(self.h, nv, nf, _p(arrs[0]), arrs[1].ctypes.data_as(C.POINTER(C.c_int32)),
+                              *[_p(a) for a in arrs[2:]], mesh.mu, mesh.lambda_, mesh.shear_stiffness,
+                              mesh.stiffness, mesh.friction_coeff)
+
+    def get_mesh(self) -> dict:
+        nv, nf = len(self.mesh.vertex_positions), len(self.mesh.faces)
+        xv, vv, xe, ve = np.empty(3 * nv), np.empty(3 * nv), np.empty(3 * nf), np.empty(3 * nf)
+        Bv, Be, d = np.empty(9 * nv), np.empty(9 * nf), np.empty(9 * nf)
+        self.lib.orc_get_mesh(self.h, _p(xv), _p(vv), _p(Bv), _p(xe), _p(ve), _p(Be), _p(d))
+        return dict(vertex_positions=vec_from_ref(xv, nv), vertex_velocities=vec_from_ref(vv, nv),
+                    vertex_affine_momenta=rows_from_ref(Bv, nv), element_positions=vec_from_ref(xe, nf),
+                    element_velocities=vec_from_ref(ve, nf), element_affine_momenta=rows_from_ref(Be, nf),
+                    element_directions=dirs_from_ref(d, nf))
 
     def init(self, volumes: bool = True):
         """weights + first P2G of solve (HybridSolver.cpp:829-855)."""
