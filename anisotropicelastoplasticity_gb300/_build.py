@@ -16,7 +16,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libaep.so"
-SOURCES = ["aep_kernels.cu", "aep_sort.cu", "aep_capi.cu", "aep_noalloc.cu"]
+SOURCES = ["aep_kernels.cu", "aep_sort.cu", "aep_capi.cu", "aep_noalloc.cu", "aep_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -89,7 +89,9 @@ class aep_stats(C.Structure):
         ("active_nodes", C.c_int64),
         ("total_mass", C.c_double),
         ("total_momentum", C.c_double * 3),
-        ("reserved", C.c_double * 7),
+        ("learned_accepted", C.c_int64),
+        ("learned_fallbacks", C.c_int64),
+        ("reserved", C.c_double * 5),
     ]
 
 
@@ -121,7 +123,21 @@ SIGNATURES = {
     "aep_p2g_noalloc": (C.c_int, [C.POINTER(aep_grid_desc), C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
     "aep_last_error": (C.c_char_p, [_solver_p]),
+    "aep_mlp_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    "aep_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "aep_mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
+    "aep_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
+    "aep_mlp_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "aep_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_double, C.c_double,
+                                C.POINTER(C.c_double), C.c_void_p]),
+    "aep_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "aep_mlp_last_error": (C.c_char_p, [C.c_void_p]),
+    "aep_set_harvest": (C.c_int, [_solver_p, C.c_void_p, C.c_int64, C.c_int32]),
+    "aep_get_harvest_count": (C.c_int, [_solver_p, C.POINTER(C.c_int64)]),
+    "aep_set_return_map": (C.c_int, [_solver_p, C.c_void_p, C.c_double]),
 }
+
+AEP_MLP_NUM_PARAMS = 9928
 
 PHASES = ["sort", "p2g", "normalize", "force", "grid", "g2p"]
 

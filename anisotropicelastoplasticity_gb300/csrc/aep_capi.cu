@@ -42,6 +42,13 @@ struct aep_solver {
     int32_t* slot_of = nullptr;
     int32_t* curidx_of = nullptr;
     double cloth[5] = {0, 0, 0, 0, 0};  // mu, lambda, shear, stiffness, friction
+    // training-pair harvest and learned return map
+    float* harvest = nullptr;
+    unsigned long long* harvest_count = nullptr;
+    int64_t harvest_cap = 0;
+    int32_t harvest_stride = 1;
+    const aep_mlp* mlp = nullptr;
+    double learned_tol = 1e-4;
     ParticleSet set[2];
     PArrays P[2];
     int cur = 0;
@@ -428,6 +435,7 @@ aep_status aep_solver_destroy(aep_solver* s) {
     cudaFree(s->G.nactive);
     cudaFree(s->dstats);
     cudaFree(s->dforce);
+    cudaFree(s->harvest_count);
     for (int r = 0; r < aep_solver::kRing; ++r)
         for (int p = 0; p <= AEP_NUM_PHASES; ++p)
             if (s->ev[r][p]) cudaEventDestroy(s->ev[r][p]);
@@ -723,7 +731,11 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
     if (stage == AEP_STAGE_GRID) return AEP_OK;
     if (timed) mark(s, AEP_PHASE_G2P);
     const int nx = 1 - s->cur;
-    launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, dtf, s->keys, s->dstats, M, s->stream);
+    Harvest H{s->harvest, s->harvest_count, s->harvest_cap, s->harvest_stride};
+    MlpParams mp{};
+    if (s->mlp) mp = mlp_device_params(s->mlp);
+    launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, dtf, s->keys, s->dstats, M, s->stream, H,
+               s->mlp ? &mp : nullptr, (float)s->learned_tol);
     CKLAUNCH();
     if (timed) {
         mark(s, AEP_NUM_PHASES);
@@ -809,9 +821,41 @@ aep_status aep_get_stats(aep_solver* s, aep_stats* out) {
     out->fp64_fallbacks = (int64_t)h.fallbacks;
     out->overflow = (int64_t)h.overflow;
     out->active_nodes = (int64_t)h.nodes;
+    out->learned_accepted = (int64_t)h.learned_ok;
+    out->learned_fallbacks = (int64_t)h.learned_rejected;
     double im = std::ldexp(s->m_max, -s->prm.mass_bits), ip = std::ldexp(s->m_max, -s->prm.momentum_bits);
     out->total_mass = (double)(long long)h.mass * im;
     for (int a = 0; a < 3; ++a) out->total_momentum[a] = (double)(long long)h.mom[a] * ip;
+    return AEP_OK;
+}
+
+aep_status aep_set_harvest(aep_solver* s, float* d_records, int64_t capacity, int32_t stride) {
+    if (!s) return AEP_INVALID_ARG;
+    if (d_records && (capacity <= 0 || stride < 1))
+        return fail(s, AEP_INVALID_ARG, "aep_set_harvest: capacity > 0, stride >= 1");
+    CK(cudaStreamSynchronize(s->stream));
+    s->harvest = d_records;
+    s->harvest_cap = d_records ? capacity : 0;
+    s->harvest_stride = stride < 1 ? 1 : stride;
+    if (!s->harvest_count) CK(cudaMalloc(&s->harvest_count, sizeof(unsigned long long)));
+    CK(cudaMemset(s->harvest_count, 0, sizeof(unsigned long long)));
+    return AEP_OK;
+}
+
+aep_status aep_get_harvest_count(aep_solver* s, int64_t* count) {
+    if (!s || !count) return AEP_INVALID_ARG;
+    CK(cudaStreamSynchronize(s->stream));
+    unsigned long long c = 0;
+    if (s->harvest_count) CK(cudaMemcpy(&c, s->harvest_count, sizeof(c), cudaMemcpyDeviceToHost));
+    *count = (int64_t)std::min<unsigned long long>(c, (unsigned long long)s->harvest_cap);
+    return AEP_OK;
+}
+
+aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance) {
+    if (!s) return AEP_INVALID_ARG;
+    if (m && !(tolerance >= 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_return_map: tolerance >= 0");
+    s->mlp = m;
+    s->learned_tol = tolerance;
     return AEP_OK;
 }
 

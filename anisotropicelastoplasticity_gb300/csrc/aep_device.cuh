@@ -98,6 +98,17 @@ struct DevStats {
     unsigned long long mass;       // int64 sums, exact
     unsigned long long mom[3];
     unsigned long long nodes;      // nodes with mass after P2G
+    unsigned long long learned_ok;      // learned return maps accepted
+    unsigned long long learned_rejected;  // learned outputs replaced by the exact mapping
+};
+
+// Training-pair harvest from the exact return mapping (plain G2P): records of 8
+// floats [ln s trial sorted desc (3), q, material, ln s_new - ln s trial (3)].
+struct Harvest {
+    float* buf;
+    unsigned long long* count;
+    long long capacity;
+    int stride;  // every stride-th particle slot
 };
 
 // ---------------------------------------------------------------------------------

@@ -24,6 +24,7 @@
 // batch of 16 particles.
 #include "aep_device.cuh"
 #include "aep_kernels.h"
+#include "aep_mlp.cuh"
 
 namespace aep {
 
@@ -718,9 +719,24 @@ __device__ __forceinline__ void apic_damp(const float C[9], float damp, float Bn
 }
 
 // G2P + APIC + advection + F update + return mapping, one thread per particle
+__device__ __forceinline__ void harvest_record(const Harvest& H, int mat, const float s_tr[3], const float s_new[3],
+                                               float q_old) {
+    const unsigned long long slot = atomicAdd(H.count, 1ull);
+    if ((long long)slot >= H.capacity) return;
+    float ln[3] = {logf(s_tr[0]), logf(s_tr[1]), logf(s_tr[2])}, srt[3];
+    int pm[3];
+    sort3_desc(ln, srt, pm);
+    float* r = H.buf + 8ull * slot;
+    r[0] = srt[0]; r[1] = srt[1]; r[2] = srt[2];
+    r[3] = q_old;
+    r[4] = (float)mat;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[5 + k] = logf(s_new[pm[k]]) - srt[k];
+}
+
 __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
                                              int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
-                                             DevStats* st) {
+                                             DevStats* st, Harvest H) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const int pj = perm[j];
@@ -802,7 +818,9 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
     bool ok = svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
     if (ok) {
         sn[0] = s[0]; sn[1] = s[1]; sn[2] = s[2];
+        const float q_old = q;
         return_map<float>(P, mat, sn, q);
+        if (H.buf && (j % H.stride) == 0) harvest_record(H, mat, s, sn, q_old);
         sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
         float US[9];
 #pragma unroll
@@ -876,6 +894,210 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
     int ncell[3];
     float nf[3];
     bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nf);
+    keys_next[j] = make_key(P, ncell);
+    if (clamped) atomicAdd(&st->out_of_domain, 1ull);
+}
+
+// ===================================================================================
+// G2P with the learned return map: as k_g2p, but the singular-value return mapping
+// of snow and sand particles is predicted by the MLP (aep_mlp.cuh) on the tensor
+// cores, 32 particles per warp.  Each prediction is checked in the kernel against
+// the exact mapping (HybridSolver.cpp:626-674): if any projected log singular value
+// differs by more than `tol`, the exact value is used instead and counted as a
+// fallback.  No lane leaves before the warp-wide MLP call.
+__global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PArrays nxt,
+                                                     const int32_t* __restrict__ perm, int n, GArrays G, float dt,
+                                                     uint32_t* __restrict__ keys_next, DevStats* st, MlpParams mlp,
+                                                     float tol) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const MlpSmem W = mlp_smem_carve(smem_raw);
+    mlp_load_smem(mlp, W, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* wbase = smem_raw + kMlpSmemBytes + warp * kMlpWarpBytes;
+    __nv_bfloat16* MX = reinterpret_cast<__nv_bfloat16*>(wbase);
+    __nv_bfloat16* MH0 = MX + kMlpWarpX;
+    __nv_bfloat16* MH1 = MH0 + kMlpWarpH;
+    float* MY = reinterpret_cast<float*>(MH1 + kMlpWarpH);
+
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = j < n;
+    const int pj = live ? perm[j] : 0;
+    const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
+    const bool active = live && mat != kClothElement;
+    const bool rm = active && mat <= kSand;
+    float xn[3] = {0, 0, 0}, vp[3] = {0, 0, 0}, Bn[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Ftr[9];
+    float U[9], s[3] = {1, 1, 1}, V[9];
+    bool ok = false;
+    float q = 0.0f;
+    if (active) {
+        float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
+        int cell[3];
+        float f[3], w[3][4], dw[3][4];
+        locate(P, xp[0], xp[1], xp[2], cell, f);
+        const bool truncated = particle_weights(P, cell, f, w, dw);
+        int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+        uint32_t X[4], Y[4], Z[4];
+        stencil_offsets(P, base, X, Y, Z);
+        float xi[3][4];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
+        float xs[3], C[9], Gb[9];
+        g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) xn[a] = xp[a] + dt * xs[a];
+        if (truncated) {
+            float s0[3], s1[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                s0[a] = w[a][0] + w[a][1] + w[a][2] + w[a][3];
+                s1[a] = w[a][0] * xi[a][0] + w[a][1] * xi[a][1] + w[a][2] * xi[a][2] + w[a][3] * xi[a][3];
+            }
+            const float sw = s0[0] * s0[1] * s0[2];
+            const float swx[3] = {s1[0] * s0[1] * s0[2], s0[0] * s1[1] * s0[2], s0[0] * s0[1] * s1[2]};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) xn[a] += xp[a] * (sw - 1.0f) + swx[a];
+        }
+        apic_damp(C, mat == kClothVertex ? P.mesh_damp : P.particle_damp, Bn);
+        if (rm) {
+            float F[9], GF[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
+            mat_mul(Gb, F, GF);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
+            q = cur.plastic[pj];
+            ok = svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
+        }
+    }
+    // features: sorted trial log singular values (zero rows for lanes without a map)
+    float lns[3] = {0, 0, 0}, srt[3] = {0, 0, 0};
+    int pm[3] = {0, 1, 2};
+    if (rm && ok) {
+        lns[0] = logf(s[0]); lns[1] = logf(s[1]); lns[2] = logf(s[2]);
+        sort3_desc(lns, srt, pm);
+    }
+    mlp_features(srt, q, (rm && ok) ? mat : 0, MX + lane * kStrideIn);
+    mlp_forward_warp(W, MX, MH0, MH1, MY, lane);
+
+    if (!active) return;
+    if (mat == kClothVertex) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            nxt.x[a][j] = xn[a];
+            nxt.v[a][j] = vp[a];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            nxt.B[k][j] = Bn[k];
+            nxt.F[k][j] = cur.F[k][pj];
+        }
+        nxt.plastic[j] = cur.plastic[pj];
+    } else {
+        float Fe[9], sn[3], sprod = 1.0f;
+        double Ud[9], sd[3], Vd[9];
+        bool used_fp64 = false;
+        if (ok) {
+            // exact mapping (the check) and the prediction, both in sorted order
+            float ex[3] = {s[0], s[1], s[2]};
+            float qe = q;
+            return_map<float>(P, mat, ex, qe);
+            float pred_ln[3];
+            bool accept = true;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int src = pm[k];
+                pred_ln[src] = srt[k] + MY[lane * kMlpOut + k] / kLnScale;
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) accept = accept && fabsf(pred_ln[a] - logf(ex[a])) <= tol;
+            if (accept) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) sn[a] = expf(pred_ln[a]);
+                if (mat == kSand && qe != q) {  // plastic: q grows by the projection distance
+                    const float d0 = pred_ln[0] - lns[0], d1 = pred_ln[1] - lns[1], d2 = pred_ln[2] - lns[2];
+                    q += sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+                }
+                atomicAdd(&st->learned_ok, 1ull);
+            } else {
+                sn[0] = ex[0]; sn[1] = ex[1]; sn[2] = ex[2];
+                q = qe;
+                atomicAdd(&st->learned_rejected, 1ull);
+            }
+            sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
+            float US[9];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) US[3 * r + c] = U[3 * r + c] * sn[c];
+            mat_mul_bt(US, V, Fe);
+        } else {
+            used_fp64 = true;
+            double Fd[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Fd[k] = Ftr[k];
+            svd3<double>(Fd, Ud, sd, Vd, 40, 1e-15, 0.0);
+            svd3_complete(Ud, sd);
+            double s0[3] = {sd[0], sd[1], sd[2]};
+            double qd = q;
+            return_map<double>(P, mat, sd, qd);
+            q = (float)qd;
+            sprod = (float)((s0[0] / sd[0]) * (s0[1] / sd[1]) * (s0[2] / sd[2]));
+            double US[9], Fed[9];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) US[3 * r + c] = Ud[3 * r + c] * sd[c];
+            mat_mul_bt(US, Vd, Fed);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Fe[k] = (float)Fed[k];
+            atomicAdd(&st->fallbacks, 1ull);
+        }
+        if (P.track_fp) {
+            float Fp[9], Ft[9], M[9], Fpn[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
+            mat_mul(Ftr, Fp, Ft);
+            if (!used_fp64) {
+                float VS[9];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) VS[3 * r + c] = V[3 * r + c] / sn[c];
+                mat_mul_bt(VS, U, M);
+            } else {
+                double VSd[9], Md[9];
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c) VSd[3 * r + c] = Vd[3 * r + c] / sd[c];
+                mat_mul_bt(VSd, Ud, Md);
+                for (int k = 0; k < 9; ++k) M[k] = (float)Md[k];
+            }
+            mat_mul(M, Ft, Fpn);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = Fpn[k];
+            if (mat == kSnow) q = mat_det(Fpn);
+        } else if (mat == kSnow) {
+            q *= sprod;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            nxt.x[a][j] = xn[a];
+            nxt.v[a][j] = vp[a];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            nxt.B[k][j] = Bn[k];
+            nxt.F[k][j] = Fe[k];
+        }
+        nxt.plastic[j] = q;
+    }
+    nxt.mat[j] = (uint8_t)mat;
+    nxt.m[j] = cur.m[pj];
+    nxt.vol[j] = cur.vol[pj];
+    nxt.id[j] = cur.id[pj];
+    int ncell[3];
+    float nf[3];
+    const bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nf);
     keys_next[j] = make_key(P, ncell);
     if (clamped) atomicAdd(&st->out_of_domain, 1ull);
 }
@@ -1110,8 +1332,18 @@ void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s) {
     k_grid_clear<<<grid_blocks, 256, 0, s>>>(G);
 }
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
-                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s) {
-    if (n > 0) k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st);
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s,
+                const Harvest& H, const MlpParams* mlp, float learned_tol) {
+    if (n > 0) {
+        if (mlp) {
+            const int smem = kMlpSmemBytes + 4 * kMlpWarpBytes;
+            cudaFuncSetAttribute(k_g2p_learned, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            k_g2p_learned<<<blocks_for(n, 128), 128, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp,
+                                                               learned_tol);
+        } else {
+            k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H);
+        }
+    }
     if (M.nf > 0) k_cloth_g2p<<<blocks_for(M.nf, 128), 128, 0, s>>>(P, cur, nxt, G, M, dt, keys_next, st);
 }
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,

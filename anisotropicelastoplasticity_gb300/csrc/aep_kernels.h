@@ -1,7 +1,9 @@
 // aep_kernels.h -- host launchers of the kernels in aep_kernels.cu.
 #pragma once
 
+#include "../../include/aep.h"
 #include "aep_device.cuh"
+#include "aep_mlp.cuh"
 
 namespace aep {
 
@@ -15,7 +17,8 @@ void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_f
                  int grid_blocks, cudaStream_t s);
 void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s);
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
-                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s);
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s,
+                const Harvest& H, const MlpParams* mlp, float learned_tol);
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s);
 void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s);
@@ -26,6 +29,9 @@ void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int ha
 void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s);
 void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double* vel, double* vbf,
                        int grid_blocks, cudaStream_t s);
+
+// device view of a trained MLP (aep_mlp.cu)
+MlpParams mlp_device_params(const aep_mlp* m);
 
 // radix sort of (key, index) pairs; implemented with CUB in aep_sort.cu
 size_t sort_temp_bytes(int n, int key_bits);

@@ -410,6 +410,21 @@ class HybridSolver:
         return dict(masses=m, velocities=vec_from_ref(v, ng), velocities_before_friction=vec_from_ref(vbf, ng),
                     forces=vec_from_ref(f, ng))
 
+    def set_harvest(self, records_ptr: int | None, capacity: int = 0, stride: int = 1):
+        """Collect (trial, projected) records from the exact return mapping of later steps
+        into a caller-owned device buffer of `capacity` x 8 float32 (None stops)."""
+        self._check(self._lib.aep_set_harvest(self._h, C.c_void_p(records_ptr or 0), int(capacity), int(stride)))
+
+    def harvest_count(self) -> int:
+        cnt = C.c_int64()
+        self._check(self._lib.aep_get_harvest_count(self._h, C.byref(cnt)))
+        return cnt.value
+
+    def set_return_map(self, mlp=None, tolerance: float = 1e-4):
+        """Use a trained ReturnMapMLP (None: the exact mapping of the reference)."""
+        self._mlp_ref = mlp
+        self._check(self._lib.aep_set_return_map(self._h, mlp.handle if mlp is not None else None, tolerance))
+
     def set_stream(self, cuda_stream_ptr: int | None):
         """Order the solver's work on an external cudaStream_t (e.g. torch.cuda.Stream.cuda_stream)."""
         self._check(self._lib.aep_set_stream(self._h, C.c_void_p(cuda_stream_ptr or 0)))
@@ -429,5 +444,6 @@ class HybridSolver:
         self._check(self._lib.aep_get_stats(self._h, C.byref(s)))
         return dict(steps=s.steps, num_particles=s.num_particles, active_blocks=s.active_blocks,
                     out_of_domain=s.out_of_domain, fp64_fallbacks=s.fp64_fallbacks, overflow=s.overflow,
-                    active_nodes=s.active_nodes,
+                    active_nodes=s.active_nodes, learned_accepted=s.learned_accepted,
+                    learned_fallbacks=s.learned_fallbacks,
                     total_mass=s.total_mass, total_momentum=list(s.total_momentum))

@@ -131,7 +131,9 @@ typedef struct aep_stats {
     int64_t active_nodes;       /* grid nodes with mass after the last P2G               */
     double total_mass;          /* grid mass after the last P2G (exact fixed-point sum)  */
     double total_momentum[3];   /* grid momentum after the last P2G                      */
-    double reserved[7];
+    int64_t learned_accepted;   /* learned return maps used in the last step             */
+    int64_t learned_fallbacks;  /* learned outputs replaced by the exact mapping         */
+    double reserved[5];
 } aep_stats;
 
 /* ---- version / defaults ------------------------------------------------------- */
@@ -267,6 +269,48 @@ aep_status aep_set_profiling(aep_solver* s, int32_t on);
 /* Accumulated milliseconds per phase since profiling was enabled, and the
  * number of timed steps.  Synchronises the handle's stream.                  */
 aep_status aep_get_phase_times(aep_solver* s, double ms[AEP_NUM_PHASES], int64_t* steps);
+
+/* ---- learned return map ----------------------------------------------------------- */
+
+/* No counterpart in the reference.  A small MLP (6 -> 64 -> 64 -> 64 -> 3, SiLU,
+ * BF16 weights on the tensor cores, FP32 accumulation) that maps the trial log
+ * singular values (sorted, descending), the sand plastic amount and the material
+ * to the projected log singular values of the return mapping
+ * (HybridSolver.cpp:626-674).  It is trained on the device from (trial, projected)
+ * pairs that the exact mapping produces during plain steps (aep_set_harvest).
+ *
+ * Training records: 8 floats each, [ln s0, ln s1, ln s2 (trial, sorted desc),
+ * q, material, d0, d1, d2] with d = ln s_projected - ln s_trial.                 */
+typedef struct aep_mlp aep_mlp;
+#define AEP_MLP_NUM_PARAMS 9928  /* f32 master parameters: W1^T, W2^T, W3^T, W4^T, b1..b4 */
+
+aep_status aep_mlp_create(uint64_t seed, aep_mlp** out);
+aep_status aep_mlp_destroy(aep_mlp* m);
+aep_status aep_mlp_get_params(aep_mlp* m, float* host_params, int64_t count);
+aep_status aep_mlp_set_params(aep_mlp* m, const float* host_params, int64_t count);
+/* Gradient of the mean squared error (outputs scaled by 50) over n device records,
+ * with respect to the packed f32 parameters; also returns the loss.           */
+aep_status aep_mlp_gradient(aep_mlp* m, const float* d_records, int64_t n, float* host_grad, double* loss);
+/* Adam steps over batches drawn cyclically from n device records; the learning
+ * rate decays from lr to lr_final (cosine).  Returns the last batch's loss.   */
+aep_status aep_mlp_train(aep_mlp* m, const float* d_records, int64_t n, int64_t steps, int32_t batch,
+                         double lr, double lr_final, double* final_loss, void* cuda_stream);
+/* Predicted corrections d (3 floats per record, ln units) for n device records. */
+aep_status aep_mlp_forward(aep_mlp* m, const float* d_records, int64_t n, float* d_out, void* cuda_stream);
+const char* aep_mlp_last_error(aep_mlp* m);
+
+/* Collect training records from the exact return mapping of every `stride`-th
+ * particle slot during later plain steps into the caller's device buffer
+ * d_records (8 floats per record), up to `capacity` records; d_records = NULL
+ * stops collecting.  The buffer must stay valid while collecting.              */
+aep_status aep_set_harvest(aep_solver* s, float* d_records, int64_t capacity, int32_t stride);
+/* Number of records written so far (capped at the capacity). */
+aep_status aep_get_harvest_count(aep_solver* s, int64_t* count);
+/* Use the learned return map in later steps (NULL: the exact mapping).  Every
+ * prediction is checked in the kernel against the exact mapping; if a projected
+ * log singular value differs by more than `tolerance`, the exact value is used
+ * (aep_stats.learned_fallbacks).  The handle must outlive its use.             */
+aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance);
 
 /* ---- particle-to-grid without allocation --------------------------------------------- */
 

@@ -1,0 +1,105 @@
+"""FP64 numpy restatement of the learned return map's network (forward, loss and
+backward) for the gradient checks of the GPU kernels.
+
+TEST INFRASTRUCTURE ONLY (the checker): used by tests/ only.  With bf16=True the
+weights and every GEMM input are rounded to bfloat16 (round to nearest even) at the
+same points as the tensor-core kernels (aep_mlp.cu), so the two differ only by FP32
+accumulation order; with bf16=False it is the exact FP64 function, which the tests
+pin against central finite differences.
+
+Packed parameters (9928 floats): W1^T [64][16], W2^T [64][64], W3^T [64][64],
+W4^T [8][64], b1 [64], b2 [64], b3 [64], b4 [8].  Records: [ln s0, ln s1, ln s2,
+q, material, d0, d1, d2]; features and targets are scaled by 50.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+LN_SCALE = 50.0
+LAYOUT = [("w1t", (64, 16)), ("w2t", (64, 64)), ("w3t", (64, 64)), ("w4t", (8, 64)),
+          ("b1", (64,)), ("b2", (64,)), ("b3", (64,)), ("b4", (8,))]
+
+
+def unpack(p):
+    out, off = {}, 0
+    for name, shape in LAYOUT:
+        k = int(np.prod(shape))
+        out[name] = np.asarray(p[off:off + k], np.float64).reshape(shape)
+        off += k
+    return out
+
+
+def pack(d):
+    return np.concatenate([np.asarray(d[name], np.float64).ravel() for name, _ in LAYOUT])
+
+
+def bf16(x):
+    """Round float32 values to bfloat16 (nearest, ties to even); returns float64."""
+    a = np.ascontiguousarray(np.asarray(x, np.float32))
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def features(rec, rnd=True):
+    rec = np.asarray(rec, np.float64)
+    n = len(rec)
+    X = np.zeros((n, 16))
+    ln = rec[:, 0:3].astype(np.float32) * np.float32(LN_SCALE)
+    X[:, 0:3] = ln
+    mat = rec[:, 4].astype(int)
+    X[:, 3] = np.where(mat == 1, rec[:, 3].astype(np.float32), 0.0)
+    X[:, 4] = (mat == 0)
+    X[:, 5] = (mat == 1)
+    return bf16(X) if rnd else X
+
+
+def silu(z):
+    return z / (1.0 + np.exp(-z))
+
+
+def dsilu(z):
+    s = 1.0 / (1.0 + np.exp(-z))
+    return s * (1.0 + z * (1.0 - s))
+
+
+def forward(p, rec, bf=True):
+    P = unpack(p)
+    r = bf16 if bf else (lambda a: np.asarray(a, np.float64))
+    W = [r(P["w1t"]), r(P["w2t"]), r(P["w3t"]), r(P["w4t"])]
+    b = [P["b1"], P["b2"], P["b3"], P["b4"]]
+    X = features(rec, bf)
+    Z, H = [], [X]
+    for l in range(3):
+        z = H[-1] @ W[l].T + b[l]
+        Z.append(z)
+        H.append(r(silu(z)))
+    Y = H[-1] @ W[3].T + b[3]
+    return dict(W=W, X=X, Z=Z, H=H, Y=Y)
+
+
+def loss_and_grad(p, rec, bf=True):
+    rec = np.asarray(rec, np.float64)
+    n = len(rec)
+    f = forward(p, rec, bf)
+    r = bf16 if bf else (lambda a: np.asarray(a, np.float64))
+    T = rec[:, 5:8] * LN_SCALE
+    diff = f["Y"][:, :3] - T
+    loss = float((diff ** 2).sum() / (3.0 * n))
+    dY = np.zeros((n, 8))
+    dY[:, :3] = 2.0 * diff / (3.0 * n)
+    dY = r(dY)
+    W, Z, H = f["W"], f["Z"], f["H"]
+    g = {"w4t": dY.T @ H[3], "b4": dY.sum(0)}
+    dZ = r((dY @ W[3]) * dsilu(Z[2]))
+    for l in (2, 1, 0):
+        g[f"w{l + 1}t"] = dZ.T @ H[l]
+        g[f"b{l + 1}"] = dZ.sum(0)
+        if l > 0:
+            dZ = r((dZ @ W[l]) * dsilu(Z[l - 1]))
+    return loss, pack(g)
+
+
+def predict(p, rec, bf=True):
+    """Predicted corrections d (ln units), [n, 3]."""
+    return forward(p, rec, bf)["Y"][:, :3] / LN_SCALE

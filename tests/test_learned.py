@@ -1,0 +1,176 @@
+"""The learned return map: the numpy oracle of the network is pinned by finite
+differences (CPU); the GPU's tensor-core forward and backward kernels match the
+oracle on the same parameters and records; training on harvested (trial,
+projected) pairs reduces the loss; the learned G2P path stays within its stated
+tolerance of the FP64 oracle step; and the trained network is compared with an
+untrained one (what training gains: accepted predictions and error)."""
+import numpy as np
+import pytest
+
+from anisotropicelastoplasticity_gb300 import HybridSolver, scenes
+from oracle import mlp_oracle as mo
+
+NP = 9928
+
+
+def random_records(n, seed=0):
+    rng = np.random.default_rng(seed)
+    rec = np.zeros((n, 8), np.float32)
+    ln = np.sort(rng.normal(0, 0.02, (n, 3)), axis=1)[:, ::-1]
+    rec[:, 0:3] = ln
+    rec[:, 3] = rng.random(n) * 0.5
+    rec[:, 4] = rng.integers(0, 2, n)
+    rec[:, 5:8] = -0.3 * np.maximum(ln, 0) + 0.01 * rng.normal(size=(n, 3))
+    return rec
+
+
+def random_params(seed=1):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(NP, np.float32)
+    d = mo.unpack(p.astype(np.float64))
+    d["w1t"][:, :6] = rng.normal(0, np.sqrt(2 / 6), (64, 6))
+    d["w2t"][:] = rng.normal(0, np.sqrt(2 / 64), (64, 64))
+    d["w3t"][:] = rng.normal(0, np.sqrt(2 / 64), (64, 64))
+    d["w4t"][:3] = rng.normal(0, 0.1 * np.sqrt(2 / 64), (3, 64))
+    for b in ("b1", "b2", "b3"):
+        d[b][:] = 0.1 * rng.normal(size=64)
+    d["b4"][:3] = 0.1 * rng.normal(size=3)
+    return mo.pack(d).astype(np.float32)
+
+
+def test_bf16_rounding_known_values():
+    x = np.array([1.0, 1.00390625, 1.005859375, -2.5, 3.0e-3], np.float32)
+    r = mo.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125 and r[3] == -2.5
+    assert abs(r[4] - 3.0e-3) / 3.0e-3 < 2 ** -8
+
+
+def test_oracle_backward_matches_finite_differences():
+    rec = random_records(24, seed=3)
+    p = random_params(4).astype(np.float64)
+    loss, g = mo.loss_and_grad(p, rec, bf=False)
+    rng = np.random.default_rng(5)
+    idx = np.concatenate([rng.choice(np.arange(0, 64 * 16).reshape(64, 16)[:, :6].ravel(), 10),
+                          rng.integers(1024, 9728, 40), rng.integers(9728, 9728 + 195, 10)])
+    for i in idx:
+        h = 1e-6 * max(1.0, abs(p[i]))
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (mo.loss_and_grad(pp, rec, bf=False)[0] - mo.loss_and_grad(pm, rec, bf=False)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(abs(g).max(), 1e-12) + 1e-5 * abs(g[i]), (i, fd, g[i])
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_matches_oracle():
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP
+
+    rec = random_records(300, seed=7)  # several blocks of 64 rows, a partial last block
+    p = random_params(8)
+    m = ReturnMapMLP(seed=0)
+    m.set_params(p)
+    d = torch.from_numpy(rec).cuda()
+    g_gpu, loss_gpu = m.gradient(d.data_ptr(), len(rec))
+    loss_o, g_o = mo.loss_and_grad(p.astype(np.float64), rec, bf=True)
+    assert abs(loss_gpu - loss_o) / loss_o < 1e-4
+    go, gg = mo.unpack(g_o), mo.unpack(g_gpu.astype(np.float64))
+    for name, _ in mo.LAYOUT:
+        ref = go[name]
+        if name == "w1t":
+            ref, got = ref[:, :6], gg[name][:, :6]
+        elif name in ("w4t", "b4"):
+            ref, got = ref[:3], gg[name][:3]
+        else:
+            got = gg[name]
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err < 1e-2, (name, err)
+
+
+@pytest.mark.gpu
+def test_gpu_forward_matches_oracle():
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP
+
+    rec = random_records(1000, seed=9)
+    p = random_params(10)
+    m = ReturnMapMLP()
+    m.set_params(p)
+    d = torch.from_numpy(rec).cuda()
+    out = torch.empty((len(rec), 3), dtype=torch.float32, device="cuda")
+    m.forward(d.data_ptr(), len(rec), out.data_ptr())
+    torch.cuda.synchronize()
+    ref = mo.predict(p.astype(np.float64), rec, bf=True)
+    assert np.abs(out.cpu().numpy() - ref).max() < 2e-4 * max(np.abs(ref).max(), 1e-3)
+
+
+def _harvest_small(torch):
+    from anisotropicelastoplasticity_gb300.learned import harvest_records
+
+    recs = [harvest_records(scenes.snow_block(n=4096, res=32, seed=1), steps=40, capacity=200000, stride=1),
+            harvest_records(scenes.sand_column(n=12000, res=32, seed=2), steps=40, capacity=400000, stride=1)]
+    return torch.cat(recs)
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss_on_harvested_pairs():
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP
+
+    rec = _harvest_small(torch)
+    n = len(rec)
+    assert n > 100000
+    host = rec.cpu().numpy()
+    assert np.all(np.isfinite(host))
+    plastic = np.abs(host[:, 5:8]).max(axis=1) > 0
+    assert plastic.mean() > 0.01  # the harvest contains projected states
+    m = ReturnMapMLP(seed=3)
+    _, loss0 = m.gradient(rec.data_ptr(), n)
+    loss1 = m.train(rec.data_ptr(), n, steps=1500, batch=4096, lr=2e-3, lr_final=2e-5)
+    _, loss_end = m.gradient(rec.data_ptr(), n)
+    assert loss_end < 0.05 * loss0, (loss0, loss1, loss_end)
+
+
+def _learned_run(mlp, scene, steps, tol=1e-4):
+    s = HybridSolver(scene.particles, scene.grid, scene.params)
+    s.set_level_set(scene.levelset)
+    s.init_volumes()
+    s.set_return_map(mlp, tol)
+    acc = fb = 0
+    for _ in range(steps):
+        s.step(scene.dt)
+        st = s.stats()
+        acc += st["learned_accepted"]
+        fb += st["learned_fallbacks"]
+    return s, acc, fb
+
+
+@pytest.mark.gpu
+def test_learned_step_matches_oracle_and_training_gains():
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP
+    from oracle.oracle import Oracle
+
+    rec = _harvest_small(torch)
+    trained = ReturnMapMLP(seed=3)
+    trained.train(rec.data_ptr(), len(rec), steps=2000, batch=4096, lr=2e-3, lr_final=2e-5)
+    untrained = ReturnMapMLP(seed=3)
+    sc = scenes.sand_column(n=12000, res=32, seed=5)
+    steps = 10
+    s_tr, acc_tr, fb_tr = _learned_run(trained, sc, steps)
+    s_un, acc_un, fb_un = _learned_run(untrained, sc, steps)
+    # what training gains: most predictions accepted instead of (nearly) none
+    rate_tr = acc_tr / max(acc_tr + fb_tr, 1)
+    rate_un = acc_un / max(acc_un + fb_un, 1)
+    assert acc_tr + fb_tr == steps * len(sc.particles)
+    assert rate_tr > 0.9 and rate_tr > rate_un + 0.5, (rate_tr, rate_un)
+    # the learned path stays within its tolerance of the FP64 oracle step
+    o = Oracle(sc.grid, sc.params)
+    o.set_particle_system(sc.particles)
+    o.set_level_set(sc.levelset)
+    o.init(volumes=True)
+    for _ in range(steps):
+        o.step(sc.dt)
+    gp, op = s_tr.get_particles(), o.get_particles()
+    assert np.abs(gp["positions"] - op["positions"]).max() < 2e-6
+    assert np.abs(gp["elastic_deformation_gradients"] - op["elastic_deformation_gradients"]).max() < 5e-4
