@@ -80,6 +80,7 @@ struct aep_solver {
     int ev_slot = 0;
     double phase_ms[AEP_NUM_PHASES] = {};
     int64_t timed_steps = 0;
+    unsigned long long* check = nullptr;  // upload validation result
     std::string err;
 };
 
@@ -254,8 +255,9 @@ aep_status ensure_capacity(aep_solver* s, int64_t n, int64_t keep = 0) {
     CK(cudaMalloc(&s->perm, sizeof(int32_t) * (size_t)n));
     s->sort_bytes = sort_temp_bytes((int)n, s->key_bits);
     CK(cudaMalloc(&s->sort_tmp, s->sort_bytes));
-    s->staging_bytes = sizeof(double) * 9 * (size_t)n;
+    s->staging_bytes = sizeof(double) * 36 * (size_t)n;  // every field of one particle set at once
     CK(cudaMalloc(&s->staging, s->staging_bytes));
+    if (!s->check) CK(cudaMalloc(&s->check, 2 * sizeof(unsigned long long)));
     std::vector<int32_t> io((size_t)n);
     for (int64_t i = 0; i < n; ++i) io[(size_t)i] = (int32_t)i;
     CK(cudaMemcpy(s->iota, io.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice));
@@ -265,28 +267,33 @@ aep_status ensure_capacity(aep_solver* s, int64_t n, int64_t keep = 0) {
 }
 
 // upload `count` doubles per item for items [id0, id0 + n) of set 0
+// src: host array of `count` doubles per item; `off` doubles into the staging buffer
+// (distinct offsets let consecutive uploads run without waiting on each other)
 aep_status upload(aep_solver* s, const double* src, int count, int mode, float* const* dst, int64_t n = -1,
-                  int64_t id0 = 0) {
+                  int64_t id0 = 0, const int32_t* map = nullptr, size_t off = 0) {
     if (n < 0) n = s->n;
-    CK(cudaMemcpyAsync(s->staging, src, sizeof(double) * count * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    double* st = s->staging + off;
+    if (src != st)
+        CK(cudaMemcpyAsync(st, src, sizeof(double) * count * (size_t)n, cudaMemcpyHostToDevice, s->stream));
     float* d[9] = {};
     int nd = mode == 3 ? 1 : (mode == 0 ? 3 : 9);
     for (int k = 0; k < nd; ++k) d[k] = dst[k] + id0;
-    launch_upload((int)n, mode, s->staging, d, s->stream);
+    launch_upload((int)n, mode, st, d, s->stream, map);
     CKLAUNCH();
     return AEP_OK;
 }
 
-// download ids [id_lo, id_hi) in id order
+// download ids [id_lo, id_hi) in id order through staging offset `off` (doubles);
+// the caller synchronises once after all fields
 aep_status download(aep_solver* s, double* dst, int count, int mode, float* const* src, int64_t id_lo = 0,
-                    int64_t id_hi = -1) {
+                    int64_t id_hi = -1, size_t off = 0, bool sync = true) {
     if (id_hi < 0) id_hi = s->n;
     const PArrays& P = s->P[s->cur];
-    launch_download((int)s->n, mode, P.id, s->staging, src, s->stream, (int)id_lo, (int)id_hi);
+    double* st = s->staging + off;
+    launch_download((int)s->n, mode, P.id, st, src, s->stream, (int)id_lo, (int)id_hi);
     CKLAUNCH();
-    CK(cudaMemcpyAsync(dst, s->staging, sizeof(double) * count * (size_t)(id_hi - id_lo), cudaMemcpyDeviceToHost,
-                       s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpyAsync(dst, st, sizeof(double) * count * (size_t)(id_hi - id_lo), cudaMemcpyDeviceToHost, s->stream));
+    if (sync) CK(cudaStreamSynchronize(s->stream));
     return AEP_OK;
 }
 
@@ -436,6 +443,7 @@ aep_status aep_solver_destroy(aep_solver* s) {
     cudaFree(s->dstats);
     cudaFree(s->dforce);
     cudaFree(s->harvest_count);
+    cudaFree(s->check);
     for (int r = 0; r < aep_solver::kRing; ++r)
         for (int p = 0; p <= AEP_NUM_PHASES; ++p)
             if (s->ev[r][p]) cudaEventDestroy(s->ev[r][p]);
@@ -450,58 +458,80 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     if (!s) return AEP_INVALID_ARG;
     if (n <= 0 || n > (int64_t)INT32_MAX / 2 || !x || !Fe || !m)
         return fail(s, AEP_INVALID_ARG, "aep_set_particles: need n > 0 and non-null x, Fe, m");
-    double mm = 0.0;
-    for (int64_t p = 0; p < n; ++p) {
-        if (!(m[p] >= 0.0) || !std::isfinite(m[p])) return fail(s, AEP_INVALID_ARG, "aep_set_particles: bad mass");
-        mm = std::max(mm, m[p]);
-    }
-    if (material)
-        for (int64_t p = 0; p < n; ++p)
-            if (material[p] > AEP_SAND) return fail(s, AEP_INVALID_ARG, "aep_set_particles: unknown material tag");
-    if (!(mm > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_particles: all masses are zero");
     CK(cudaStreamSynchronize(s->stream));
+    if (s->cap < n) {  // room for the staging copies used by the validation below
+        free_mesh(s);
+        s->have_particles = false;
+        s->n = s->np = 0;
+        aep_status st0 = ensure_capacity(s, n);
+        if (st0 != AEP_OK) return st0;
+    }
+    // validation on the device: largest mass, bad masses, unknown material tags
+    double* dm = s->staging + 27 * (size_t)n;  // masses stay here for the upload below
+    uint8_t* dmat = reinterpret_cast<uint8_t*>(s->staging + 35 * (size_t)n);
+    CK(cudaMemcpyAsync(dm, m, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    if (material) CK(cudaMemcpyAsync(dmat, material, (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->check, 0, 2 * sizeof(unsigned long long), s->stream));
+    launch_check_upload((int)n, dm, material ? dmat : nullptr, s->check, s->stream);
+    CKLAUNCH();
+    unsigned long long chk[2] = {0, 0};
+    CK(cudaMemcpyAsync(chk, s->check, sizeof(chk), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (chk[1]) return fail(s, AEP_INVALID_ARG, "aep_set_particles: bad mass or unknown material tag");
+    double mm = 0.0;
+    std::memcpy(&mm, &chk[0], sizeof(mm));
+    if (!(mm > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_particles: all masses are zero");
+    // Re-uploading the same particle set keeps the device's current (sorted) order:
+    // item q goes to the slot its id occupies now, so the next sort sees nearly
+    // sorted keys and the permuted particle reads stay coalesced.
+    const bool keep_order = s->have_particles && s->n == n && s->np == n && s->nf == 0;
+    const int32_t* map = nullptr;
+    if (keep_order) {
+        launch_inverse_ids((int)n, s->P[s->cur].id, s->perm, s->stream);
+        CKLAUNCH();
+        map = s->perm;
+    }
     free_mesh(s);  // a mesh must be (re)attached after the particles
     aep_status st = ensure_capacity(s, n);
     if (st != AEP_OK) return st;
     s->n = s->np = n;
-    s->cur = 0;
     s->m_max = mm;
     fill_kparams(s);
-    PArrays& P = s->P[0];
-    st = upload(s, x, 3, 0, P.x);
+    if (!keep_order) s->cur = 0;
+    PArrays& P = s->P[s->cur];
+    // staging layout (doubles): x 0, v 3n, B 6n, Fe 15n, Fp 24n... (Fp reuses B's area
+    // after B is converted), m 27n, vol 28n, plastic 29n, material bytes at 35n
+    const size_t N = (size_t)n;
+    st = upload(s, x, 3, 0, P.x, -1, 0, map, 0);
     if (st) return st;
-    if (v) { st = upload(s, v, 3, 0, P.v); if (st) return st; }
+    if (v) { st = upload(s, v, 3, 0, P.v, -1, 0, map, 3 * N); if (st) return st; }
     else for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(P.v[a], 0, sizeof(float) * n, s->stream));
-    if (B) { st = upload(s, B, 9, 1, P.B); if (st) return st; }
+    if (B) { st = upload(s, B, 9, 1, P.B, -1, 0, map, 6 * N); if (st) return st; }
     else for (int a = 0; a < 9; ++a) CK(cudaMemsetAsync(P.B[a], 0, sizeof(float) * n, s->stream));
-    st = upload(s, Fe, 9, 2, P.F);
+    st = upload(s, Fe, 9, 2, P.F, -1, 0, map, 15 * N);
     if (st) return st;
-    st = upload(s, m, 1, 3, &P.m);
+    st = upload(s, dm, 1, 3, &P.m, -1, 0, map, 27 * N);  // already on the device
     if (st) return st;
-    if (vol) { st = upload(s, vol, 1, 3, &P.vol); if (st) return st; }
+    if (vol) { st = upload(s, vol, 1, 3, &P.vol, -1, 0, map, 28 * N); if (st) return st; }
     else CK(cudaMemsetAsync(P.vol, 0, sizeof(float) * n, s->stream));
-    if (plastic) { st = upload(s, plastic, 1, 3, &P.plastic); if (st) return st; }
+    if (plastic) { st = upload(s, plastic, 1, 3, &P.plastic, -1, 0, map, 29 * N); if (st) return st; }
     else CK(cudaMemsetAsync(P.plastic, 0, sizeof(float) * n, s->stream));
     // material tags and ids
-    uint8_t* dmat = nullptr;
-    if (material) {
-        dmat = reinterpret_cast<uint8_t*>(s->staging);
-        CK(cudaMemcpyAsync(dmat, material, (size_t)n, cudaMemcpyHostToDevice, s->stream));
-    }
-    launch_init_particles((int)n, P, dmat, Fp != nullptr, s->prm.track_plastic_F, s->stream);
+    launch_init_particles((int)n, P, material ? dmat : nullptr, Fp != nullptr, s->prm.track_plastic_F, s->stream, 0,
+                          -1, map);
     CKLAUNCH();
-    if (s->prm.track_plastic_F && Fp) {
-        st = upload(s, Fp, 9, 2, P.Fp);
-        if (st) return st;
-    }
-    // snow particles: J_P = det F_P into `plastic`
+    // F_P: full copy with track_plastic_F; snow particles get J_P = det F_P
     double* dFp = nullptr;
     if (Fp) {
-        dFp = s->staging;
-        CK(cudaMemcpyAsync(dFp, Fp, sizeof(double) * 9 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        dFp = s->staging + 6 * N;  // after B's conversion (stream order)
+        CK(cudaMemcpyAsync(dFp, Fp, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, s->stream));
+        if (s->prm.track_plastic_F) {
+            st = upload(s, dFp, 9, 2, P.Fp, -1, 0, map, 6 * N);
+            if (st) return st;
+        }
     }
-    if (!s->prm.track_plastic_F) {
-        launch_snow_jp((int)n, P, dFp, s->stream);
+    if (!s->prm.track_plastic_F && (Fp || !plastic)) {  // else J_P of snow comes from `plastic`
+        launch_snow_jp((int)n, P, dFp, s->stream, map);
         CKLAUNCH();
     }
     CK(cudaStreamSynchronize(s->stream));
@@ -767,13 +797,15 @@ aep_status aep_get_particles(aep_solver* s, int64_t n, double* x, double* v, dou
     PArrays& P = s->P[s->cur];
     aep_status st;
     const int64_t np = s->np;
-    if (x && (st = download(s, x, 3, 0, P.x, 0, np))) return st;
-    if (v && (st = download(s, v, 3, 0, P.v, 0, np))) return st;
-    if (B && (st = download(s, B, 9, 1, P.B, 0, np))) return st;
-    if (Fe && (st = download(s, Fe, 9, 2, P.F, 0, np))) return st;
-    if (Fp && (st = download(s, Fp, 9, 2, P.Fp, 0, np))) return st;
-    if (vol && (st = download(s, vol, 1, 3, &P.vol, 0, np))) return st;
-    if (plastic && (st = download(s, plastic, 1, 3, &P.plastic, 0, np))) return st;
+    const size_t N = (size_t)np;
+    if (x && (st = download(s, x, 3, 0, P.x, 0, np, 0, false))) return st;
+    if (v && (st = download(s, v, 3, 0, P.v, 0, np, 3 * N, false))) return st;
+    if (B && (st = download(s, B, 9, 1, P.B, 0, np, 6 * N, false))) return st;
+    if (Fe && (st = download(s, Fe, 9, 2, P.F, 0, np, 15 * N, false))) return st;
+    if (Fp && (st = download(s, Fp, 9, 2, P.Fp, 0, np, 24 * N, false))) return st;
+    if (vol && (st = download(s, vol, 1, 3, &P.vol, 0, np, 33 * N, false))) return st;
+    if (plastic && (st = download(s, plastic, 1, 3, &P.plastic, 0, np, 34 * N, false))) return st;
+    CK(cudaStreamSynchronize(s->stream));
     return AEP_OK;
 }
 

@@ -22,6 +22,8 @@
 // registers before any atomic (one atomic per node per run instead of one per
 // particle); __match_any_sync + __ballot_sync find the run structure of each
 // batch of 16 particles.
+#include <algorithm>
+
 #include "aep_device.cuh"
 #include "aep_kernels.h"
 #include "aep_mlp.cuh"
@@ -820,7 +822,8 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
         sn[0] = s[0]; sn[1] = s[1]; sn[2] = s[2];
         const float q_old = q;
         return_map<float>(P, mat, sn, q);
-        if (H.buf && (j % H.stride) == 0) harvest_record(H, mat, s, sn, q_old);
+        if (H.buf && (j % H.stride) == 0 && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2]))
+            harvest_record(H, mat, s, sn, q_old);  // plastic states only
         sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
         float US[9];
 #pragma unroll
@@ -900,11 +903,14 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
 
 // ===================================================================================
 // G2P with the learned return map: as k_g2p, but the singular-value return mapping
-// of snow and sand particles is predicted by the MLP (aep_mlp.cuh) on the tensor
-// cores, 32 particles per warp.  Each prediction is checked in the kernel against
-// the exact mapping (HybridSolver.cpp:626-674): if any projected log singular value
-// differs by more than `tol`, the exact value is used instead and counted as a
-// fallback.  No lane leaves before the warp-wide MLP call.
+// of plastic snow and sand states is predicted by the MLP (aep_mlp.cuh) on the
+// tensor cores, 32 particles per warp.  The yield check (the exact mapping,
+// HybridSolver.cpp:626-674) decides whether a state is plastic; elastic states
+// keep their trial values.  Each plastic prediction is checked against the exact
+// projection: if the projected log singular values differ by more than `tol`
+// relative to their largest magnitude (absolute floor 1e-5), the exact value is
+// used instead and counted as a fallback.  No lane leaves before the warp-wide
+// MLP call.
 __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PArrays nxt,
                                                      const int32_t* __restrict__ perm, int n, GArrays G, float dt,
                                                      uint32_t* __restrict__ keys_next, DevStats* st, MlpParams mlp,
@@ -920,7 +926,10 @@ __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PAr
     __nv_bfloat16* MH1 = MH0 + kMlpWarpH;
     float* MY = reinterpret_cast<float*>(MH1 + kMlpWarpH);
 
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    // persistent: the weights are loaded once per block, which then walks chunks of
+    // blockDim.x particles (all threads run the same number of iterations)
+    for (long chunk = blockIdx.x; chunk * blockDim.x < n; chunk += gridDim.x) {
+    const int j = (int)(chunk * blockDim.x) + threadIdx.x;
     const bool live = j < n;
     const int pj = live ? perm[j] : 0;
     const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
@@ -979,10 +988,10 @@ __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PAr
         lns[0] = logf(s[0]); lns[1] = logf(s[1]); lns[2] = logf(s[2]);
         sort3_desc(lns, srt, pm);
     }
-    mlp_features(srt, q, (rm && ok) ? mat : 0, MX + lane * kStrideIn);
+    const float osc = mlp_features(srt, q, (rm && ok) ? mat : 0, MX + lane * kStrideIn);
     mlp_forward_warp(W, MX, MH0, MH1, MY, lane);
 
-    if (!active) return;
+    if (!active) continue;
     if (mat == kClothVertex) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -1000,20 +1009,31 @@ __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PAr
         double Ud[9], sd[3], Vd[9];
         bool used_fp64 = false;
         if (ok) {
-            // exact mapping (the check) and the prediction, both in sorted order
+            // the exact mapping decides whether the state is plastic (the yield check)
+            // and is the reference of the residual check
             float ex[3] = {s[0], s[1], s[2]};
             float qe = q;
             return_map<float>(P, mat, ex, qe);
+            const bool plastic = ex[0] != s[0] || ex[1] != s[1] || ex[2] != s[2];
             float pred_ln[3];
-            bool accept = true;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const int src = pm[k];
-                pred_ln[src] = srt[k] + MY[lane * kMlpOut + k] / kLnScale;
+                pred_ln[src] = srt[k] + MY[lane * kMlpOut + k] / osc;
             }
+            // relative residual of the projected log singular values: the stress is
+            // nearly linear in them, so this bounds the relative stress error
+            float err = 0.0f, ref = 0.0f;
 #pragma unroll
-            for (int a = 0; a < 3; ++a) accept = accept && fabsf(pred_ln[a] - logf(ex[a])) <= tol;
-            if (accept) {
+            for (int a = 0; a < 3; ++a) {
+                const float le = logf(ex[a]);
+                err = fmaxf(err, fabsf(pred_ln[a] - le));
+                ref = fmaxf(ref, fabsf(le));
+            }
+            const bool accept = plastic && err <= tol * fmaxf(ref, 1e-5f);
+            if (!plastic) {  // elastic: the mapping is the identity, nothing to predict
+                sn[0] = s[0]; sn[1] = s[1]; sn[2] = s[2];
+            } else if (accept) {
 #pragma unroll
                 for (int a = 0; a < 3; ++a) sn[a] = expf(pred_ln[a]);
                 if (mat == kSand && qe != q) {  // plastic: q grows by the projection distance
@@ -1100,6 +1120,7 @@ __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PAr
     const bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nf);
     keys_next[j] = make_key(P, ncell);
     if (clamped) atomicAdd(&st->out_of_domain, 1ull);
+    }
 }
 
 // ===================================================================================
@@ -1205,24 +1226,27 @@ __global__ void k_volumes(KParams P, PArrays cur, const int32_t* __restrict__ pe
 // mode: 0 = N x 3 column-major vector field into dst[3], 1 = 9N B rows (see aep.h),
 // 2 = 9N per-particle column-major 3x3 into row-major dst[9], 3 = N scalars,
 // 4 = element directions d1 | d2 | d3 (each N x 3 column-major) into the columns of dst[9]
+// map (optional): item q of the source goes to slot map[q] (keeps the device order)
 __global__ void k_upload(int n, int mode, const double* __restrict__ src, float* d0, float* d1, float* d2,
-                         float* d3, float* d4, float* d5, float* d6, float* d7, float* d8) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
+                         float* d3, float* d4, float* d5, float* d6, float* d7, float* d8,
+                         const int32_t* __restrict__ map) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // source item
+    if (q >= n) return;
+    const long p = map ? map[q] : q;                       // destination slot
     float* d[9] = {d0, d1, d2, d3, d4, d5, d6, d7, d8};
     if (mode == 0) {
-        for (int a = 0; a < 3; ++a) d[a][p] = (float)src[(long)a * n + p];
+        for (int a = 0; a < 3; ++a) d[a][p] = (float)src[(long)a * n + q];
     } else if (mode == 1) {
         for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[(long)a * 3 * n + (long)b * n + p];
+            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[(long)a * 3 * n + (long)b * n + q];
     } else if (mode == 2) {
         for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[9l * p + a + 3 * b];
+            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[9l * q + a + 3 * b];
     } else if (mode == 4) {
         for (int c = 0; c < 3; ++c)
-            for (int a = 0; a < 3; ++a) d[3 * a + c][p] = (float)src[(long)c * 3 * n + (long)a * n + p];
+            for (int a = 0; a < 3; ++a) d[3 * a + c][p] = (float)src[(long)c * 3 * n + (long)a * n + q];
     } else {
-        d[0][p] = (float)src[p];
+        d[0][p] = (float)src[q];
     }
 }
 
@@ -1255,11 +1279,11 @@ __global__ void k_download(int n, int mode, const int32_t* __restrict__ id, doub
 }
 
 __global__ void k_init_particles(int n, PArrays cur, const uint8_t* __restrict__ mat_in, int has_fp, int track_fp,
-                                 int id0, int fixed_mat) {
+                                 int id0, int fixed_mat, const int32_t* __restrict__ map) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    const int p = id0 + q;
-    cur.id[p] = p;
+    const int p = map ? map[q] : id0 + q;  // slot
+    cur.id[p] = id0 + q;
     int mat = fixed_mat >= 0 ? fixed_mat : (mat_in ? mat_in[q] : kSand);
     cur.mat[p] = (uint8_t)mat;
     if (!has_fp && track_fp)
@@ -1267,14 +1291,43 @@ __global__ void k_init_particles(int n, PArrays cur, const uint8_t* __restrict__
 }
 
 // snow particles carry J_P = det F_P in `plastic` when F_P is not tracked
-__global__ void k_snow_jp(int n, PArrays cur, const double* __restrict__ Fp) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
+__global__ void k_snow_jp(int n, PArrays cur, const double* __restrict__ Fp, const int32_t* __restrict__ map) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int p = map ? map[q] : q;
     if (cur.mat[p] != kSnow) return;
     double A[9];
     for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b) A[3 * a + b] = Fp ? Fp[9l * p + a + 3 * b] : (a == b ? 1.0 : 0.0);
+        for (int b = 0; b < 3; ++b) A[3 * a + b] = Fp ? Fp[9l * q + a + 3 * b] : (a == b ? 1.0 : 0.0);
     cur.plastic[p] = (float)mat_det(A);
+}
+
+// upload validation: largest mass (bit pattern of a non-negative double is monotonic),
+// bad masses (negative, NaN, inf) and unknown material tags; out = {max bits, bad}
+__global__ void k_check_upload(int n, const double* __restrict__ m, const uint8_t* __restrict__ mat,
+                               unsigned long long* out) {
+    unsigned long long mx = 0ull, bad = 0ull;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const double v = m[i];
+        if (!(v >= 0.0) || !isfinite(v)) bad = 1ull;
+        else if (v > 0.0) mx = max(mx, (unsigned long long)__double_as_longlong(v));
+        if (mat && mat[i] > kSand) bad = 1ull;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (mx) atomicMax(out, mx);
+        if (bad) atomicOr(out + 1, bad);
+    }
+}
+
+// inverse of the id map of the current order: inv[id[j]] = j
+__global__ void k_inverse_ids(int n, const int32_t* __restrict__ id, int32_t* __restrict__ inv) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) inv[id[j]] = j;
 }
 
 // dense grid readback in reference order (mode 0: P2G state; 1: after grid update)
@@ -1338,8 +1391,12 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
         if (mlp) {
             const int smem = kMlpSmemBytes + 4 * kMlpWarpBytes;
             cudaFuncSetAttribute(k_g2p_learned, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            k_g2p_learned<<<blocks_for(n, 128), 128, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp,
-                                                               learned_tol);
+            int dev = 0, sms = 0, per_sm = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_g2p_learned, 128, smem);
+            const int blocks = std::min(blocks_for(n, 128), std::max(1, sms * std::max(per_sm, 1)));
+            k_g2p_learned<<<blocks, 128, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp, learned_tol);
         } else {
             k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H);
         }
@@ -1350,10 +1407,16 @@ void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, i
                     cudaStream_t s) {
     if (n > 0) k_volumes<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, perm, n, G);
 }
-void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s) {
+void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s, const int32_t* map) {
     if (n > 0)
         k_upload<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, src, dst[0], dst[1], dst[2], dst[3], dst[4], dst[5],
-                                                    dst[6], dst[7], dst[8]);
+                                                    dst[6], dst[7], dst[8], map);
+}
+void launch_check_upload(int n, const double* m, const uint8_t* mat, unsigned long long* out, cudaStream_t s) {
+    if (n > 0) k_check_upload<<<std::min(1024, blocks_for(n, 256)), 256, 0, s>>>(n, m, mat, out);
+}
+void launch_inverse_ids(int n, const int32_t* id, int32_t* inv, cudaStream_t s) {
+    if (n > 0) k_inverse_ids<<<blocks_for(n, 256), 256, 0, s>>>(n, id, inv);
 }
 void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s, int id_lo,
                      int id_hi) {
@@ -1363,11 +1426,11 @@ void launch_download(int n, int mode, const int32_t* id, double* dst, float* con
                                                       src[5], src[6], src[7], src[8], id_lo, id_hi);
 }
 void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp, cudaStream_t s,
-                           int id0, int fixed_mat) {
-    if (n > 0) k_init_particles<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, mat, has_fp, track_fp, id0, fixed_mat);
+                           int id0, int fixed_mat, const int32_t* map) {
+    if (n > 0) k_init_particles<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, mat, has_fp, track_fp, id0, fixed_mat, map);
 }
-void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s) {
-    if (n > 0) k_snow_jp<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, Fp);
+void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s, const int32_t* map) {
+    if (n > 0) k_snow_jp<<<blocks_for(n, 256), 256, 0, s>>>(n, cur, Fp, map);
 }
 void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double* vel, double* vbf, int grid_blocks,
                        cudaStream_t s) {

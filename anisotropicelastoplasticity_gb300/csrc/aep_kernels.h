@@ -21,12 +21,15 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
                 const Harvest& H, const MlpParams* mlp, float learned_tol);
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s);
-void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s);
+void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s,
+                   const int32_t* map = nullptr);
+void launch_inverse_ids(int n, const int32_t* id, int32_t* inv, cudaStream_t s);
+void launch_check_upload(int n, const double* m, const uint8_t* mat, unsigned long long* out, cudaStream_t s);
 void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s,
                      int id_lo = 0, int id_hi = -1);
 void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp,
-                           cudaStream_t s, int id0 = 0, int fixed_mat = -1);
-void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s);
+                           cudaStream_t s, int id0 = 0, int fixed_mat = -1, const int32_t* map = nullptr);
+void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s, const int32_t* map = nullptr);
 void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double* vel, double* vbf,
                        int grid_blocks, cudaStream_t s);
 

@@ -5,9 +5,11 @@
 //                      gradients are added to one f32 gradient vector
 //   k_mlp_adam       : Adam on the f32 master parameters, refreshes the bf16 copies
 //   k_mlp_infer      : batched forward pass (32 rows per warp), as used inside G2P
-// Training records (harvested from the exact return mapping, 8 floats each):
+// Training records (harvested from the exact return mapping where it changed the
+// state, 8 floats each):
 //   [ln s0, ln s1, ln s2 (trial, sorted descending), q, material, d0, d1, d2]
-// with d = ln s_projected - ln s_trial in the same order.
+// with d = ln s_projected - ln s_trial in the same order.  The loss is the mean
+// squared error of the network output against d in the scaling of mlp_features.
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -104,8 +106,8 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         const float* q = rec + 8 * gi;
         const bool live = base + r < row0 + rows_total;
         float ln[3] = {q[0], q[1], q[2]};
-        mlp_features(ln, q[3], (int)q[4], S.X + r * 16);
-        for (int k = 0; k < 3; ++k) S.T[r * 4 + k] = live ? q[5 + k] * kLnScale : 0.0f;
+        const float sc = mlp_features(ln, q[3], (int)q[4], S.X + r * 16);
+        for (int k = 0; k < 3; ++k) S.T[r * 4 + k] = live ? q[5 + k] * sc : 0.0f;
         S.T[r * 4 + 3] = live ? 1.0f : 0.0f;  // row weight
     }
     __syncthreads();
@@ -264,17 +266,18 @@ __global__ void __launch_bounds__(128) k_mlp_infer(MlpParams P, const float* __r
     bf16* H1 = H0 + kMlpWarpH;
     float* Y = reinterpret_cast<float*>(H1 + kMlpWarpH);
     const long r = ((long)blockIdx.x * 4 + warp) * 32 + lane;
+    float sc = 1.0f;
     if (r < n) {
         const float* q = rec + 8 * r;
         float ln[3] = {q[0], q[1], q[2]};
-        mlp_features(ln, q[3], (int)q[4], X + lane * kStrideIn);
+        sc = mlp_features(ln, q[3], (int)q[4], X + lane * kStrideIn);
     } else {
         float ln[3] = {0, 0, 0};
         mlp_features(ln, 0.0f, 0, X + lane * kStrideIn);
     }
     mlp_forward_warp(W, X, H0, H1, Y, lane);
     if (r < n)
-        for (int k = 0; k < 3; ++k) out[3 * r + k] = Y[lane * kMlpOut + k] / kLnScale;
+        for (int k = 0; k < 3; ++k) out[3 * r + k] = Y[lane * kMlpOut + k] / sc;
 }
 
 }  // namespace

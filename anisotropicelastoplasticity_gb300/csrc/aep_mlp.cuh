@@ -1,10 +1,11 @@
 // aep_mlp.cuh -- the learned return map: a 6 -> 64 -> 64 -> 64 -> 3 MLP with SiLU,
 // BF16 weights on the tensor cores (mma.sync m16n8k16, FP32 accumulation).
 //
-// Input features (one row per particle, scaled by kLnScale): the trial log singular
-// values of F_E^tr sorted descending (3), the sand plastic amount q (1), and the
-// material one-hot (snow, sand) (2); padded to 16 columns.  Output: the scaled
-// correction (ln s_projected - ln s_trial) * kLnScale in the same order (3 of 8).
+// Input features (one row per particle): the trial log singular values of F_E^tr
+// sorted descending (3; normalised for sand, scaled by kLnScale for snow, see
+// mlp_features), the sand plastic amount q (1), and the material one-hot (snow,
+// sand) (2); padded to 16 columns.  Output: the correction (ln s_projected -
+// ln s_trial) in the same order and the same scaling (3 of 8).
 // The return mappings it stands in for (HybridSolver.cpp:626-674) are invariant
 // under permutations of the singular values, so sorting canonicalises the input.
 //
@@ -166,16 +167,27 @@ __device__ __forceinline__ void mlp_forward_warp(const MlpSmem& W, __nv_bfloat16
     __syncwarp();
 }
 
-// feature row of one particle: sorted (descending) trial ln s, plastic amount, one-hot
-__device__ __forceinline__ void mlp_features(const float ln_sorted[3], float q, int mat, __nv_bfloat16* row) {
-    row[0] = __float2bfloat16(ln_sorted[0] * kLnScale);
-    row[1] = __float2bfloat16(ln_sorted[1] * kLnScale);
-    row[2] = __float2bfloat16(ln_sorted[2] * kLnScale);
+// Feature row of one particle and the scale of its output.  Sand: the Drucker-Prager
+// projection onto a cone is positively homogeneous in ln s, so the sorted trial
+// log singular values are normalised by their norm r and the network predicts the
+// correction divided by r.  Snow: the clamp bounds are absolute, so ln s and the
+// correction are scaled by kLnScale.  Returns the factor that maps a correction to
+// the network's output (sand: 1/r, snow: kLnScale).
+__device__ __forceinline__ float mlp_features(const float ln_sorted[3], float q, int mat, __nv_bfloat16* row) {
+    float sc = kLnScale;
+    if (mat == 1) {
+        const float r = sqrtf(ln_sorted[0] * ln_sorted[0] + ln_sorted[1] * ln_sorted[1] + ln_sorted[2] * ln_sorted[2]);
+        sc = 1.0f / fmaxf(r, 1e-20f);
+    }
+    row[0] = __float2bfloat16(ln_sorted[0] * sc);
+    row[1] = __float2bfloat16(ln_sorted[1] * sc);
+    row[2] = __float2bfloat16(ln_sorted[2] * sc);
     row[3] = __float2bfloat16(mat == 1 ? q : 0.0f);
     row[4] = __float2bfloat16(mat == 0 ? 1.0f : 0.0f);
     row[5] = __float2bfloat16(mat == 1 ? 1.0f : 0.0f);
 #pragma unroll
     for (int k = 6; k < kMlpIn; ++k) row[k] = __float2bfloat16(0.0f);
+    return sc;
 }
 
 // sort three values descending, remembering the permutation (perm[i] = source index)

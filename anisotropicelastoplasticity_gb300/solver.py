@@ -420,7 +420,7 @@ class HybridSolver:
         self._check(self._lib.aep_get_harvest_count(self._h, C.byref(cnt)))
         return cnt.value
 
-    def set_return_map(self, mlp=None, tolerance: float = 1e-4):
+    def set_return_map(self, mlp=None, tolerance: float = 1e-3):
         """Use a trained ReturnMapMLP (None: the exact mapping of the reference)."""
         self._mlp_ref = mlp
         self._check(self._lib.aep_set_return_map(self._h, mlp.handle if mlp is not None else None, tolerance))

@@ -262,6 +262,8 @@ def run_ours(args):
     out["clocks"] = clk.summary()
     if e2e is not None:
         out["e2e"] = e2e
+    if rank == 0 and not args.no_learned:
+        out["learned_vs_plain"] = run_learned_vs_plain(args, torch, flush)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, args.cpu_steps)
     if world > 1:
@@ -269,6 +271,148 @@ def run_ours(args):
 
         dist.destroy_process_group()
     return out if rank == 0 else None
+
+
+def stress(F, plastic, mat, prm, vol=1.0):
+    """Per-particle stress V P(F) F^T of the reference's two laws (HybridSolver.cpp:314-339)
+    evaluated in FP64 on the host, for error statistics; F: (N, 3, 3)."""
+    F = np.asarray(F, np.float64)
+    U, S, Vt = np.linalg.svd(F)
+    out = np.zeros_like(F)
+    snow = mat == 0
+    if snow.any():
+        E, nu, xi = prm.snow.E, prm.snow.nu, prm.snow.xi
+        lam0, mu0 = E * nu / (1 + nu) / (1 - 2 * nu), E / 2 / (1 + nu)
+        hard = np.exp(xi * (1 - plastic[snow]))
+        Fs = F[snow]
+        R = U[snow] @ Vt[snow]
+        J = np.linalg.det(Fs)
+        cof = np.linalg.inv(Fs).transpose(0, 2, 1) * J[:, None, None]
+        P = 2 * (mu0 * hard)[:, None, None] * (Fs - R) + ((lam0 * hard) * (J - 1))[:, None, None] * cof
+        out[snow] = P @ Fs.transpose(0, 2, 1)
+    sand = mat == 1
+    if sand.any():
+        E, nu = prm.sand.E, prm.sand.nu
+        lam, mu = E * nu / (1 + nu) / (1 - 2 * nu), E / 2 / (1 + nu)
+        ln = np.log(S[sand])
+        d = (2 * mu * ln + lam * ln.sum(1, keepdims=True)) / S[sand]
+        P = U[sand] @ (d[:, :, None] * Vt[sand])
+        out[sand] = P @ F[sand].transpose(0, 2, 1)
+    return out * np.asarray(vol, np.float64).reshape(-1, 1, 1)
+
+
+def rel_stats(a, b):
+    """Per-particle |P_gpu - P_fp64| / max(|P_fp64|, 1e-2 * rms |P_fp64|) (Frobenius)."""
+    na = np.linalg.norm((a - b).reshape(len(a), -1), axis=1)
+    nb = np.linalg.norm(b.reshape(len(b), -1), axis=1)
+    floor = 1e-2 * np.sqrt(np.mean(nb ** 2))
+    r = na / np.maximum(nb, floor)
+    return {"median": float(np.median(r)), "p99": float(np.percentile(r, 99)), "max": float(r.max()),
+            "particles": int(len(r)), "floor": float(floor)}
+
+
+def run_learned_vs_plain(args, torch, flush):
+    """Train the learned return map on pairs harvested from the snow block and the sand
+    column (configs 0-1), then time the plain and the learned step on the mixed
+    snow+sand collision (2,097,152 particles, 256^3), and measure the stress error of
+    both against the FP64 oracle on a bounded sample of the same scene."""
+    from anisotropicelastoplasticity_gb300 import HybridSolver, scenes
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP, harvest_records
+
+    t0 = time.perf_counter()
+    cap = args.harvest // 2
+    recs = torch.cat([harvest_records(scenes.snow_block(), steps=200, capacity=cap, stride=1),
+                      harvest_records(scenes.sand_column(), steps=100, capacity=cap, stride=16)])
+    n_rec = len(recs)
+    t1 = time.perf_counter()
+    mlp = ReturnMapMLP(seed=0)
+    _, loss0 = mlp.gradient(recs.data_ptr(), n_rec)
+    mlp.train(recs.data_ptr(), n_rec, steps=args.train_steps, batch=8192, lr=2e-3, lr_final=2e-5)
+    _, loss1 = mlp.gradient(recs.data_ptr(), n_rec)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+
+    def timed(scene, learned, steps):
+        s = HybridSolver(scene.particles, scene.grid, scene.params)
+        s.set_level_set(scene.levelset)
+        stream = torch.cuda.Stream()
+        s.set_stream(stream.cuda_stream)
+        s.init_volumes()
+        if learned:
+            s.set_return_map(mlp, args.learned_tol)
+        for _ in range(3):
+            s.step(scene.dt)
+        s.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        acc = fb = 0
+        with torch.cuda.stream(stream):
+            for a, b in ev:
+                flush.zero_()
+                a.record(stream)
+                s.step(scene.dt)
+                b.record(stream)
+                st = s.stats()
+                acc += st["learned_accepted"]
+                fb += st["learned_fallbacks"]
+        s.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        s.close()
+        return len(scene.particles) * steps / (ms * 1e-3), acc, fb
+
+    big = scenes.snow_sand_collision()
+    plain_v, _, _ = timed(big, False, args.learned_steps)
+    learned_v, acc, fb = timed(big, True, args.learned_steps)
+
+    # stress error against the FP64 oracle on a bounded sample of the same scene
+    from oracle.oracle import Oracle
+
+    small = scenes.snow_sand_collision(n=args.err_particles, res=128, seed=3)
+    # start from strained states (+-1% random elastic strain) so that every particle
+    # carries stress and the sand return mapping is active from the first step
+    rng = np.random.default_rng(11)
+    ps = small.particles
+    ps.elastic_deformation_gradients = np.eye(3) + 0.01 * rng.standard_normal((len(ps), 3, 3))
+    o = Oracle(small.grid, small.params, threads=os.cpu_count() or 1)
+    o.set_particle_system(small.particles)
+    o.set_level_set(small.levelset)
+    o.init(volumes=True)
+    runs = {}
+    for name, learned in (("plain", False), ("learned", True)):
+        s = HybridSolver(small.particles, small.grid, small.params)
+        s.set_level_set(small.levelset)
+        s.init_volumes()
+        if learned:
+            s.set_return_map(mlp, args.learned_tol)
+        runs[name] = s
+    errs = {"plain": [], "learned": []}
+    mat = small.particles.material
+    for k in range(args.err_steps):
+        o.step(small.dt)
+        op = o.get_particles()
+        ref = stress(op["elastic_deformation_gradients"], op["plastic"], mat, small.params, op["volumes"])
+        for name, s in runs.items():
+            s.step(small.dt)
+            gp = s.get_particles()
+            errs[name] = rel_stats(stress(gp["elastic_deformation_gradients"], gp["plastic"], mat, small.params,
+                                          gp["volumes"]), ref)
+    for s in runs.values():
+        s.close()
+    t3 = time.perf_counter()
+    return {
+        "workload": "snow_sand_collision", "particles": len(big.particles), "grid": [256] * 3, "dt": big.dt,
+        "steps": args.learned_steps, "plain": plain_v, "learned": learned_v, "learned_over_plain": learned_v / plain_v,
+        "fallback_rate": fb / max(acc + fb, 1), "learned_tolerance_rel": args.learned_tol,
+        "stress_rel_err_vs_fp64": {"plain": errs["plain"], "learned": errs["learned"],
+                                   "sample": f"{args.err_particles} particles of the same scene on 128^3 with "
+                                             f"+-1% random initial elastic strain, after {args.err_steps} steps, "
+                                             f"per-particle |dP| / max(|P|, 1e-2 rms|P|)"},
+        "training": {"records": n_rec, "sources": "snow_block 200 steps + sand_column 100 steps (stride 16)",
+                     "steps": args.train_steps, "batch": 8192, "loss_before": loss0, "loss_after": loss1,
+                     "harvest_s": t1 - t0, "train_s": t2 - t1},
+        "note": "the MLP cannot skip the SVD and is checked against the exact mapping in the kernel, so it adds "
+                "work to the step; reported as measured",
+        "wall_s": t3 - t0,
+    }
 
 
 def run_e2e(args, solver, sc, stream):
@@ -332,6 +476,13 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-steps", type=int, default=10)
+    ap.add_argument("--learned-tol", type=float, default=1e-3)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--harvest", type=int, default=4000000)
+    ap.add_argument("--err-particles", type=int, default=65536)
+    ap.add_argument("--err-steps", type=int, default=5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":

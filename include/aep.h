@@ -158,7 +158,9 @@ aep_status aep_solver_destroy(aep_solver* s);
  * B: 9N (see top), may be NULL (zero); Fe, Fp: 9N (3x3 column-major per
  * particle), Fp may be NULL (identity); m, vol: N; plastic: N, the sand
  * plasticAmount (ParticleSystem.h:31), may be NULL (zero); material: N tags.
- * For snow particles the scalar J_P = det(Fp) is derived from Fp.             */
+ * For snow particles the scalar J_P is det(Fp) when Fp is given, else `plastic`
+ * (what aep_get_particles returns for snow), else 1.  Re-uploading the same
+ * number of particles keeps the device's current particle order.             */
 aep_status aep_set_particles(aep_solver* s, int64_t n,
                              const double* x, const double* v, const double* B,
                              const double* Fe, const double* Fp,
@@ -307,8 +309,9 @@ aep_status aep_set_harvest(aep_solver* s, float* d_records, int64_t capacity, in
 /* Number of records written so far (capped at the capacity). */
 aep_status aep_get_harvest_count(aep_solver* s, int64_t* count);
 /* Use the learned return map in later steps (NULL: the exact mapping).  Every
- * prediction is checked in the kernel against the exact mapping; if a projected
- * log singular value differs by more than `tolerance`, the exact value is used
+ * prediction is checked in the kernel against the exact mapping; if the projected
+ * log singular values differ by more than `tolerance` times their largest
+ * magnitude (absolute floor 1e-5), the exact value is used
  * (aep_stats.learned_fallbacks).  The handle must outlive its use.             */
 aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance);
 

@@ -9,7 +9,8 @@ pin against central finite differences.
 
 Packed parameters (9928 floats): W1^T [64][16], W2^T [64][64], W3^T [64][64],
 W4^T [8][64], b1 [64], b2 [64], b3 [64], b4 [8].  Records: [ln s0, ln s1, ln s2,
-q, material, d0, d1, d2]; features and targets are scaled by 50.
+q, material, d0, d1, d2]; features and targets are scaled per record (sand by
+1/|ln s|, snow by 50), as the kernels do.
 """
 from __future__ import annotations
 
@@ -41,12 +42,24 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+def scales(rec):
+    """Per-record scaling of features and outputs: sand 1/|ln s| (the cone projection
+    is positively homogeneous), snow 50."""
+    rec = np.asarray(rec, np.float64)
+    ln = rec[:, 0:3].astype(np.float32)
+    r = np.sqrt((ln * ln).sum(1, dtype=np.float32)).astype(np.float32)
+    sand = rec[:, 4].astype(int) == 1
+    sc = np.full(len(rec), np.float32(LN_SCALE), np.float32)
+    sc[sand] = np.float32(1.0) / np.maximum(r[sand], np.float32(1e-20))
+    return sc
+
+
 def features(rec, rnd=True):
     rec = np.asarray(rec, np.float64)
     n = len(rec)
     X = np.zeros((n, 16))
-    ln = rec[:, 0:3].astype(np.float32) * np.float32(LN_SCALE)
-    X[:, 0:3] = ln
+    sc = scales(rec)
+    X[:, 0:3] = rec[:, 0:3].astype(np.float32) * sc[:, None]
     mat = rec[:, 4].astype(int)
     X[:, 3] = np.where(mat == 1, rec[:, 3].astype(np.float32), 0.0)
     X[:, 4] = (mat == 0)
@@ -83,7 +96,7 @@ def loss_and_grad(p, rec, bf=True):
     n = len(rec)
     f = forward(p, rec, bf)
     r = bf16 if bf else (lambda a: np.asarray(a, np.float64))
-    T = rec[:, 5:8] * LN_SCALE
+    T = rec[:, 5:8] * scales(rec)[:, None].astype(np.float64)
     diff = f["Y"][:, :3] - T
     loss = float((diff ** 2).sum() / (3.0 * n))
     dY = np.zeros((n, 8))
@@ -102,4 +115,4 @@ def loss_and_grad(p, rec, bf=True):
 
 def predict(p, rec, bf=True):
     """Predicted corrections d (ln units), [n, 3]."""
-    return forward(p, rec, bf)["Y"][:, :3] / LN_SCALE
+    return forward(p, rec, bf)["Y"][:, :3] / scales(rec)[:, None].astype(np.float64)
