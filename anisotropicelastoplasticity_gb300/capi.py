@@ -95,9 +95,24 @@ class aep_stats(C.Structure):
     ]
 
 
+class aep_solve_state(C.Structure):
+    _fields_ = [
+        ("t", C.c_double),
+        ("inner_t", C.c_double),
+        ("dt", C.c_double),
+        ("steps", C.c_int64),
+        ("frames", C.c_int32),
+        ("frame_done", C.c_int32),
+        ("reserved", C.c_double * 4),
+    ]
+
+
 _dp = C.POINTER(C.c_double)
 _u8p = C.POINTER(C.c_uint8)
 _solver_p = C.c_void_p
+
+# int32_t (*)(aep_solver*, const aep_solve_state*, void*)
+SOLVE_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.POINTER(aep_solve_state), C.c_void_p)
 
 # name -> (restype, argtypes); every symbol declared in include/aep.h
 SIGNATURES = {
@@ -117,6 +132,16 @@ SIGNATURES = {
     "aep_get_grid": (C.c_int, [_solver_p, _dp, _dp, _dp, _dp]),
     "aep_get_stats": (C.c_int, [_solver_p, C.POINTER(aep_stats)]),
     "aep_step_stage": (C.c_int, [_solver_p, C.c_double, C.c_int32]),
+    "aep_step_split": (C.c_int, [_solver_p, C.c_double, C.c_double]),
+    "aep_set_fixed_vertices": (C.c_int, [_solver_p, C.c_int64, _dp]),
+    "aep_set_solve_callback": (C.c_int, [_solver_p, SOLVE_FN, C.c_void_p]),
+    "aep_set_max_steps": (C.c_int, [_solver_p, C.c_int64]),
+    "aep_solve": (C.c_int, [_solver_p, C.c_double, C.c_double, C.c_double]),
+    "aep_get_solve_state": (C.c_int, [_solver_p, C.POINTER(aep_solve_state)]),
+    "aep_get_weights": (C.c_int, [_solver_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _dp, _dp]),
+    "aep_checkpoint_size": (C.c_int, [_solver_p, C.POINTER(C.c_int64)]),
+    "aep_checkpoint_save": (C.c_int, [_solver_p, C.c_void_p, C.c_int64]),
+    "aep_checkpoint_load": (C.c_int, [_solver_p, C.c_void_p, C.c_int64]),
     "aep_set_stream": (C.c_int, [_solver_p, C.c_void_p]),
     "aep_set_profiling": (C.c_int, [_solver_p, C.c_int32]),
     "aep_get_phase_times": (C.c_int, [_solver_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

@@ -81,6 +81,17 @@ struct aep_solver {
     double phase_ms[AEP_NUM_PHASES] = {};
     int64_t timed_steps = 0;
     unsigned long long* check = nullptr;  // upload validation result
+    // fixed cloth vertices (vertex indices 0..nv-1)
+    int32_t* fixed = nullptr;
+    int nfixed = 0;
+    // adaptive solve loop: device state, its pinned host copy, callback
+    SolveState* solve = nullptr;
+    SolveState* solve_host = nullptr;
+    DevStats* stats_host = nullptr;
+    aep_solve_fn solve_fn = nullptr;
+    void* solve_user = nullptr;
+    int64_t max_steps = 0;
+    aep_solve_state solve_last{};
     std::string err;
 };
 
@@ -185,6 +196,9 @@ void free_mesh(aep_solver* s) {
     s->vforce = nullptr;
     s->slot_of = s->curidx_of = nullptr;
     s->nv = s->nf = 0;
+    cudaFree(s->fixed);
+    s->fixed = nullptr;
+    s->nfixed = 0;
 }
 
 void build_parrays(aep_solver* s, int which) {
@@ -444,6 +458,9 @@ aep_status aep_solver_destroy(aep_solver* s) {
     cudaFree(s->dforce);
     cudaFree(s->harvest_count);
     cudaFree(s->check);
+    cudaFree(s->solve);
+    cudaFreeHost(s->solve_host);
+    cudaFreeHost(s->stats_host);
     for (int r = 0; r < aep_solver::kRing; ++r)
         for (int p = 0; p <= AEP_NUM_PHASES; ++p)
             if (s->ev[r][p]) cudaEventDestroy(s->ev[r][p]);
@@ -721,11 +738,23 @@ aep_status aep_init_volumes(aep_solver* s) {
     return check_overflow(s);
 }
 
-aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
-    if (!s) return AEP_INVALID_ARG;
+namespace {
+
+// One step up to `stage`.  adaptive: the kernels read Dt from the solve state
+// and reduce max |v| into it (aep_solve); otherwise dt_force / dt are used.
+aep_status step_impl(aep_solver* s, double dt_force, double dt, int32_t stage, bool adaptive) {
     if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_step: no particles");
-    if (!(dt > 0.0) || !std::isfinite(dt)) return fail(s, AEP_INVALID_ARG, "aep_step: dt must be > 0");
+    if (!adaptive && (!(dt > 0.0) || !std::isfinite(dt) || !(dt_force > 0.0) || !std::isfinite(dt_force)))
+        return fail(s, AEP_INVALID_ARG, "aep_step: dt must be > 0");
     if (stage < AEP_STAGE_P2G || stage > AEP_STAGE_FULL) return fail(s, AEP_INVALID_ARG, "aep_step: bad stage");
+    if (adaptive) {
+        s->kp.dt_dev = s->solve->dt;
+        s->kp.vmax2 = s->solve->vmax2;
+    }
+    struct Restore {
+        KParams& k;
+        ~Restore() { k.dt_dev = nullptr; k.vmax2 = nullptr; }
+    } restore{s->kp};
     const bool timed = s->profiling && stage == AEP_STAGE_FULL;
     const bool prof_saved = s->profiling;
     if (s->profiling && !timed) s->profiling = false;  // only whole steps are timed
@@ -741,7 +770,11 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
         s->dirty_grid = true;
         return AEP_OK;
     }
-    const float dtf = (float)dt;
+    if (adaptive) {
+        launch_solve_dt(s->solve, 0, s->stream);
+        CKLAUNCH();
+    }
+    const float dtf = (float)dt_force;
     const PArrays& P = s->P[s->cur];
     const MeshArrays M = mesh_arrays(s);
     launch_force(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, dtf, s->dstats, M, s->stream);
@@ -758,13 +791,21 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
     }
     launch_grid(s->kp, s->G, dtf, 0, nullptr, s->grid_blocks, s->stream);
     CKLAUNCH();
+    if (s->nfixed > 0) {
+        launch_fixed_vertices(s->kp, P, s->G, M, s->fixed, s->nfixed, s->stream);
+        CKLAUNCH();
+    }
+    if (adaptive) {
+        launch_solve_dt(s->solve, 1, s->stream);
+        CKLAUNCH();
+    }
     if (stage == AEP_STAGE_GRID) return AEP_OK;
     if (timed) mark(s, AEP_PHASE_G2P);
     const int nx = 1 - s->cur;
     Harvest H{s->harvest, s->harvest_count, s->harvest_cap, s->harvest_stride};
     MlpParams mp{};
     if (s->mlp) mp = mlp_device_params(s->mlp);
-    launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, dtf, s->keys, s->dstats, M, s->stream, H,
+    launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, (float)dt, s->keys, s->dstats, M, s->stream, H,
                s->mlp ? &mp : nullptr, (float)s->learned_tol);
     CKLAUNCH();
     if (timed) {
@@ -779,7 +820,292 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
     return AEP_OK;
 }
 
-aep_status aep_step(aep_solver* s, double dt) { return aep_step_stage(s, dt, AEP_STAGE_FULL); }
+}  // namespace
+
+aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage) {
+    if (!s) return AEP_INVALID_ARG;
+    return step_impl(s, dt, dt, stage, false);
+}
+
+aep_status aep_step(aep_solver* s, double dt) {
+    if (!s) return AEP_INVALID_ARG;
+    return step_impl(s, dt, dt, AEP_STAGE_FULL, false);
+}
+
+aep_status aep_step_split(aep_solver* s, double dt_force, double dt) {
+    if (!s) return AEP_INVALID_ARG;
+    return step_impl(s, dt_force, dt, AEP_STAGE_FULL, false);
+}
+
+aep_status aep_set_solve_callback(aep_solver* s, aep_solve_fn fn, void* user) {
+    if (!s) return AEP_INVALID_ARG;
+    s->solve_fn = fn;
+    s->solve_user = user;
+    return AEP_OK;
+}
+
+aep_status aep_set_max_steps(aep_solver* s, int64_t max_steps) {
+    if (!s) return AEP_INVALID_ARG;
+    if (max_steps < 0) return fail(s, AEP_INVALID_ARG, "aep_set_max_steps: max_steps must be >= 0");
+    s->max_steps = max_steps;
+    return AEP_OK;
+}
+
+aep_status aep_get_solve_state(aep_solver* s, aep_solve_state* out) {
+    if (!s || !out) return AEP_INVALID_ARG;
+    *out = s->solve_last;
+    return AEP_OK;
+}
+
+aep_status aep_solve(aep_solver* s, double cfl, double maxt, double alpha) {
+    (void)alpha;  // HybridSolver::updateParticleVelocities_ ignores it (:739-758)
+    if (!s) return AEP_INVALID_ARG;
+    if (!(cfl > 0.0) || !std::isfinite(cfl) || !std::isfinite(maxt))
+        return fail(s, AEP_INVALID_ARG, "aep_solve: need cfl > 0 and a finite maxt");
+    if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_solve: no particles");
+    if (!s->solve) {
+        CK(cudaMalloc(&s->solve, sizeof(SolveState)));
+        CK(cudaMallocHost(&s->solve_host, sizeof(SolveState)));
+        CK(cudaMallocHost(&s->stats_host, sizeof(DevStats)));
+    }
+    // the first P2G of solve computes densities and volumes (:853-855)
+    aep_status st = aep_init_volumes(s);
+    if (st) return st;
+    double hmin = 1e300;
+    for (int a = 0; a < 3; ++a) hmin = std::min(hmin, (s->grid.max[a] - s->grid.min[a]) / s->grid.res[a]);
+    SolveState init{};
+    init.cfl = cfl;
+    init.inv_hmin = 1.0 / hmin;
+    CK(cudaMemcpyAsync(s->solve, &init, sizeof(init), cudaMemcpyHostToDevice, s->stream));
+    s->solve_last = aep_solve_state{};
+    double t = 0.0;
+    int64_t it = 0;
+    while (t <= maxt && (s->max_steps <= 0 || it < s->max_steps)) {
+        st = step_impl(s, 0.0, 0.0, AEP_STAGE_FULL, true);
+        if (st) return st;
+        CK(cudaMemcpyAsync(s->solve_host, s->solve, sizeof(SolveState), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(s->stats_host, s->dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->stats_host->overflow) return fail(s, AEP_OVERFLOW, "fixed-point grid accumulator overflow");
+        const SolveState& h = *s->solve_host;
+        t = h.t;
+        ++it;
+        aep_solve_state& o = s->solve_last;
+        o.t = h.t;
+        o.inner_t = h.inner;
+        o.dt = h.Dt;
+        o.steps = it;
+        o.frames = h.frame;
+        o.frame_done = h.frame_flag;
+        if (s->solve_fn && s->solve_fn(s, &o, s->solve_user) != 0) break;
+    }
+    return AEP_OK;
+}
+
+aep_status aep_set_fixed_vertices(aep_solver* s, int64_t nv, const double* vertex_is_fixed) {
+    if (!s) return AEP_INVALID_ARG;
+    cudaFree(s->fixed);
+    s->fixed = nullptr;
+    s->nfixed = 0;
+    if (!vertex_is_fixed) return AEP_OK;
+    if (s->nv <= 0 || nv != s->nv)
+        return fail(s, AEP_INVALID_ARG, "aep_set_fixed_vertices: need one value per mesh vertex (set the mesh first)");
+    std::vector<int32_t> ids;
+    for (int64_t v = 0; v < nv; ++v)
+        if (vertex_is_fixed[v] != 0.0) ids.push_back((int32_t)v);
+    if (ids.empty()) return AEP_OK;
+    CK(cudaMalloc(&s->fixed, sizeof(int32_t) * ids.size()));
+    CK(cudaMemcpy(s->fixed, ids.data(), sizeof(int32_t) * ids.size(), cudaMemcpyHostToDevice));
+    s->nfixed = (int)ids.size();
+    return AEP_OK;
+}
+
+aep_status aep_get_weights(aep_solver* s, int64_t count, const int64_t* ids, int64_t* nodes, double* w,
+                           double* grad) {
+    if (!s) return AEP_INVALID_ARG;
+    if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_get_weights: no particles");
+    if (count < 0 || (count > 0 && (!ids || !nodes || !w || !grad)) || count > (int64_t)INT32_MAX / 64)
+        return fail(s, AEP_INVALID_ARG, "aep_get_weights: need count >= 0 and non-null arrays");
+    for (int64_t q = 0; q < count; ++q)
+        if (ids[q] < 0 || ids[q] >= s->n) return fail(s, AEP_INVALID_ARG, "aep_get_weights: id out of range");
+    if (count == 0) return AEP_OK;
+    CK(cudaStreamSynchronize(s->stream));
+    // scratch: inverse id map, ids, then the three outputs
+    const size_t b_inv = sizeof(int32_t) * (size_t)s->n, b_ids = sizeof(int64_t) * (size_t)count;
+    const size_t b_nodes = sizeof(int64_t) * 64 * (size_t)count, b_w = sizeof(double) * 64 * (size_t)count;
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    char* buf = nullptr;
+    CK(cudaMalloc(&buf, up(b_inv) + up(b_ids) + up(b_nodes) + up(b_w) + 3 * b_w));
+    int32_t* inv = reinterpret_cast<int32_t*>(buf);
+    int64_t* dids = reinterpret_cast<int64_t*>(buf + up(b_inv));
+    int64_t* dn = reinterpret_cast<int64_t*>(buf + up(b_inv) + up(b_ids));
+    double* dw = reinterpret_cast<double*>(buf + up(b_inv) + up(b_ids) + up(b_nodes));
+    double* dg = reinterpret_cast<double*>(buf + up(b_inv) + up(b_ids) + up(b_nodes) + up(b_w));
+    aep_status st = AEP_OK;
+    cudaError_t e = cudaSuccess;
+    launch_inverse_ids((int)s->n, s->P[s->cur].id, inv, s->stream);
+    if ((e = cudaMemcpyAsync(dids, ids, b_ids, cudaMemcpyHostToDevice, s->stream)) == cudaSuccess) {
+        launch_query_weights(s->kp, s->P[s->cur], inv, dids, (int)count, dn, dw, dg, s->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nodes, dn, b_nodes, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w, dw, b_w, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(grad, dg, 3 * b_w, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) st = fail(s, AEP_CUDA_ERROR, cudaGetErrorString(e));
+    cudaFree(buf);
+    return st;
+}
+
+namespace {
+
+// checkpoint blob: header, then per item the float arrays of the current set
+// (n floats each), material tags, ids; the mesh faces and rest data; the fixed
+// vertex list
+struct CkptHeader {
+    char magic[8];
+    int32_t version, float_arrays;
+    int64_t n, np, nv, nf, steps;
+    aep_grid_desc grid;
+    aep_params prm;
+    double m_max;
+    double cloth[5];
+    int32_t nshapes, nfixed;
+    DevShape shapes[kMaxShapes];
+};
+constexpr char kCkptMagic[8] = {'A', 'E', 'P', 'C', 'K', 'P', 'T', '1'};
+constexpr int32_t kCkptVersion = 1;
+
+int float_arrays(const aep_params& p) { return kFloatArrays + (p.track_plastic_F ? kFpArrays : 0); }
+
+size_t ckpt_bytes(int64_t n, int64_t nf, int nfixed, int nfa) {
+    return sizeof(CkptHeader) + (size_t)n * (sizeof(float) * nfa + 1 + sizeof(int32_t)) +
+           (size_t)nf * (3 * sizeof(int32_t) + 6 * sizeof(float)) + (size_t)nfixed * sizeof(int32_t);
+}
+
+}  // namespace
+
+aep_status aep_checkpoint_size(aep_solver* s, int64_t* bytes) {
+    if (!s || !bytes) return AEP_INVALID_ARG;
+    if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_checkpoint_size: no particles");
+    *bytes = (int64_t)ckpt_bytes(s->n, s->nf, s->nfixed, float_arrays(s->prm));
+    return AEP_OK;
+}
+
+aep_status aep_checkpoint_save(aep_solver* s, void* buf, int64_t bytes) {
+    if (!s || !buf) return AEP_INVALID_ARG;
+    if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_checkpoint_save: no particles");
+    const int nfa = float_arrays(s->prm);
+    if (bytes != (int64_t)ckpt_bytes(s->n, s->nf, s->nfixed, nfa))
+        return fail(s, AEP_INVALID_ARG, "aep_checkpoint_save: bytes must be aep_checkpoint_size");
+    CK(cudaStreamSynchronize(s->stream));
+    CkptHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kCkptMagic, 8);
+    h.version = kCkptVersion;
+    h.float_arrays = nfa;
+    h.n = s->n;
+    h.np = s->np;
+    h.nv = s->nv;
+    h.nf = s->nf;
+    h.steps = s->steps;
+    h.grid = s->grid;
+    h.prm = s->prm;
+    h.m_max = s->m_max;
+    for (int k = 0; k < 5; ++k) h.cloth[k] = s->cloth[k];
+    h.nshapes = s->kp.nshapes;
+    h.nfixed = s->nfixed;
+    for (int k = 0; k < kMaxShapes; ++k) h.shapes[k] = s->kp.shapes[k];
+    char* p = static_cast<char*>(buf);
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    const ParticleSet& set = s->set[s->cur];
+    const size_t n = (size_t)s->n;
+    for (int k = 0; k < nfa; ++k, p += sizeof(float) * n)
+        CK(cudaMemcpy(p, set.f + (size_t)k * s->cap, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(p, set.mat, n, cudaMemcpyDeviceToHost));
+    p += n;
+    CK(cudaMemcpy(p, set.id, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    p += sizeof(int32_t) * n;
+    if (s->nf > 0) {
+        CK(cudaMemcpy(p, s->faces, sizeof(int32_t) * 3 * s->nf, cudaMemcpyDeviceToHost));
+        p += sizeof(int32_t) * 3 * s->nf;
+        CK(cudaMemcpy(p, s->rest, sizeof(float) * 6 * s->nf, cudaMemcpyDeviceToHost));
+        p += sizeof(float) * 6 * s->nf;
+    }
+    if (s->nfixed > 0) CK(cudaMemcpy(p, s->fixed, sizeof(int32_t) * s->nfixed, cudaMemcpyDeviceToHost));
+    return AEP_OK;
+}
+
+aep_status aep_checkpoint_load(aep_solver* s, const void* buf, int64_t bytes) {
+    if (!s || !buf) return AEP_INVALID_ARG;
+    CkptHeader h;
+    if (bytes < (int64_t)sizeof(h)) return fail(s, AEP_INVALID_ARG, "aep_checkpoint_load: truncated");
+    std::memcpy(&h, buf, sizeof(h));
+    if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != kCkptVersion)
+        return fail(s, AEP_INVALID_ARG, "aep_checkpoint_load: not a checkpoint of this version");
+    if (h.float_arrays != float_arrays(h.prm) || h.n <= 0 || h.n != h.np + h.nv + h.nf || h.np < 0 || h.nv < 0 ||
+        h.nf < 0 || (h.nf > 0) != (h.nv > 0) || h.nshapes < 0 || h.nshapes > kMaxShapes || h.nfixed < 0 ||
+        h.nfixed > h.nv || h.n > (int64_t)INT32_MAX / 2 || !(h.m_max > 0.0))
+        return fail(s, AEP_INVALID_ARG, "aep_checkpoint_load: inconsistent header");
+    if (bytes != (int64_t)ckpt_bytes(h.n, h.nf, h.nfixed, h.float_arrays))
+        return fail(s, AEP_INVALID_ARG, "aep_checkpoint_load: size does not match the header");
+    for (int a = 0; a < 3; ++a)
+        if (h.grid.res[a] != s->grid.res[a] || h.grid.min[a] != s->grid.min[a] || h.grid.max[a] != s->grid.max[a])
+            return fail(s, AEP_INVALID_ARG, "aep_checkpoint_load: the grid differs from the handle's");
+    CK(cudaStreamSynchronize(s->stream));
+    free_mesh(s);
+    free_particles(s);
+    s->cap = 0;
+    s->have_particles = false;
+    s->n = s->np = 0;
+    s->prm = h.prm;
+    s->m_max = h.m_max;
+    aep_status st = ensure_capacity(s, h.n);
+    if (st != AEP_OK) return st;
+    s->n = h.n;
+    s->np = h.np;
+    s->cur = 0;
+    fill_kparams(s);
+    s->kp.nshapes = h.nshapes;
+    for (int k = 0; k < kMaxShapes; ++k) s->kp.shapes[k] = h.shapes[k];
+    const char* p = static_cast<const char*>(buf) + sizeof(h);
+    const ParticleSet& set = s->set[0];
+    const size_t n = (size_t)h.n;
+    for (int k = 0; k < h.float_arrays; ++k, p += sizeof(float) * n)
+        CK(cudaMemcpy(set.f + (size_t)k * s->cap, p, sizeof(float) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(set.mat, p, n, cudaMemcpyHostToDevice));
+    p += n;
+    CK(cudaMemcpy(set.id, p, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    p += sizeof(int32_t) * n;
+    if (h.nf > 0) {
+        s->nv = h.nv;
+        s->nf = h.nf;
+        for (int k = 0; k < 5; ++k) s->cloth[k] = h.cloth[k];
+        CK(cudaMalloc(&s->faces, sizeof(int32_t) * 3 * h.nf));
+        CK(cudaMalloc(&s->rest, sizeof(float) * 6 * h.nf));
+        CK(cudaMalloc(&s->estress, sizeof(float) * 9 * h.nf));
+        CK(cudaMalloc(&s->vforce, sizeof(unsigned long long) * 3 * h.nv));
+        CK(cudaMalloc(&s->slot_of, sizeof(int32_t) * n));
+        CK(cudaMalloc(&s->curidx_of, sizeof(int32_t) * n));
+        CK(cudaMemcpy(s->faces, p, sizeof(int32_t) * 3 * h.nf, cudaMemcpyHostToDevice));
+        p += sizeof(int32_t) * 3 * h.nf;
+        CK(cudaMemcpy(s->rest, p, sizeof(float) * 6 * h.nf, cudaMemcpyHostToDevice));
+        p += sizeof(float) * 6 * h.nf;
+        CK(cudaMemset(s->vforce, 0, sizeof(unsigned long long) * 3 * h.nv));
+    }
+    if (h.nfixed > 0) {
+        CK(cudaMalloc(&s->fixed, sizeof(int32_t) * h.nfixed));
+        CK(cudaMemcpy(s->fixed, p, sizeof(int32_t) * h.nfixed, cudaMemcpyHostToDevice));
+        s->nfixed = h.nfixed;
+    }
+    s->steps = h.steps;
+    s->have_particles = true;
+    s->keys_valid = false;
+    s->stepped_since_upload = h.steps > 0;
+    s->last_stage = 0;
+    return AEP_OK;
+}
 
 aep_status aep_synchronize(aep_solver* s) {
     if (!s) return AEP_INVALID_ARG;

@@ -49,6 +49,35 @@ struct KParams {
     int nshapes;
     DevShape shapes[kMaxShapes];
     float cell_volume;
+    // adaptive time stepping (HybridSolver::solve): when set, the force pass and
+    // grid update take dt_dev[0] and the G2P takes dt_dev[1] instead of their
+    // dt arguments, and the normalisation / grid update reduce max |v|^2 into
+    // vmax2[0] / vmax2[1] (float bits; non-negative floats order like integers)
+    const float* dt_dev;
+    unsigned int* vmax2;
+};
+
+__device__ __forceinline__ float step_dt(const KParams& P, float dt, int which) {
+    return P.dt_dev ? P.dt_dev[which] : dt;
+}
+
+// warp max of a non-negative float, one atomic per warp (all lanes call it)
+__device__ __forceinline__ void warp_max_atomic(unsigned int* dst, float v2) {
+    unsigned int b = __float_as_uint(v2);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if ((threadIdx.x & 31) == 0 && b) atomicMax(dst, b);
+}
+
+// device state of the adaptive solve loop (HybridSolver.cpp:859-892)
+struct SolveState {
+    double cfl, inv_hmin;  // Dt = cfl / max(300, max|v| / hmin)
+    double t, inner, Dt;   // simulated time, time inside the current frame, current Dt
+    int initialized;       // the first Dt comes from the P2G velocities (:860)
+    int frame, frame_flag; // frames completed; this step completed a frame
+    int steps;
+    float dt[2];           // Dt for the force pass / grid update, Dt for the G2P
+    unsigned int vmax2[2]; // max |v|^2 after the normalisation / the grid update
 };
 
 // Particle state, structure of arrays.

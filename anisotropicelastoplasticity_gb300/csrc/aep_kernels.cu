@@ -235,6 +235,7 @@ __global__ void k_normalize(KParams P, GArrays G, DevStats* st) {
     long long sm_ = 0, sx = 0, sy = 0, sz = 0;
     unsigned long long cnt = 0;
     bool ovf = false;
+    float vmax = 0.0f;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         uint32_t node = ((uint32_t)G.active[i >> 6] << 6) | (uint32_t)(i & 63);
         longlong2* a2 = reinterpret_cast<longlong2*>(G.acc + 4ull * node);
@@ -246,6 +247,7 @@ __global__ void k_normalize(KParams P, GArrays G, DevStats* st) {
             float inv = 1.0f / m;
             out = make_float4(__ll2float_rn(a.y) * P.inv_mom_scale * inv, __ll2float_rn(b.x) * P.inv_mom_scale * inv,
                               __ll2float_rn(b.y) * P.inv_mom_scale * inv, m);
+            vmax = fmaxf(vmax, out.x * out.x + out.y * out.y + out.z * out.z);
         }
         const long long lim = 1ll << 61;
         ovf |= (a.x > lim) | (a.y > lim) | (a.y < -lim) | (b.x > lim) | (b.x < -lim) | (b.y > lim) | (b.y < -lim);
@@ -254,6 +256,7 @@ __global__ void k_normalize(KParams P, GArrays G, DevStats* st) {
         a2[1] = make_longlong2(0, 0);
         sm_ += a.x; sx += a.y; sy += b.x; sz += b.y;
     }
+    if (P.vmax2) warp_max_atomic(P.vmax2 + 0, vmax);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         sm_ += __shfl_xor_sync(0xffffffffu, sm_, o);
@@ -404,6 +407,7 @@ __global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur
                                                        const int32_t* __restrict__ perm, int n, GArrays G,
                                                        float dt_force, DevStats* st, MeshArrays M) {
     __shared__ float4 sm4[(kFrcThreads / 32) * kFrcWarpBuf];
+    dt_force = step_dt(P, dt_force, 0);
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const buf = sm4 + wid * kFrcWarpBuf;
     const long chunk0 = ((long)blockIdx.x * (kFrcThreads / 32) + wid) * 32;
@@ -524,6 +528,7 @@ __global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur
 __global__ void k_cloth_force(KParams P, PArrays cur, MeshArrays M, float dt_force) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= M.nf) return;
+    dt_force = step_dt(P, dt_force, 0);
     const int pc = M.curidx_of[M.ebase + e];
     float D[9], Q[9], R[9];
 #pragma unroll
@@ -553,6 +558,9 @@ __global__ void k_cloth_force(KParams P, PArrays cur, MeshArrays M, float dt_for
 __global__ void k_grid(KParams P, GArrays G, float dt_force, int write_force, double* force_out) {
     const int nact = *G.nactive;
     const long total = (long)nact * 64;
+    dt_force = step_dt(P, dt_force, 0);
+    float vmax = 0.0f;  // max |v|^2 after the update, before collision (RegularGrid.cpp:188-200, HS:878)
+    // the loop trip count differs between threads: the warp reduction runs after it
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         const uint32_t blk = (uint32_t)G.active[i >> 6];
         const uint32_t node = (blk << 6) | (uint32_t)(i & 63);
@@ -566,6 +574,7 @@ __global__ void k_grid(KParams P, GArrays G, float dt_force, int write_force, do
             float vx = v4.x + __ll2float_rn(a.y) * inv + dt_force * P.gravity[0];
             float vy = v4.y + __ll2float_rn(b.x) * inv + dt_force * P.gravity[1];
             float vz = v4.z + __ll2float_rn(b.y) * inv + dt_force * P.gravity[2];
+            vmax = fmaxf(vmax, vx * vx + vy * vy + vz * vz);
             bf = make_float4(vx, vy, vz, 0.f);
             // node position (unpadded coordinates)
             uint32_t bx = blk % (uint32_t)P.nb[0], r = blk / (uint32_t)P.nb[0];
@@ -614,6 +623,103 @@ __global__ void k_grid(KParams P, GArrays G, float dt_force, int write_force, do
         a2[1] = make_longlong2(0, 0);
         if ((i & 63) == 0) G.flag[blk] = 0u;
     }
+    if (P.vmax2) warp_max_atomic(P.vmax2 + 1, vmax);
+}
+
+// Fixed cloth vertices (HybridSolver.cpp:513-550): for every node in the stencil
+// of a fixed vertex (positive weight on all three axes, inside the grid), zero the
+// velocity and the before-friction velocity of the 3x3x3 nodes around it.  The
+// neighbours are addressed by the reference's linear index k*Rx*Ry + j*Rx + i
+// and kept when 0 <= index < Rx*Ry*Rz, so i +- 1 wraps into the next row as in
+// the reference.  One thread per (fixed vertex, stencil node, neighbour).
+__global__ void k_fixed_vertices(KParams P, PArrays cur, GArrays G, MeshArrays M, const int32_t* __restrict__ fixed,
+                                 int nfixed) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)nfixed * 64 * 27) return;
+    const int fv = (int)(t / (64 * 27)), r = (int)(t % (64 * 27));
+    const int o = r / 27, nb = r % 27;
+    const int pj = M.curidx_of[M.vbase + fixed[fv]];
+    int cell[3];
+    float f[3], w[3][4], dw[3][4];
+    locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
+    particle_weights(P, cell, f, w, dw);
+    const int ox = o & 3, oy = (o >> 2) & 3, oz = o >> 4;
+    if (!(w[0][ox] > 0.0f && w[1][oy] > 0.0f && w[2][oz] > 0.0f)) return;
+    const long rx = P.res[0], ry = P.res[1], ng = rx * ry * P.res[2];
+    const long ri = cell[0] - 1 + ox, rj = cell[1] - 1 + oy, rk = cell[2] - 1 + oz;
+    const long idx = (rk + nb / 9 - 1) * rx * ry + (rj + (nb / 3) % 3 - 1) * rx + (ri + nb % 3 - 1);
+    if (idx < 0 || idx >= ng) return;
+    const int ix = (int)(idx % rx), iy = (int)((idx / rx) % ry), iz = (int)(idx / (rx * ry));
+    const uint32_t node = node_index(P, ix + 4, iy + 4, iz + 4);
+    float4 v = G.vel[node];
+    G.vel[node] = make_float4(0.f, 0.f, 0.f, v.w);
+    G.vbf[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Interpolation weights of selected items (one row of the reference's sparse
+// omegas / domegas_1..3 matrices, HybridSolver.cpp:18-97): one thread per (item,
+// stencil node); node = reference linear index k*Rx*Ry + j*Rx + i, or -1 where
+// the node is outside the grid or its weight is zero.  Entries are in ascending
+// node order, as in the row of the reference's column-sorted matrix.
+__global__ void k_query_weights(KParams P, PArrays cur, const int32_t* __restrict__ inv,
+                                const int64_t* __restrict__ ids, int count, int64_t* nodes, double* w, double* g) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)count * 64) return;
+    const int q = (int)(t >> 6), o = (int)(t & 63);
+    const int pj = inv[ids[q]];
+    int cell[3];
+    float f[3], wa[3][4], da[3][4];
+    locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
+    particle_weights(P, cell, f, wa, da);
+    const int ox = o & 3, oy = (o >> 2) & 3, oz = o >> 4;
+    const float wx = wa[0][ox], wy = wa[1][oy], wz = wa[2][oz];
+    if (wx > 0.0f && wy > 0.0f && wz > 0.0f) {
+        const long i = cell[0] - 1 + ox, j = cell[1] - 1 + oy, k = cell[2] - 1 + oz;
+        nodes[t] = (k * P.res[1] + j) * P.res[0] + i;
+        w[t] = (double)(wx * wy * wz);
+        g[3 * t + 0] = (double)(da[0][ox] * wy * wz);
+        g[3 * t + 1] = (double)(wx * da[1][oy] * wz);
+        g[3 * t + 2] = (double)(wx * wy * da[2][oz]);
+    } else {
+        nodes[t] = -1;
+        w[t] = 0.0;
+        g[3 * t + 0] = g[3 * t + 1] = g[3 * t + 2] = 0.0;
+    }
+}
+
+// One thread: the Dt logic of HybridSolver::solve.  phase 0 (after the P2G
+// normalisation): the first Dt of a solve comes from the P2G velocities (:860);
+// the force pass and grid update use the current Dt (:873, :877).  phase 1 (after
+// the grid update): Dt = CFL / max(300, max|v| / hmin) (:878) with the frame
+// clamp (:880-892); the G2P of this step and the force pass of the next use it.
+__global__ void k_solve_dt(SolveState* S, int phase) {
+    if (phase == 0) {
+        if (!S->initialized) {
+            const double v = sqrt((double)__uint_as_float(S->vmax2[0]));
+            S->Dt = S->cfl / fmax(3e2, v * S->inv_hmin);
+            S->initialized = 1;
+        }
+        S->dt[0] = (float)S->Dt;
+        S->vmax2[0] = 0u;
+        S->vmax2[1] = 0u;
+        S->frame_flag = 0;
+        return;
+    }
+    const double v = sqrt((double)__uint_as_float(S->vmax2[1]));
+    double Dt = S->cfl / fmax(3e2, v * S->inv_hmin);
+    const double frame_dt = 1.0 / 60.0;
+    if (S->inner + Dt >= frame_dt) {
+        Dt = frame_dt - S->inner;
+        S->t += frame_dt;
+        S->inner = 0.0;
+        S->frame_flag = 1;
+        S->frame += 1;
+    } else {
+        S->inner += Dt;
+    }
+    S->Dt = Dt;
+    S->dt[1] = (float)Dt;
+    S->steps += 1;
 }
 
 // clear accumulators and flags of the touched blocks (after a partial step)
@@ -741,6 +847,7 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
                                              DevStats* st, Harvest H) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
+    dt = step_dt(P, dt, 1);
     const int pj = perm[j];
     const int mat = cur.mat[pj];
     if (mat == kClothElement) return;  // elements follow their vertices (k_cloth_g2p)
@@ -916,6 +1023,7 @@ __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PAr
                                                      uint32_t* __restrict__ keys_next, DevStats* st, MlpParams mlp,
                                                      float tol) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    dt = step_dt(P, dt, 1);
     const MlpSmem W = mlp_smem_carve(smem_raw);
     mlp_load_smem(mlp, W, threadIdx.x, blockDim.x);
     __syncthreads();
@@ -1133,6 +1241,7 @@ __global__ void k_cloth_g2p(KParams P, PArrays cur, PArrays nxt, GArrays G, Mesh
                             uint32_t* __restrict__ keys_next, DevStats* st) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= M.nf) return;
+    dt = step_dt(P, dt, 1);
     const int id = M.ebase + e;
     const int j = M.slot_of[id];
     const int pc = M.curidx_of[id];
@@ -1411,6 +1520,17 @@ void launch_upload(int n, int mode, const double* src, float* const* dst, cudaSt
     if (n > 0)
         k_upload<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, src, dst[0], dst[1], dst[2], dst[3], dst[4], dst[5],
                                                     dst[6], dst[7], dst[8], map);
+}
+void launch_fixed_vertices(const KParams& P, const PArrays& cur, const GArrays& G, const MeshArrays& M,
+                           const int32_t* fixed, int nfixed, cudaStream_t s) {
+    const long threads = (long)nfixed * 64 * 27;
+    if (threads > 0) k_fixed_vertices<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(P, cur, G, M, fixed, nfixed);
+}
+void launch_solve_dt(SolveState* S, int phase, cudaStream_t s) { k_solve_dt<<<1, 1, 0, s>>>(S, phase); }
+void launch_query_weights(const KParams& P, const PArrays& cur, const int32_t* inv, const int64_t* ids, int count,
+                          int64_t* nodes, double* w, double* g, cudaStream_t s) {
+    const long threads = (long)count * 64;
+    if (threads > 0) k_query_weights<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(P, cur, inv, ids, count, nodes, w, g);
 }
 void launch_check_upload(int n, const double* m, const uint8_t* mat, unsigned long long* out, cudaStream_t s) {
     if (n > 0) k_check_upload<<<std::min(1024, blocks_for(n, 256)), 256, 0, s>>>(n, m, mat, out);

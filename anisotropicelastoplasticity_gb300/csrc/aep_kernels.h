@@ -24,6 +24,11 @@ void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, i
 void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s,
                    const int32_t* map = nullptr);
 void launch_inverse_ids(int n, const int32_t* id, int32_t* inv, cudaStream_t s);
+void launch_fixed_vertices(const KParams& P, const PArrays& cur, const GArrays& G, const MeshArrays& M,
+                           const int32_t* fixed, int nfixed, cudaStream_t s);
+void launch_solve_dt(SolveState* S, int phase, cudaStream_t s);
+void launch_query_weights(const KParams& P, const PArrays& cur, const int32_t* inv, const int64_t* ids, int count,
+                          int64_t* nodes, double* w, double* g, cudaStream_t s);
 void launch_check_upload(int n, const double* m, const uint8_t* mat, unsigned long long* out, cudaStream_t s);
 void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s,
                      int id_lo = 0, int id_hi = -1);

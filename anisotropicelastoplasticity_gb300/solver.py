@@ -316,6 +316,7 @@ class HybridSolver:
 
     def set_particle_system(self, ps: ParticleSystem):
         self.ps = ps
+        self._np = None
         n = len(ps)
         x = vec_to_ref(ps.positions)
         v = vec_to_ref(ps.velocities)
@@ -358,13 +359,96 @@ class HybridSolver:
         arr, n = ls.to_c()
         self._check(self._lib.aep_set_levelset(self._h, arr, n))
 
+    def bind_constraints(self, vertex_is_fixed):
+        """LagrangianMesh::bindConstraints (LagrangianMesh.cpp:354-363) on the attached
+        mesh: one value per vertex, nonzero = fixed; None removes the constraints."""
+        if vertex_is_fixed is None:
+            self._check(self._lib.aep_set_fixed_vertices(self._h, 0, None))
+            return
+        a = np.ascontiguousarray(vertex_is_fixed, np.float64)
+        self._keep_fixed = a
+        self._check(self._lib.aep_set_fixed_vertices(self._h, len(a), _dp(a)))
+
     # --- stepping ---------------------------------------------------------------
     def init_volumes(self):
         """First P2G of solve with evaluateVolumesAndDensities (HybridSolver.cpp:242-249)."""
         self._check(self._lib.aep_init_volumes(self._h))
 
-    def step(self, dt: float):
-        self._check(self._lib.aep_step(self._h, float(dt)))
+    def step(self, dt: float, dt_force: float | None = None):
+        """One loop body; dt_force (default dt) drives the force pass and grid update."""
+        if dt_force is None:
+            self._check(self._lib.aep_step(self._h, float(dt)))
+        else:
+            self._check(self._lib.aep_step_split(self._h, float(dt_force), float(dt)))
+
+    def solve(self, cfl: float, maxt: float, alpha: float = 0.0, callback=None, max_steps: int = 0) -> dict:
+        """HybridSolver::solve(CFL, maxt, alpha) (HybridSolver.cpp:827-989) with the
+        adaptive Dt on the device.  callback(state: dict) runs after every step
+        (state['frame_done'] marks a completed 1/60 s frame); returning True stops."""
+        cb = None
+        if callback is not None:
+            def _cb(_h, st, _u):
+                s_ = st.contents
+                d = dict(t=s_.t, inner_t=s_.inner_t, dt=s_.dt, steps=s_.steps, frames=s_.frames,
+                         frame_done=bool(s_.frame_done))
+                try:
+                    return 1 if callback(d) else 0
+                except Exception:  # an exception cannot cross the C frame: stop the solve
+                    self._cb_error = True
+                    return 1
+            cb = capi.SOLVE_FN(_cb)
+        self._cb_error = False
+        self._check(self._lib.aep_set_solve_callback(self._h, cb if cb is not None else capi.SOLVE_FN(), None))
+        self._check(self._lib.aep_set_max_steps(self._h, int(max_steps)))
+        try:
+            self._check(self._lib.aep_solve(self._h, float(cfl), float(maxt), float(alpha)))
+        finally:
+            self._lib.aep_set_solve_callback(self._h, capi.SOLVE_FN(), None)
+        if self._cb_error:
+            raise RuntimeError("solve callback raised")
+        return self.solve_state()
+
+    def weights(self, ids) -> tuple:
+        """Rows of evaluateInterpolationWeights_ (HybridSolver.cpp:18-97) for item ids at
+        the current positions: (nodes (k, 64) with -1 for no node, w (k, 64), grad (k, 64, 3))."""
+        ids = np.ascontiguousarray(np.atleast_1d(ids), np.int64)
+        k = len(ids)
+        nodes = np.empty((k, 64), np.int64)
+        w = np.empty((k, 64))
+        g = np.empty((k, 64, 3))
+        p64 = C.POINTER(C.c_int64)
+        self._check(self._lib.aep_get_weights(self._h, k, ids.ctypes.data_as(p64), nodes.ctypes.data_as(p64), _dp(w),
+                                              _dp(g)))
+        return nodes, w, g
+
+    def checkpoint(self) -> bytes:
+        """Full device state (current particle order, mesh, parameters, level set, fixed
+        vertices); load_checkpoint of it resumes bit for bit."""
+        n = C.c_int64()
+        self._check(self._lib.aep_checkpoint_size(self._h, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self._check(self._lib.aep_checkpoint_save(self._h, buf, n.value))
+        return buf.raw
+
+    def load_checkpoint(self, blob: bytes):
+        buf = C.create_string_buffer(bytes(blob), len(blob))
+        self._check(self._lib.aep_checkpoint_load(self._h, buf, len(blob)))
+        # header: magic[8], version, float_arrays (int32), n, np (int64), ...
+        self._np = int(np.frombuffer(blob, np.int64, count=1, offset=24)[0])
+
+    def save_checkpoint_file(self, path):
+        with open(path, "wb") as f:
+            f.write(self.checkpoint())
+
+    def load_checkpoint_file(self, path):
+        with open(path, "rb") as f:
+            self.load_checkpoint(f.read())
+
+    def solve_state(self) -> dict:
+        st = capi.aep_solve_state()
+        self._check(self._lib.aep_get_solve_state(self._h, C.byref(st)))
+        return dict(t=st.t, inner_t=st.inner_t, dt=st.dt, steps=st.steps, frames=st.frames,
+                    frame_done=bool(st.frame_done))
 
     def step_stage(self, dt: float, stage: int):
         self._check(self._lib.aep_step_stage(self._h, float(dt), int(stage)))
@@ -374,7 +458,9 @@ class HybridSolver:
 
     # --- readback -----------------------------------------------------------------
     def get_particles(self, want_fp: bool = False) -> dict:
-        n = len(self.ps) if self.ps is not None else 0
+        n = getattr(self, "_np", None)
+        if n is None:
+            n = len(self.ps) if self.ps is not None else 0
         x, v = np.empty(3 * n), np.empty(3 * n)
         B, Fe = np.empty(9 * n), np.empty(9 * n)
         Fp = np.empty(9 * n) if want_fp else None

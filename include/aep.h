@@ -191,6 +191,15 @@ aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv,
 aep_status aep_get_mesh(aep_solver* s, double* xv, double* vv, double* Bv, double* xe,
                         double* ve, double* Be, double* d);
 
+/* Replaces LagrangianMesh::bindConstraints(VectorXd* vertexIsFixed)
+ * (LagrangianMesh.cpp:354-363): one value per mesh vertex, nonzero = fixed
+ * (LagrangianMesh::vertexIsFixed, :462-475).  After the collision pass, every
+ * grid node in the stencil of a fixed vertex zeroes the velocity and the
+ * before-friction velocity of its 3x3x3 neighbours (HybridSolver.cpp:513-550).
+ * nv must equal the mesh's vertex count; vertex_is_fixed == NULL removes the
+ * constraints.  aep_set_mesh removes them too.                                 */
+aep_status aep_set_fixed_vertices(aep_solver* s, int64_t nv, const double* vertex_is_fixed);
+
 /* Replaces HybridSolver::setLevelSet(phi, dphi) (HybridSolver.h:89). */
 aep_status aep_set_levelset(aep_solver* s, const aep_sdf* shapes, int32_t n);
 
@@ -208,6 +217,74 @@ aep_status aep_init_volumes(aep_solver* s);
  * affine, advection) -> F update -> return mapping.  Stream-ordered, returns
  * without waiting for the GPU.                                                 */
 aep_status aep_step(aep_solver* s, double dt);
+
+/* One step with the two time steps of the reference loop: the force pass and
+ * the grid update take dt_force (the Dt of the previous iteration, :873, :877),
+ * the grid-to-particle part takes dt (the Dt computed at :878).  aep_step(dt)
+ * is aep_step_split(dt, dt).                                                   */
+aep_status aep_step_split(aep_solver* s, double dt_force, double dt);
+
+/* ---- the adaptive solve loop (HybridSolver::solve, HybridSolver.cpp:827-989) ---- */
+
+typedef struct aep_solve_state {
+    double t;                /* simulated time: advances by 1/60 per completed frame  */
+    double inner_t;          /* time inside the current frame                         */
+    double dt;               /* Dt of the last step                                   */
+    int64_t steps;           /* steps of this solve call                              */
+    int32_t frames;          /* frames completed by this solve call                   */
+    int32_t frame_done;      /* the last step completed a frame (:880-887)            */
+    double reserved[4];
+} aep_solve_state;
+
+/* Called by aep_solve after every step with the device state read back; the
+ * frame files of the reference (:991-1030) are written from here when
+ * state->frame_done (frame number = state->frames - 1).  A nonzero return ends
+ * the solve (aep_solve then returns AEP_OK).                                   */
+typedef int32_t (*aep_solve_fn)(aep_solver* s, const aep_solve_state* state, void* user);
+aep_status aep_set_solve_callback(aep_solver* s, aep_solve_fn fn, void* user);
+
+/* Upper bound on the steps of one aep_solve call (0: none, the default). */
+aep_status aep_set_max_steps(aep_solver* s, int64_t max_steps);
+
+/* Replaces HybridSolver::solve(CFL, maxt, alpha) (HybridSolver.h:90,
+ * HybridSolver.cpp:827-989): the first P2G with volumes (:854, as
+ * aep_init_volumes), Dt = CFL / max(300, max|v_i| / hmin) from the P2G
+ * velocities (:860), then while t <= maxt: a step whose force pass and grid
+ * update use the previous Dt, whose Dt is recomputed from the updated grid
+ * velocities before collision (:878, RegularGrid.cpp:188-200) and clamped to
+ * end the 1/60 s frame (:880-892).  Dt and the frame clock live on the device;
+ * the host reads them once per step.  alpha is accepted and unused, as in the
+ * reference (:739).                                                            */
+aep_status aep_solve(aep_solver* s, double cfl, double maxt, double alpha);
+
+/* The state after the last step of the current or last aep_solve call. */
+aep_status aep_get_solve_state(aep_solver* s, aep_solve_state* out);
+
+/* ---- interpolation weights ------------------------------------------------------- */
+
+/* One row per item of the reference's weight matrices omegas_ and domegas_1..3
+ * (HybridSolver::evaluateInterpolationWeights_, HybridSolver.cpp:18-97) at the
+ * current positions, as the GPU step evaluates them (FP32, widened to double).
+ * ids: `count` item indices (particles 0..Np-1, then mesh vertices Np..Np+Nv-1,
+ * then mesh elements); per id 64 entries in ascending node order: nodes (the
+ * reference index k*Rx*Ry + j*Rx + i, or -1 where the weight is zero or the node
+ * is outside the grid), w, and grad (3 per entry: d/dx, d/dy, d/dz).          */
+aep_status aep_get_weights(aep_solver* s, int64_t count, const int64_t* ids, int64_t* nodes,
+                           double* w, double* grad);
+
+/* ---- checkpoint (full device state, bit-exact resume) --------------------------- */
+
+/* Bytes of a checkpoint of the current state. */
+aep_status aep_checkpoint_size(aep_solver* s, int64_t* bytes);
+/* Copy the particle and mesh state in the device's current order, the
+ * parameters, level set and fixed vertices into buf (`bytes` from
+ * aep_checkpoint_size).  Steps after aep_checkpoint_load of this buffer repeat
+ * the steps after the save bit for bit.  The learned return map, harvest and
+ * stream settings are not part of it.                                           */
+aep_status aep_checkpoint_save(aep_solver* s, void* buf, int64_t bytes);
+/* Restore a checkpoint into a handle created with the same grid description;
+ * replaces particles, mesh, parameters, level set and fixed vertices.          */
+aep_status aep_checkpoint_load(aep_solver* s, const void* buf, int64_t bytes);
 
 /* Wait for all work of the handle; returns the status of the work (overflow). */
 aep_status aep_synchronize(aep_solver* s);

@@ -347,6 +347,7 @@ struct Mesh {
     std::vector<M3> D, Drest;  // columns d1 d2 d3
     double mu = 0, lambda = 0, shear = 0, stiffness = 0, friction = 0;
     std::vector<double> inplane;  // per element: 2x2 (invRest * P), column-major
+    std::vector<uint8_t> fixed;   // LagrangianMesh::vertexIsFixed (LM:354-363, 462-475)
 };
 
 struct Oracle {
@@ -623,8 +624,33 @@ void update_grid_velocities(Oracle& o, double dt) {
             for (int a = 0; a < 3; ++a) o.gv[n][a] += dt * o.gf[n][a] / o.gm[n];
 }
 
-// HybridSolver.cpp:460-511 (fixed-vertex sweep :513-550 not restated: no
-// constraints are bound in the restated scenes)
+// HybridSolver.cpp:513-550: every node of a fixed vertex's stencil zeroes the
+// velocity and before-friction velocity of its 3x3x3 neighbours, addressed by the
+// linear index k*Rx*Ry + j*Rx + i with the range check 0 <= index < Ng (i +- 1
+// wraps into the next row, as in the reference; the distance test <= 12 always holds)
+void fixed_vertices(Oracle& o) {
+    if (!o.has_mesh || o.mesh.fixed.empty()) return;
+    const Weights& W = o.Wv;
+    const int64_t rx = o.g.res[0], ry = o.g.res[1], ng = o.g.ng();
+    for (int64_t v = 0; v < o.mesh.nv; ++v) {
+        if (!o.mesh.fixed[v]) continue;
+        for (int64_t e = W.rowptr[v]; e < W.rowptr[v + 1]; ++e) {
+            const int64_t node = W.node[e];
+            const int64_t ri = node % rx, rj = (node / rx) % ry, rk = node / (rx * ry);
+            for (int64_t i = ri - 1; i <= ri + 1; ++i)
+                for (int64_t j = rj - 1; j <= rj + 1; ++j)
+                    for (int64_t k = rk - 1; k <= rk + 1; ++k) {
+                        const int64_t idx = k * rx * ry + j * rx + i;
+                        if (0 <= idx && idx < ng) {
+                            o.gv[idx] = V3{0, 0, 0};
+                            o.gvbf[idx] = V3{0, 0, 0};
+                        }
+                    }
+        }
+    }
+}
+
+// HybridSolver.cpp:460-511, then the fixed-vertex sweep (:513-550)
 void collision(Oracle& o) {
     int64_t ng = o.g.ng();
     o.gvbf = o.gv;
@@ -652,6 +678,7 @@ void collision(Oracle& o) {
             o.gv[n] = vr;
         }
     }
+    fixed_vertices(o);
 }
 
 // G2P velocity, APIC (:739-825), advection (:940-951) for one particle set
@@ -816,6 +843,56 @@ void step(Oracle& o, double dt_force, double dt, int stage) {
     o.steps++;
 }
 
+// RegularGrid::max_velocity / CFL_condition (RegularGrid.cpp:188-200, RegularGrid.h:60)
+double cfl_condition(const Oracle& o) {
+    double vmax = 0.0;
+    for (const V3& v : o.gv) vmax = std::max(vmax, norm(v));
+    double hmin = std::min(o.g.h[0], std::min(o.g.h[1], o.g.h[2]));
+    return vmax / hmin;
+}
+
+// HybridSolver::solve (:827-989) after the initial weights and P2G (orc_init with
+// volumes): Dt from the P2G velocities; per iteration the force pass and grid
+// update use the previous Dt, the new Dt (with the 1/60 s frame clamp) drives
+// the rest.  Stops when t > maxt or after max_steps iterations (0: no limit).
+// frame_t, if given, receives t after each completed frame (up to max_frames).
+int64_t solve(Oracle& o, double cfl, double maxt, int64_t max_steps, double* t_out, int* frames_out,
+              double* frame_t, int max_frames, double* dt_trace, int64_t trace_cap) {
+    double t = 0.0, inner = 0.0;
+    double Dt = cfl / std::max(3e2, cfl_condition(o));
+    int frames = 0;
+    int64_t it = 0;
+    const double frame_dt = 1.0 / 60.0;
+    while (t <= maxt && (max_steps <= 0 || it < max_steps)) {
+        compute_forces(o, Dt);
+        update_grid_velocities(o, Dt);
+        Dt = cfl / std::max(3e2, cfl_condition(o));
+        if (inner + Dt >= frame_dt) {
+            Dt = frame_dt - inner;
+            t += frame_dt;
+            inner = 0.0;
+            if (frame_t && frames < max_frames) frame_t[frames] = t;
+            ++frames;
+        } else {
+            inner += Dt;
+        }
+        if (dt_trace && it < trace_cap) dt_trace[it] = Dt;
+        collision(o);
+        if (o.np) {
+            g2p_set(o, o.W, o.x, o.v, o.B, o.prm.particle_damp, Dt, true, true);
+            plasticity_particles(o, Dt);
+        }
+        if (o.has_mesh) mesh_g2p_and_plasticity(o, Dt);
+        rebuild_weights(o);
+        p2g(o, false);
+        o.steps++;
+        ++it;
+    }
+    if (t_out) *t_out = t;
+    if (frames_out) *frames_out = frames;
+    return it;
+}
+
 }  // namespace
 
 // =========================== C API (ctypes) ===========================================
@@ -880,6 +957,7 @@ int orc_set_mesh(void* h, int64_t nv, int64_t nf, const double* xv, const int32_
     Mesh& me = o->mesh;
     o->has_mesh = true;
     me.nv = nv; me.nf = nf;
+    me.fixed.clear();
     me.xv.resize(nv); me.vv.resize(nv); me.Bv.assign(nv, M3{}); me.mv.resize(nv); me.volv.resize(nv);
     me.xe.resize(nf); me.ve.resize(nf); me.Be.assign(nf, M3{}); me.me.resize(nf); me.vole.resize(nf);
     me.faces.resize(nf); me.D.resize(nf); me.Drest.resize(nf);
@@ -925,6 +1003,24 @@ int orc_init(void* h, int compute_volumes) {
     Oracle* o = (Oracle*)h;
     rebuild_weights(*o);
     p2g(*o, compute_volumes != 0);
+    return 0;
+}
+
+int64_t orc_solve(void* h, double cfl, double maxt, int64_t max_steps, double* t_out, int* frames_out,
+                  double* frame_t, int max_frames, double* dt_trace, int64_t trace_cap) {
+    return solve(*(Oracle*)h, cfl, maxt, max_steps, t_out, frames_out, frame_t, max_frames, dt_trace, trace_cap);
+}
+
+// vertex_is_fixed: nv doubles, nonzero = fixed (LagrangianMesh::bindConstraints); null clears
+int orc_set_fixed_vertices(void* h, int64_t nv, const double* vertex_is_fixed) {
+    Oracle* o = (Oracle*)h;
+    if (!vertex_is_fixed) {
+        o->mesh.fixed.clear();
+        return 0;
+    }
+    if (!o->has_mesh || nv != o->mesh.nv) return 1;
+    o->mesh.fixed.assign((size_t)nv, 0);
+    for (int64_t v = 0; v < nv; ++v) o->mesh.fixed[v] = vertex_is_fixed[v] != 0.0;
     return 0;
 }
 

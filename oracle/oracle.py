@@ -38,6 +38,11 @@ def load() -> C.CDLL:
         lib.orc_set_levelset.argtypes = [vp, C.POINTER(capi.aep_sdf), C.c_int32]
         lib.orc_init.argtypes = [vp, C.c_int]
         lib.orc_step.argtypes = [vp, C.c_double, C.c_double, C.c_int]
+        lib.orc_solve.restype = C.c_int64
+        lib.orc_solve.argtypes = [vp, C.c_double, C.c_double, C.c_int64, _dp, C.POINTER(C.c_int), _dp, C.c_int, _dp,
+                                  C.c_int64]
+        lib.orc_set_fixed_vertices.restype = C.c_int
+        lib.orc_set_fixed_vertices.argtypes = [vp, C.c_int64, _dp]
         lib.orc_get_particles.argtypes = [vp, C.c_int64] + [_dp] * 7
         lib.orc_get_mesh.argtypes = [vp] + [_dp] * 7
         lib.orc_get_grid.argtypes = [vp] + [_dp] * 4
@@ -124,6 +129,27 @@ class Oracle:
 
     def step(self, dt: float, stage: int = capi.AEP_STAGE_FULL, dt_force: float | None = None):
         self.lib.orc_step(self.h, float(dt if dt_force is None else dt_force), float(dt), int(stage))
+
+    def solve(self, cfl: float, maxt: float, max_steps: int = 0, max_frames: int = 64, trace: int = 0) -> dict:
+        """HybridSolver::solve (HS:827-989) after init(): adaptive Dt with the frame
+        clamp.  Returns steps, final t, frames, the t of each frame and the Dt trace."""
+        t = C.c_double(0.0)
+        frames = C.c_int(0)
+        ft = np.zeros(max(1, max_frames))
+        dts = np.zeros(max(1, trace))
+        it = self.lib.orc_solve(self.h, float(cfl), float(maxt), int(max_steps), C.byref(t), C.byref(frames), _p(ft),
+                                int(max_frames), _p(dts), int(trace))
+        nf = min(frames.value, max_frames)
+        return dict(steps=int(it), t=t.value, frames=frames.value, frame_t=ft[:nf], dt=dts[:min(it, trace)])
+
+    def set_fixed_vertices(self, vertex_is_fixed):
+        """LagrangianMesh::bindConstraints: one value per vertex, nonzero = fixed; None clears."""
+        if vertex_is_fixed is None:
+            self.lib.orc_set_fixed_vertices(self.h, 0, None)
+            return
+        a = np.ascontiguousarray(vertex_is_fixed, float)
+        if self.lib.orc_set_fixed_vertices(self.h, len(a), _p(a)) != 0:
+            raise ValueError("vertex_is_fixed must have one entry per mesh vertex")
 
     def get_particles(self) -> dict:
         n = self.n

@@ -138,3 +138,61 @@ def test_cloth_mass_conserved_exactly():
         assert s["total_mass"] == m0
     total = mesh.vertex_masses.sum() + mesh.element_masses.sum()
     assert abs(m0 - total) / total < 1e-6
+
+
+def _edge_fixed(mesh, nside=20):
+    """vertexIsFixed for the x-min edge of the sheet, its first nside vertices
+    (LagrangianMesh::bindConstraints)."""
+    f = np.zeros(len(mesh.vertex_positions))
+    f[:nside] = 1.0
+    return f
+
+
+@pytest.mark.parametrize("with_sand", [False, True])
+def test_fixed_vertices_grid_matches_oracle(with_sand):
+    grid, ps, mesh, ls, prm = small_cloth(with_sand)
+    fixed = _edge_fixed(mesh)
+    assert 10 <= fixed.sum() <= 40
+    gpu, orc = pair(grid, ps, mesh, ls, prm)
+    gpu.bind_constraints(fixed)
+    orc.set_fixed_vertices(fixed)
+    dt = 2e-5
+    gpu.step_stage(dt, capi.AEP_STAGE_GRID)
+    g = gpu.get_grid()
+    orc.init(volumes=False)
+    orc.step(dt, stage=capi.AEP_STAGE_GRID)
+    o = orc.get_grid()
+    # nodes the constraint zeroed: v and v_bf both zero (a sticking collision
+    # zeroes v alone and keeps the tangential v_bf)
+    zeroed = ((np.abs(o["velocities"]).max(axis=1) == 0) & (np.abs(o["velocities_before_friction"]).max(axis=1) == 0)
+              & (o["masses"] > 0))
+    assert zeroed.sum() > 100  # a band of nodes with mass
+    assert np.all(g["velocities"][zeroed] == 0) and np.all(g["velocities_before_friction"][zeroed] == 0)
+    assert mass_weighted_rel(g["velocities"], o["velocities"], o["masses"]) < 1e-4
+
+
+def test_fixed_vertices_ten_steps_match_oracle_and_stay():
+    grid, ps, mesh, ls, prm = small_cloth(True, seed=9)
+    fixed = _edge_fixed(mesh)
+    gpu, orc = pair(grid, ps, mesh, ls, prm)
+    gpu.bind_constraints(fixed)
+    orc.set_fixed_vertices(fixed)
+    gpu.init_volumes()
+    orc.init(volumes=True)
+    for _ in range(10):
+        gpu.step(2e-5)
+        orc.step(2e-5)
+    gm, om = gpu.get_mesh(), orc.get_mesh()
+    _compare_mesh(gm, om, 2e-6, 1e-3, 2e-5, 5e-3)
+    f = fixed > 0
+    assert np.abs(gm["vertex_positions"][f] - mesh.vertex_positions[f]).max() < 1e-6
+    assert np.abs(gm["vertex_velocities"][f]).max() == 0.0
+
+
+def test_fixed_vertices_argument_checks():
+    grid, ps, mesh, ls, prm = small_cloth(False)
+    gpu = HybridSolver(None, grid, prm)
+    gpu.set_lagrangian_mesh(mesh)
+    with pytest.raises(capi.AepError):
+        gpu.bind_constraints(np.ones(3))
+    gpu.bind_constraints(None)

@@ -12,7 +12,10 @@ golden vectors, so the pins come from the mathematics of the reference step):
    points unchanged, projected points on the yield cone, tension to the apex,
    idempotence;
 6. P2G conserves mass and momentum; an affine velocity field survives the APIC
-   P2G -> G2P round trip exactly (zero stiffness, no gravity).
+   P2G -> G2P round trip exactly (zero stiffness, no gravity);
+7. fixed cloth vertices (HS:513-550): a fixed vertex keeps its position and has
+   zero velocity after steps (its whole stencil is zeroed, and the weights
+   reproduce linear fields).
 """
 import numpy as np
 import pytest
@@ -172,3 +175,30 @@ def test_apic_round_trip_of_an_affine_field_is_exact():
     assert np.abs(r["velocities"] - ps.velocities).max() < 1e-12
     assert np.abs(r["affine_momenta"] - ps.affine_momenta).max() < 1e-14
     assert np.abs(r["positions"] - (ps.positions + 1e-5 * ps.velocities)).max() < 1e-15 + 1e-12
+
+
+def test_fixed_vertices_stay_put():
+    from anisotropicelastoplasticity_gb300 import LagrangianMesh, scenes
+
+    rng = np.random.default_rng(1)
+    V, F = scenes.sheet(12, 0.4, (0.5, 0.5), 0.6, 1e-4, rng)
+    mesh = LagrangianMesh.from_triangles(V, F, density=6.4, thickness=1 / 32, youngs_modulus=5.0, poisson_ratio=0.3,
+                                         shear_stiffness=1e3, stiffness=1e3, friction_coeff=0.3)
+    mesh.vertex_velocities = 0.2 * rng.standard_normal((len(V), 3))
+    grid = RegularGrid([0, 0, 0], [1, 1, 1], [32, 32, 32])
+    o = Oracle(grid, make_params())
+    o.set_lagrangian_mesh(mesh)
+    o.set_level_set(LevelSet.ground(0.05))
+    fixed = np.zeros(len(V))
+    fixed[[0, 11, 60]] = 1.0
+    o.set_fixed_vertices(fixed)
+    o.init(volumes=False)
+    for _ in range(5):
+        o.step(2e-5)
+    m = o.get_mesh()
+    f = fixed > 0
+    assert np.abs(m["vertex_positions"][f] - V[f]).max() < 1e-14
+    assert np.abs(m["vertex_velocities"][f]).max() == 0.0
+    assert np.abs(m["vertex_positions"][~f] - V[~f]).max() > 1e-6  # the others move
+    with pytest.raises(ValueError):
+        o.set_fixed_vertices(np.ones(5))
