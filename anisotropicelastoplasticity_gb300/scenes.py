@@ -139,4 +139,57 @@ def cloth_drape(nside: int = 256, res: int = 128, seed: int = 2, shear_stiffness
                  f"element volume", mesh)
 
 
+# --- the reference's particle factories (ParticleSystem.cpp:119-401), seeded ---------
+# Rejection sampling of the unit ball / disk, the total mass spread evenly, volumes 1
+# (the first P2G of solve recomputes them), F_E = F_P = I.  The C++ facade
+# (include/aep/hybrid_solver.hpp) has the same factories on std::mt19937_64.
+
+def _unit_ball(rng, n, dim):
+    out = np.empty((0, dim))
+    while len(out) < n:
+        c = rng.uniform(-1.0, 1.0, (2 * (n - len(out)) + 16, dim))
+        out = np.concatenate([out, c[np.linalg.norm(c, axis=1) <= 1.0]])
+    return out[:n]
+
+
+def snow_ball(center, radius: float, n: int, seed: int = 0) -> ParticleSystem:
+    """SnowBall (ParticleSystem.cpp:119-183): total mass 100 * 3.14 r^3, snow."""
+    x = np.asarray(center, float) + radius * _unit_ball(np.random.default_rng(seed), n, 3)
+    return _particles(x, np.zeros((n, 3)), np.full(n, 100.0 * 3.14 * radius ** 3 / n), np.ones(n), capi.AEP_SNOW)
+
+
+def sand_ball(center, radius: float, n: int, seed: int = 0) -> ParticleSystem:
+    """SandBall (ParticleSystem.cpp:185-247): total mass 1300 * 3.14 r^3, sand."""
+    x = np.asarray(center, float) + radius * _unit_ball(np.random.default_rng(seed), n, 3)
+    return _particles(x, np.zeros((n, 3)), np.full(n, 1300.0 * 3.14 * radius ** 3 / n), np.ones(n), capi.AEP_SAND)
+
+
+def sand_block(bmin, bmax, hole_radius: float, n: int, seed: int = 0) -> ParticleSystem:
+    """SandBlock (ParticleSystem.cpp:249-329): uniform in the box minus the ball of
+    hole_radius at (bmin.x, bmin.y, mid z); total mass 1300 (box volume - pi R^3 / 4)."""
+    lo, hi = np.asarray(bmin, float), np.asarray(bmax, float)
+    if hole_radius * 2.0 >= hi[2] - lo[2]:
+        raise ValueError("SandBlock: the hole is too big")
+    hc = np.array([lo[0], lo[1], 0.5 * (lo[2] + hi[2])])
+    rng = np.random.default_rng(seed)
+    x = np.empty((0, 3))
+    while len(x) < n:
+        c = _block(rng, 2 * (n - len(x)) + 16, lo, hi)
+        x = np.concatenate([x, c[np.linalg.norm(c - hc, axis=1) >= hole_radius]])
+    total = 1300.0 * (np.prod(hi - lo) - 0.25 * np.pi * hole_radius ** 3)
+    return _particles(x[:n], np.zeros((n, 3)), np.full(n, total / n), np.ones(n), capi.AEP_SAND)
+
+
+def sand_cylinder(base_center, radius: float, height: float, n: int, seed: int = 0) -> ParticleSystem:
+    """SandCylinder (ParticleSystem.cpp:331-401): disk x [0, height) above base_center,
+    velocity (0, 0, -1), total mass 1300 pi r^2 h, sand."""
+    rng = np.random.default_rng(seed)
+    d = radius * _unit_ball(rng, n, 2)
+    z = rng.uniform(0.0, height, n)
+    x = np.asarray(base_center, float) + np.stack([d[:, 0], d[:, 1], z], axis=1)
+    v = np.zeros((n, 3))
+    v[:, 2] = -1.0
+    return _particles(x, v, np.full(n, 1300.0 * np.pi * radius ** 2 * height / n), np.ones(n), capi.AEP_SAND)
+
+
 CONFIGS = {0: snow_block, 1: sand_column, 2: cloth_drape, 3: snow_sand_collision}

@@ -202,3 +202,22 @@ def test_fixed_vertices_stay_put():
     assert np.abs(m["vertex_positions"][~f] - V[~f]).max() > 1e-6  # the others move
     with pytest.raises(ValueError):
         o.set_fixed_vertices(np.ones(5))
+
+
+def test_scene_factories_follow_the_reference_rules():
+    from anisotropicelastoplasticity_gb300 import scenes
+
+    b = scenes.snow_ball([0.5, 0.5, 0.5], 0.1, 4000, seed=1)
+    assert len(b) == 4000 and np.all(b.material == capi.AEP_SNOW)
+    assert np.linalg.norm(b.positions - 0.5, axis=1).max() <= 0.1
+    assert abs(b.masses.sum() - 100 * 3.14 * 1e-3) < 1e-12
+    s = scenes.sand_block([0, 0, 0], [0.4, 0.4, 0.4], 0.15, 5000, seed=2)
+    assert np.linalg.norm(s.positions - [0, 0, 0.2], axis=1).min() >= 0.15
+    with pytest.raises(ValueError):
+        scenes.sand_block([0, 0, 0], [1, 1, 0.2], 0.1, 10)
+    c = scenes.sand_cylinder([0.5, 0.5, 0.1], 0.1, 0.3, 3000, seed=3)
+    assert np.all(c.velocities[:, 2] == -1.0) and c.positions[:, 2].min() >= 0.1
+    assert np.linalg.norm(c.positions[:, :2] - 0.5, axis=1).max() <= 0.1
+    assert abs(c.masses.sum() - 1300 * np.pi * 0.01 * 0.3) < 1e-9
+    sb = scenes.sand_ball([0, 0, 0], 0.2, 100, seed=4)
+    assert abs(sb.masses.sum() - 1300 * 3.14 * 0.008) < 1e-12
