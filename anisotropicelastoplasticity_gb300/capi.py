@@ -73,7 +73,7 @@ class aep_params(C.Structure):
         ("momentum_bits", C.c_int32),
         ("mesh_damp", C.c_double),
         ("cloth_volume_weighting", C.c_int32),
-        ("reserved_i", C.c_int32),
+        ("full_sort", C.c_int32),
         ("reserved", C.c_int64 * 6),
     ]
 
@@ -91,7 +91,8 @@ class aep_stats(C.Structure):
         ("total_momentum", C.c_double * 3),
         ("learned_accepted", C.c_int64),
         ("learned_fallbacks", C.c_int64),
-        ("reserved", C.c_double * 5),
+        ("sort_movers", C.c_int64),
+        ("reserved", C.c_double * 4),
     ]
 
 

@@ -56,9 +56,23 @@ struct aep_solver {
     uint32_t* keys_sorted = nullptr;
     int32_t* iota = nullptr;
     int32_t* perm = nullptr;
+    int32_t* inv = nullptr;  // id -> slot of the current order (readback)
     void* sort_tmp = nullptr;
     size_t sort_bytes = 0;
     int key_bits = 0;
+    // incremental ordering: partition of the slots, sorted movers, mover count
+    int32_t* part = nullptr;
+    uint32_t* mk_tmp = nullptr;
+    int32_t* mj_tmp = nullptr;
+    uint32_t* mkeys = nullptr;
+    int32_t* mslot = nullptr;
+    int32_t* nmov = nullptr;       // device
+    int32_t* nmov_host = nullptr;  // pinned
+    unsigned long long* nmov_host_check = nullptr;  // pinned, 2 words: upload validation result
+    void* part_tmp = nullptr;
+    size_t part_bytes = 0;
+    bool prev_sorted = false;  // keys_sorted holds an ascending array of the current n
+    int64_t last_movers = -1;  // movers of the last incremental ordering (-1: full sort)
     GArrays G{};
     size_t nnodes = 0;
     int nblocks = 0;
@@ -231,10 +245,19 @@ void free_particles(aep_solver* s) {
     cudaFree(s->perm);
     cudaFree(s->sort_tmp);
     cudaFree(s->staging);
+    cudaFree(s->part);
+    cudaFree(s->part_tmp);
+    cudaFree(s->inv);
+    s->inv = nullptr;
     s->keys = s->keys_sorted = nullptr;
     s->iota = s->perm = nullptr;
     s->sort_tmp = nullptr;
     s->staging = nullptr;
+    s->part = nullptr;  // the mover arrays live in the same allocation
+    s->mk_tmp = s->mkeys = nullptr;
+    s->mj_tmp = s->mslot = nullptr;
+    s->part_tmp = nullptr;
+    s->prev_sorted = false;
     s->cap = 0;
 }
 
@@ -267,8 +290,24 @@ aep_status ensure_capacity(aep_solver* s, int64_t n, int64_t keep = 0) {
     CK(cudaMalloc(&s->keys_sorted, sizeof(uint32_t) * (size_t)n));
     CK(cudaMalloc(&s->iota, sizeof(int32_t) * (size_t)n));
     CK(cudaMalloc(&s->perm, sizeof(int32_t) * (size_t)n));
+    CK(cudaMalloc(&s->inv, sizeof(int32_t) * (size_t)n));
     s->sort_bytes = sort_temp_bytes((int)n, s->key_bits);
     CK(cudaMalloc(&s->sort_tmp, s->sort_bytes));
+    // partition (n) + four mover arrays (n / 4 + 1 each: larger counts take the full sort)
+    const size_t mcap = (size_t)n / 4 + 1;
+    CK(cudaMalloc(&s->part, sizeof(int32_t) * ((size_t)n + 4 * mcap)));
+    s->mk_tmp = reinterpret_cast<uint32_t*>(s->part + n);
+    s->mj_tmp = s->part + n + mcap;
+    s->mkeys = reinterpret_cast<uint32_t*>(s->part + n + 2 * mcap);
+    s->mslot = s->part + n + 3 * mcap;
+    s->part_bytes = partition_temp_bytes((int)n);
+    CK(cudaMalloc(&s->part_tmp, s->part_bytes));
+    if (!s->nmov) {
+        CK(cudaMalloc(&s->nmov, sizeof(int32_t)));
+        CK(cudaMallocHost(&s->nmov_host, sizeof(int32_t)));
+        CK(cudaMallocHost(&s->nmov_host_check, 2 * sizeof(unsigned long long)));
+    }
+    s->prev_sorted = false;
     s->staging_bytes = sizeof(double) * 36 * (size_t)n;  // every field of one particle set at once
     CK(cudaMalloc(&s->staging, s->staging_bytes));
     if (!s->check) CK(cudaMalloc(&s->check, 2 * sizeof(unsigned long long)));
@@ -280,33 +319,71 @@ aep_status ensure_capacity(aep_solver* s, int64_t n, int64_t keep = 0) {
     return AEP_OK;
 }
 
+// A device-usable alias of a caller pointer: page-locked host memory (read and
+// written by the conversion kernels directly over the host link), device and
+// managed memory; nullptr for pageable host memory, which goes through the
+// staging buffer.
+const void* device_alias(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice) return p;
+    return nullptr;
+}
+
+// A device pointer with the caller's `bytes` at `p`: the alias, or a copy in the
+// staging buffer at `off` doubles
+const void* device_source(aep_solver* s, const void* p, size_t bytes, size_t off, cudaError_t* err) {
+    const void* a = device_alias(p);
+    if (a) return a;
+    double* st = s->staging + off;
+    *err = cudaMemcpyAsync(st, p, bytes, cudaMemcpyHostToDevice, s->stream);
+    return st;
+}
+
 // upload `count` doubles per item for items [id0, id0 + n) of set 0
-// src: host array of `count` doubles per item; `off` doubles into the staging buffer
-// (distinct offsets let consecutive uploads run without waiting on each other)
+// src: caller array of `count` doubles per item; `off` doubles into the staging
+// buffer when src is pageable (distinct offsets let consecutive uploads proceed
+// without waiting on each other)
 aep_status upload(aep_solver* s, const double* src, int count, int mode, float* const* dst, int64_t n = -1,
                   int64_t id0 = 0, const int32_t* map = nullptr, size_t off = 0) {
     if (n < 0) n = s->n;
-    double* st = s->staging + off;
-    if (src != st)
-        CK(cudaMemcpyAsync(st, src, sizeof(double) * count * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    cudaError_t e = cudaSuccess;
+    const double* d_src =
+        static_cast<const double*>(device_source(s, src, sizeof(double) * count * (size_t)n, off, &e));
+    CK(e);
     float* d[9] = {};
     int nd = mode == 3 ? 1 : (mode == 0 ? 3 : 9);
     for (int k = 0; k < nd; ++k) d[k] = dst[k] + id0;
-    launch_upload((int)n, mode, st, d, s->stream, map);
+    launch_upload((int)n, mode, d_src, d, s->stream, map);
     CKLAUNCH();
     return AEP_OK;
 }
 
-// download ids [id_lo, id_hi) in id order through staging offset `off` (doubles);
-// the caller synchronises once after all fields
+// inverse of the current order's id map (inv[id] = slot), used by download()
+aep_status prepare_download(aep_solver* s) {
+    launch_inverse_ids((int)s->n, s->P[s->cur].id, s->inv, s->stream);
+    CKLAUNCH();
+    return AEP_OK;
+}
+
+// download ids [id_lo, id_hi) in id order (after prepare_download): straight into
+// dst when it is page-locked or device memory, else through staging offset `off`
+// (doubles) and a copy; the caller synchronises once after all fields
 aep_status download(aep_solver* s, double* dst, int count, int mode, float* const* src, int64_t id_lo = 0,
                     int64_t id_hi = -1, size_t off = 0, bool sync = true) {
     if (id_hi < 0) id_hi = s->n;
-    const PArrays& P = s->P[s->cur];
-    double* st = s->staging + off;
-    launch_download((int)s->n, mode, P.id, st, src, s->stream, (int)id_lo, (int)id_hi);
+    const int cnt = (int)(id_hi - id_lo);
+    double* alias = static_cast<double*>(const_cast<void*>(device_alias(dst)));
+    double* out = alias ? alias : s->staging + off;
+    launch_download(cnt, mode, s->inv, (int)id_lo, out, src, s->stream);
     CKLAUNCH();
-    CK(cudaMemcpyAsync(dst, st, sizeof(double) * count * (size_t)(id_hi - id_lo), cudaMemcpyDeviceToHost, s->stream));
+    if (!alias)
+        CK(cudaMemcpyAsync(dst, out, sizeof(double) * count * (size_t)cnt, cudaMemcpyDeviceToHost, s->stream));
     if (sync) CK(cudaStreamSynchronize(s->stream));
     return AEP_OK;
 }
@@ -335,6 +412,35 @@ inline void mark(aep_solver* s, int boundary) {
     if (s->profiling) cudaEventRecord(s->ev[s->ev_slot][boundary], s->stream);
 }
 
+// Order the current particles by key into keys_sorted / perm: incrementally from
+// the last sorted keys when few particles changed cell, else a full radix sort.
+// The incremental path reads the mover count back (one stream synchronisation).
+cudaError_t order_particles(aep_solver* s) {
+    const int n = (int)s->n;
+    s->last_movers = -1;
+    if (!s->prm.full_sort && s->prev_sorted && n >= 4096) {
+        cudaError_t e = partition_movers(s->part_tmp, s->part_bytes, s->keys, s->keys_sorted, s->iota, s->part,
+                                         s->nmov, n, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->nmov_host, s->nmov, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                                  s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return e;
+        const int m = *s->nmov_host;
+        if (m >= 0 && m <= n / 4) {
+            e = sort_movers(s->sort_tmp, s->sort_bytes, s->keys, s->part, m, s->mk_tmp, s->mj_tmp, s->mkeys,
+                            s->mslot, s->key_bits, s->stream);
+            if (e == cudaSuccess)
+                e = merge_movers(s->keys, s->part, n, m, s->mkeys, s->mslot, s->keys_sorted, s->perm, s->stream);
+            s->last_movers = m;
+            return e;
+        }
+    }
+    cudaError_t e = sort_pairs(s->sort_tmp, s->sort_bytes, s->keys, s->keys_sorted, s->iota, s->perm, n,
+                               s->key_bits, s->stream);
+    if (e == cudaSuccess) s->prev_sorted = true;
+    return e;
+}
+
 // P2G of the current particle order (sort + scatter + normalisation)
 aep_status run_p2g(aep_solver* s) {
     if (s->dirty_grid) {
@@ -350,8 +456,7 @@ aep_status run_p2g(aep_solver* s) {
         CKLAUNCH();
         s->keys_valid = true;
     }
-    CK(sort_pairs(s->sort_tmp, s->sort_bytes, s->keys, s->keys_sorted, s->iota, s->perm, (int)s->n, s->key_bits,
-                  s->stream));
+    CK(order_particles(s));
     CK(cudaMemsetAsync(s->G.nactive, 0, sizeof(int32_t), s->stream));
     mark(s, AEP_PHASE_P2G);
     launch_p2g(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, s->slot_of, s->curidx_of, s->stream);
@@ -458,6 +563,9 @@ aep_status aep_solver_destroy(aep_solver* s) {
     cudaFree(s->dforce);
     cudaFree(s->harvest_count);
     cudaFree(s->check);
+    cudaFree(s->nmov);
+    cudaFreeHost(s->nmov_host);
+    cudaFreeHost(s->nmov_host_check);
     cudaFree(s->solve);
     cudaFreeHost(s->solve_host);
     cudaFreeHost(s->stats_host);
@@ -475,51 +583,45 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     if (!s) return AEP_INVALID_ARG;
     if (n <= 0 || n > (int64_t)INT32_MAX / 2 || !x || !Fe || !m)
         return fail(s, AEP_INVALID_ARG, "aep_set_particles: need n > 0 and non-null x, Fe, m");
-    CK(cudaStreamSynchronize(s->stream));
-    if (s->cap < n) {  // room for the staging copies used by the validation below
-        free_mesh(s);
+    // Re-uploading the same particle set keeps the device's current (sorted) order:
+    // item q goes to the slot its id occupies now, so the next ordering sees nearly
+    // sorted keys and the permuted particle reads stay coalesced.
+    const bool keep_order = s->have_particles && s->n == n && s->np == n && s->nf == 0;
+    if (!keep_order) {
+        CK(cudaStreamSynchronize(s->stream));
+        free_mesh(s);  // a mesh must be (re)attached after the particles
         s->have_particles = false;
         s->n = s->np = 0;
         aep_status st0 = ensure_capacity(s, n);
         if (st0 != AEP_OK) return st0;
+        s->prev_sorted = false;
+        s->cur = 0;
     }
-    // validation on the device: largest mass, bad masses, unknown material tags
-    double* dm = s->staging + 27 * (size_t)n;  // masses stay here for the upload below
-    uint8_t* dmat = reinterpret_cast<uint8_t*>(s->staging + 35 * (size_t)n);
-    CK(cudaMemcpyAsync(dm, m, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-    if (material) CK(cudaMemcpyAsync(dmat, material, (size_t)n, cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemsetAsync(s->check, 0, 2 * sizeof(unsigned long long), s->stream));
-    launch_check_upload((int)n, dm, material ? dmat : nullptr, s->check, s->stream);
-    CKLAUNCH();
-    unsigned long long chk[2] = {0, 0};
-    CK(cudaMemcpyAsync(chk, s->check, sizeof(chk), cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    if (chk[1]) return fail(s, AEP_INVALID_ARG, "aep_set_particles: bad mass or unknown material tag");
-    double mm = 0.0;
-    std::memcpy(&mm, &chk[0], sizeof(mm));
-    if (!(mm > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_particles: all masses are zero");
-    // Re-uploading the same particle set keeps the device's current (sorted) order:
-    // item q goes to the slot its id occupies now, so the next sort sees nearly
-    // sorted keys and the permuted particle reads stay coalesced.
-    const bool keep_order = s->have_particles && s->n == n && s->np == n && s->nf == 0;
     const int32_t* map = nullptr;
     if (keep_order) {
         launch_inverse_ids((int)n, s->P[s->cur].id, s->perm, s->stream);
         CKLAUNCH();
         map = s->perm;
     }
-    free_mesh(s);  // a mesh must be (re)attached after the particles
-    aep_status st = ensure_capacity(s, n);
-    if (st != AEP_OK) return st;
     s->n = s->np = n;
-    s->m_max = mm;
-    fill_kparams(s);
-    if (!keep_order) s->cur = 0;
     PArrays& P = s->P[s->cur];
-    // staging layout (doubles): x 0, v 3n, B 6n, Fe 15n, Fp 24n... (Fp reuses B's area
-    // after B is converted), m 27n, vol 28n, plastic 29n, material bytes at 35n
+    // Arrays in page-locked host or device memory are read by the conversion
+    // kernels directly; pageable ones are staged (doubles): x 0, v 3n, B 6n (F_P
+    // reuses it after B's conversion), Fe 15n, m 27n, vol 28n, plastic 29n,
+    // material bytes at 35n.
     const size_t N = (size_t)n;
-    st = upload(s, x, 3, 0, P.x, -1, 0, map, 0);
+    cudaError_t e = cudaSuccess;
+    const double* dm = static_cast<const double*>(device_source(s, m, sizeof(double) * N, 27 * N, &e));
+    CK(e);
+    const uint8_t* dmat =
+        material ? static_cast<const uint8_t*>(device_source(s, material, N, 35 * N, &e)) : nullptr;
+    CK(e);
+    // validation on the device (largest mass, bad masses, unknown tags), read back
+    // with the final synchronisation
+    CK(cudaMemsetAsync(s->check, 0, 2 * sizeof(unsigned long long), s->stream));
+    launch_check_upload((int)n, dm, dmat, s->check, s->stream);
+    CKLAUNCH();
+    aep_status st = upload(s, x, 3, 0, P.x, -1, 0, map, 0);
     if (st) return st;
     if (v) { st = upload(s, v, 3, 0, P.v, -1, 0, map, 3 * N); if (st) return st; }
     else for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(P.v[a], 0, sizeof(float) * n, s->stream));
@@ -527,21 +629,20 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     else for (int a = 0; a < 9; ++a) CK(cudaMemsetAsync(P.B[a], 0, sizeof(float) * n, s->stream));
     st = upload(s, Fe, 9, 2, P.F, -1, 0, map, 15 * N);
     if (st) return st;
-    st = upload(s, dm, 1, 3, &P.m, -1, 0, map, 27 * N);  // already on the device
+    st = upload(s, dm, 1, 3, &P.m, -1, 0, map, 27 * N);
     if (st) return st;
     if (vol) { st = upload(s, vol, 1, 3, &P.vol, -1, 0, map, 28 * N); if (st) return st; }
     else CK(cudaMemsetAsync(P.vol, 0, sizeof(float) * n, s->stream));
     if (plastic) { st = upload(s, plastic, 1, 3, &P.plastic, -1, 0, map, 29 * N); if (st) return st; }
     else CK(cudaMemsetAsync(P.plastic, 0, sizeof(float) * n, s->stream));
     // material tags and ids
-    launch_init_particles((int)n, P, material ? dmat : nullptr, Fp != nullptr, s->prm.track_plastic_F, s->stream, 0,
-                          -1, map);
+    launch_init_particles((int)n, P, dmat, Fp != nullptr, s->prm.track_plastic_F, s->stream, 0, -1, map);
     CKLAUNCH();
     // F_P: full copy with track_plastic_F; snow particles get J_P = det F_P
-    double* dFp = nullptr;
+    const double* dFp = nullptr;
     if (Fp) {
-        dFp = s->staging + 6 * N;  // after B's conversion (stream order)
-        CK(cudaMemcpyAsync(dFp, Fp, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, s->stream));
+        dFp = static_cast<const double*>(device_source(s, Fp, sizeof(double) * 9 * N, 6 * N, &e));
+        CK(e);
         if (s->prm.track_plastic_F) {
             st = upload(s, dFp, 9, 2, P.Fp, -1, 0, map, 6 * N);
             if (st) return st;
@@ -551,7 +652,19 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
         launch_snow_jp((int)n, P, dFp, s->stream, map);
         CKLAUNCH();
     }
+    unsigned long long* chk = reinterpret_cast<unsigned long long*>(s->nmov_host_check);
+    CK(cudaMemcpyAsync(chk, s->check, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    double mm = 0.0;
+    std::memcpy(&mm, &chk[0], sizeof(mm));
+    if (chk[1] || !(mm > 0.0)) {
+        s->have_particles = false;  // the device arrays are partly overwritten
+        s->n = s->np = 0;
+        return fail(s, AEP_INVALID_ARG, chk[1] ? "aep_set_particles: bad mass or unknown material tag"
+                                               : "aep_set_particles: all masses are zero");
+    }
+    s->m_max = mm;
+    fill_kparams(s);
     s->have_particles = true;
     s->keys_valid = false;
     s->stepped_since_upload = false;
@@ -622,6 +735,7 @@ aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv,
     s->nv = nv;
     s->nf = nf;
     s->n = total;
+    s->prev_sorted = false;
     s->cur = 0;
     s->m_max = mm;
     s->cloth[0] = mu;
@@ -697,17 +811,19 @@ aep_status aep_get_mesh(aep_solver* s, double* xv, double* vv, double* Bv, doubl
                         double* d) {
     if (!s) return AEP_INVALID_ARG;
     if (s->nf == 0) return fail(s, AEP_NOT_READY, "aep_get_mesh: no mesh");
-    CK(cudaStreamSynchronize(s->stream));
     PArrays& P = s->P[s->cur];
     const int64_t vb = s->np, eb = s->np + s->nv, ee = s->n;
-    aep_status st;
-    if (xv && (st = download(s, xv, 3, 0, P.x, vb, eb))) return st;
-    if (vv && (st = download(s, vv, 3, 0, P.v, vb, eb))) return st;
-    if (Bv && (st = download(s, Bv, 9, 1, P.B, vb, eb))) return st;
-    if (xe && (st = download(s, xe, 3, 0, P.x, eb, ee))) return st;
-    if (ve && (st = download(s, ve, 3, 0, P.v, eb, ee))) return st;
-    if (Be && (st = download(s, Be, 9, 1, P.B, eb, ee))) return st;
-    if (d && (st = download(s, d, 9, 4, P.F, eb, ee))) return st;
+    const size_t V = (size_t)s->nv, F = (size_t)s->nf;
+    aep_status st = prepare_download(s);
+    if (st) return st;
+    if (xv && (st = download(s, xv, 3, 0, P.x, vb, eb, 0, false))) return st;
+    if (vv && (st = download(s, vv, 3, 0, P.v, vb, eb, 3 * V, false))) return st;
+    if (Bv && (st = download(s, Bv, 9, 1, P.B, vb, eb, 6 * V, false))) return st;
+    if (xe && (st = download(s, xe, 3, 0, P.x, eb, ee, 15 * V, false))) return st;
+    if (ve && (st = download(s, ve, 3, 0, P.v, eb, ee, 15 * V + 3 * F, false))) return st;
+    if (Be && (st = download(s, Be, 9, 1, P.B, eb, ee, 15 * V + 6 * F, false))) return st;
+    if (d && (st = download(s, d, 9, 4, P.F, eb, ee, 15 * V + 15 * F, false))) return st;
+    CK(cudaStreamSynchronize(s->stream));
     return AEP_OK;
 }
 
@@ -971,15 +1087,16 @@ struct CkptHeader {
     double m_max;
     double cloth[5];
     int32_t nshapes, nfixed;
+    int32_t prev_sorted, reserved;
     DevShape shapes[kMaxShapes];
 };
 constexpr char kCkptMagic[8] = {'A', 'E', 'P', 'C', 'K', 'P', 'T', '1'};
-constexpr int32_t kCkptVersion = 1;
+constexpr int32_t kCkptVersion = 2;
 
 int float_arrays(const aep_params& p) { return kFloatArrays + (p.track_plastic_F ? kFpArrays : 0); }
 
 size_t ckpt_bytes(int64_t n, int64_t nf, int nfixed, int nfa) {
-    return sizeof(CkptHeader) + (size_t)n * (sizeof(float) * nfa + 1 + sizeof(int32_t)) +
+    return sizeof(CkptHeader) + (size_t)n * (sizeof(float) * nfa + 1 + 2 * sizeof(int32_t)) +
            (size_t)nf * (3 * sizeof(int32_t) + 6 * sizeof(float)) + (size_t)nfixed * sizeof(int32_t);
 }
 
@@ -1015,6 +1132,7 @@ aep_status aep_checkpoint_save(aep_solver* s, void* buf, int64_t bytes) {
     for (int k = 0; k < 5; ++k) h.cloth[k] = s->cloth[k];
     h.nshapes = s->kp.nshapes;
     h.nfixed = s->nfixed;
+    h.prev_sorted = s->prev_sorted ? 1 : 0;
     for (int k = 0; k < kMaxShapes; ++k) h.shapes[k] = s->kp.shapes[k];
     char* p = static_cast<char*>(buf);
     std::memcpy(p, &h, sizeof(h));
@@ -1027,6 +1145,10 @@ aep_status aep_checkpoint_save(aep_solver* s, void* buf, int64_t bytes) {
     p += n;
     CK(cudaMemcpy(p, set.id, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
     p += sizeof(int32_t) * n;
+    // the last sorted keys: the next ordering starts from them (incremental path)
+    if (s->prev_sorted) CK(cudaMemcpy(p, s->keys_sorted, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    else std::memset(p, 0, sizeof(uint32_t) * n);
+    p += sizeof(uint32_t) * n;
     if (s->nf > 0) {
         CK(cudaMemcpy(p, s->faces, sizeof(int32_t) * 3 * s->nf, cudaMemcpyDeviceToHost));
         p += sizeof(int32_t) * 3 * s->nf;
@@ -1078,6 +1200,8 @@ aep_status aep_checkpoint_load(aep_solver* s, const void* buf, int64_t bytes) {
     p += n;
     CK(cudaMemcpy(set.id, p, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
     p += sizeof(int32_t) * n;
+    CK(cudaMemcpy(s->keys_sorted, p, sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    p += sizeof(uint32_t) * n;
     if (h.nf > 0) {
         s->nv = h.nv;
         s->nf = h.nf;
@@ -1100,6 +1224,7 @@ aep_status aep_checkpoint_load(aep_solver* s, const void* buf, int64_t bytes) {
         s->nfixed = h.nfixed;
     }
     s->steps = h.steps;
+    s->prev_sorted = h.prev_sorted != 0;
     s->have_particles = true;
     s->keys_valid = false;
     s->stepped_since_upload = h.steps > 0;
@@ -1119,11 +1244,11 @@ aep_status aep_get_particles(aep_solver* s, int64_t n, double* x, double* v, dou
     if (!s->have_particles) return fail(s, AEP_NOT_READY, "aep_get_particles: no particles");
     if (n != s->np) return fail(s, AEP_INVALID_ARG, "aep_get_particles: n mismatch");
     if (Fp && !s->prm.track_plastic_F) return fail(s, AEP_INVALID_ARG, "aep_get_particles: Fp needs track_plastic_F");
-    CK(cudaStreamSynchronize(s->stream));
     PArrays& P = s->P[s->cur];
     aep_status st;
     const int64_t np = s->np;
     const size_t N = (size_t)np;
+    if ((st = prepare_download(s))) return st;
     if (x && (st = download(s, x, 3, 0, P.x, 0, np, 0, false))) return st;
     if (v && (st = download(s, v, 3, 0, P.v, 0, np, 3 * N, false))) return st;
     if (B && (st = download(s, B, 9, 1, P.B, 0, np, 6 * N, false))) return st;
@@ -1181,6 +1306,7 @@ aep_status aep_get_stats(aep_solver* s, aep_stats* out) {
     out->active_nodes = (int64_t)h.nodes;
     out->learned_accepted = (int64_t)h.learned_ok;
     out->learned_fallbacks = (int64_t)h.learned_rejected;
+    out->sort_movers = s->last_movers;
     double im = std::ldexp(s->m_max, -s->prm.mass_bits), ip = std::ldexp(s->m_max, -s->prm.momentum_bits);
     out->total_mass = (double)(long long)h.mass * im;
     for (int a = 0; a < 3; ++a) out->total_momentum[a] = (double)(long long)h.mom[a] * ip;

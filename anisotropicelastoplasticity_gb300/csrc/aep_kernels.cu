@@ -1336,55 +1336,58 @@ __global__ void k_volumes(KParams P, PArrays cur, const int32_t* __restrict__ pe
 // 2 = 9N per-particle column-major 3x3 into row-major dst[9], 3 = N scalars,
 // 4 = element directions d1 | d2 | d3 (each N x 3 column-major) into the columns of dst[9]
 // map (optional): item q of the source goes to slot map[q] (keeps the device order)
-__global__ void k_upload(int n, int mode, const double* __restrict__ src, float* d0, float* d1, float* d2,
+// Host-layout doubles -> FP32 SoA, one thread per source double (consecutive
+// threads read consecutive doubles, so a source in pinned host memory streams
+// over the host link at full width).  Item q goes to slot map[q] (or q).
+// mode 0: N x 3 column-major; 1: affine momenta (3 blocks of N x 3, block a =
+// row a); 2: 3x3 column-major per item; 3: scalar; 4: element directions
+// (3 blocks of N x 3, block c = column c).
+__global__ void k_upload(long total, int n, int mode, const double* __restrict__ src, float* d0, float* d1, float* d2,
                          float* d3, float* d4, float* d5, float* d6, float* d7, float* d8,
                          const int32_t* __restrict__ map) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // source item
-    if (q >= n) return;
-    const long p = map ? map[q] : q;                       // destination slot
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
     float* d[9] = {d0, d1, d2, d3, d4, d5, d6, d7, d8};
-    if (mode == 0) {
-        for (int a = 0; a < 3; ++a) d[a][p] = (float)src[(long)a * n + q];
-    } else if (mode == 1) {
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[(long)a * 3 * n + (long)b * n + q];
-    } else if (mode == 2) {
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) d[3 * a + b][p] = (float)src[9l * q + a + 3 * b];
+    int k, q;
+    if (mode == 2) {
+        q = (int)(e / 9);
+        const int r = (int)(e % 9);
+        k = 3 * (r % 3) + r / 3;
     } else if (mode == 4) {
-        for (int c = 0; c < 3; ++c)
-            for (int a = 0; a < 3; ++a) d[3 * a + c][p] = (float)src[(long)c * 3 * n + (long)a * n + q];
+        const int t = (int)(e / n);
+        q = (int)(e % n);
+        k = 3 * (t % 3) + t / 3;
     } else {
-        d[0][p] = (float)src[q];
+        k = (int)(e / n);
+        q = (int)(e % n);
     }
+    const long p = map ? map[q] : q;
+    d[k][p] = (float)src[e];
 }
 
-// j runs over all n particle slots; only ids in [id_lo, id_hi) are written, at id - id_lo
-__global__ void k_download(int n, int mode, const int32_t* __restrict__ id, double* __restrict__ dst,
-                           const float* s0, const float* s1, const float* s2, const float* s3, const float* s4,
-                           const float* s5, const float* s6, const float* s7, const float* s8, int id_lo,
-                           int id_hi) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
+// FP32 SoA -> host-layout doubles for ids [id_lo, id_lo + count), one thread per
+// destination double (coalesced writes into pinned host memory); inv[id] = slot.
+__global__ void k_download(long total, int count, int mode, const int32_t* __restrict__ inv, int id_lo,
+                           double* __restrict__ dst, const float* s0, const float* s1, const float* s2,
+                           const float* s3, const float* s4, const float* s5, const float* s6, const float* s7,
+                           const float* s8) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
     const float* s[9] = {s0, s1, s2, s3, s4, s5, s6, s7, s8};
-    const int pid = id[j];
-    if (pid < id_lo || pid >= id_hi) return;
-    const long p = pid - id_lo;
-    n = id_hi - id_lo;
-    if (mode == 0) {
-        for (int a = 0; a < 3; ++a) dst[(long)a * n + p] = s[a][j];
-    } else if (mode == 1) {
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) dst[(long)a * 3 * n + (long)b * n + p] = s[3 * a + b][j];
-    } else if (mode == 2) {
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) dst[9 * p + a + 3 * b] = s[3 * a + b][j];
+    int k, p;
+    if (mode == 2) {
+        p = (int)(e / 9);
+        const int r = (int)(e % 9);
+        k = 3 * (r % 3) + r / 3;
     } else if (mode == 4) {
-        for (int c = 0; c < 3; ++c)
-            for (int a = 0; a < 3; ++a) dst[(long)c * 3 * n + (long)a * n + p] = s[3 * a + c][j];
+        const int t = (int)(e / count);
+        p = (int)(e % count);
+        k = 3 * (t % 3) + t / 3;
     } else {
-        dst[p] = s[0][j];
+        k = (int)(e / count);
+        p = (int)(e % count);
     }
+    dst[e] = (double)s[k][inv[id_lo + p]];
 }
 
 __global__ void k_init_particles(int n, PArrays cur, const uint8_t* __restrict__ mat_in, int has_fp, int track_fp,
@@ -1517,9 +1520,11 @@ void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, i
     if (n > 0) k_volumes<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, perm, n, G);
 }
 void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s, const int32_t* map) {
-    if (n > 0)
-        k_upload<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, src, dst[0], dst[1], dst[2], dst[3], dst[4], dst[5],
-                                                    dst[6], dst[7], dst[8], map);
+    const int per = mode == 3 ? 1 : (mode == 0 ? 3 : 9);
+    const long total = (long)per * n;
+    if (total > 0)
+        k_upload<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(total, n, mode, src, dst[0], dst[1], dst[2], dst[3],
+                                                                 dst[4], dst[5], dst[6], dst[7], dst[8], map);
 }
 void launch_fixed_vertices(const KParams& P, const PArrays& cur, const GArrays& G, const MeshArrays& M,
                            const int32_t* fixed, int nfixed, cudaStream_t s) {
@@ -1538,12 +1543,14 @@ void launch_check_upload(int n, const double* m, const uint8_t* mat, unsigned lo
 void launch_inverse_ids(int n, const int32_t* id, int32_t* inv, cudaStream_t s) {
     if (n > 0) k_inverse_ids<<<blocks_for(n, 256), 256, 0, s>>>(n, id, inv);
 }
-void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s, int id_lo,
-                     int id_hi) {
-    if (id_hi < 0) id_hi = n;
-    if (n > 0)
-        k_download<<<blocks_for(n, 256), 256, 0, s>>>(n, mode, id, dst, src[0], src[1], src[2], src[3], src[4],
-                                                      src[5], src[6], src[7], src[8], id_lo, id_hi);
+void launch_download(int count, int mode, const int32_t* inv, int id_lo, double* dst, float* const* src,
+                     cudaStream_t s) {
+    const int per = mode == 3 ? 1 : (mode == 0 ? 3 : 9);
+    const long total = (long)per * count;
+    if (total > 0)
+        k_download<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(total, count, mode, inv, id_lo, dst, src[0], src[1],
+                                                                   src[2], src[3], src[4], src[5], src[6], src[7],
+                                                                   src[8]);
 }
 void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp, cudaStream_t s,
                            int id0, int fixed_mat, const int32_t* map) {

@@ -30,8 +30,8 @@ void launch_solve_dt(SolveState* S, int phase, cudaStream_t s);
 void launch_query_weights(const KParams& P, const PArrays& cur, const int32_t* inv, const int64_t* ids, int count,
                           int64_t* nodes, double* w, double* g, cudaStream_t s);
 void launch_check_upload(int n, const double* m, const uint8_t* mat, unsigned long long* out, cudaStream_t s);
-void launch_download(int n, int mode, const int32_t* id, double* dst, float* const* src, cudaStream_t s,
-                     int id_lo = 0, int id_hi = -1);
+void launch_download(int count, int mode, const int32_t* inv, int id_lo, double* dst, float* const* src,
+                     cudaStream_t s);
 void launch_init_particles(int n, const PArrays& cur, const uint8_t* mat, int has_fp, int track_fp,
                            cudaStream_t s, int id0 = 0, int fixed_mat = -1, const int32_t* map = nullptr);
 void launch_snow_jp(int n, const PArrays& cur, const double* Fp, cudaStream_t s, const int32_t* map = nullptr);
@@ -40,6 +40,18 @@ void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double*
 
 // device view of a trained MLP (aep_mlp.cu)
 MlpParams mlp_device_params(const aep_mlp* m);
+
+// incremental ordering (aep_sort.cu): partition of the slots into movers and
+// stayers, sort of the movers, merge
+constexpr int kBruteMovers = 16384;  // movers ranked by brute force up to this count
+size_t partition_temp_bytes(int n);
+cudaError_t partition_movers(void* temp, size_t temp_bytes, const uint32_t* keys, const uint32_t* prev,
+                             const int32_t* iota, int32_t* part, int32_t* num_movers, int n, cudaStream_t s);
+cudaError_t sort_movers(void* temp, size_t temp_bytes, const uint32_t* keys, const int32_t* part, int m,
+                        uint32_t* mk_tmp, int32_t* mj_tmp, uint32_t* mkeys, int32_t* mslot, int key_bits,
+                        cudaStream_t s);
+cudaError_t merge_movers(const uint32_t* keys, const int32_t* part, int n, int m, const uint32_t* mkeys,
+                         const int32_t* mslot, uint32_t* keys_out, int32_t* perm_out, cudaStream_t s);
 
 // radix sort of (key, index) pairs; implemented with CUB in aep_sort.cu
 size_t sort_temp_bytes(int n, int key_bits);

@@ -531,5 +531,5 @@ class HybridSolver:
         return dict(steps=s.steps, num_particles=s.num_particles, active_blocks=s.active_blocks,
                     out_of_domain=s.out_of_domain, fp64_fallbacks=s.fp64_fallbacks, overflow=s.overflow,
                     active_nodes=s.active_nodes, learned_accepted=s.learned_accepted,
-                    learned_fallbacks=s.learned_fallbacks,
+                    learned_fallbacks=s.learned_fallbacks, sort_movers=s.sort_movers,
                     total_mass=s.total_mass, total_momentum=list(s.total_momentum))

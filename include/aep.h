@@ -116,7 +116,10 @@ typedef struct aep_params {
     int32_t cloth_volume_weighting; /* 0: in-plane vertex forces as the reference computes
                                        them, without the element volume (LagrangianMesh.cpp:
                                        452-458); 1: multiplied by the element volume        */
-    int32_t reserved_i;
+    int32_t full_sort;       /* 1: radix-sort every step; 0 (default): order incrementally
+                                from the last sorted keys when at most a quarter of the
+                                particles changed cell (same result up to the order of
+                                equal keys)                                            */
     int64_t reserved[6];
 } aep_params;
 
@@ -133,7 +136,9 @@ typedef struct aep_stats {
     double total_momentum[3];   /* grid momentum after the last P2G                      */
     int64_t learned_accepted;   /* learned return maps used in the last step             */
     int64_t learned_fallbacks;  /* learned outputs replaced by the exact mapping         */
-    double reserved[5];
+    int64_t sort_movers;        /* particles that changed cell key in the last ordering,
+                                   -1 when it was a full radix sort                      */
+    double reserved[4];
 } aep_stats;
 
 /* ---- version / defaults ------------------------------------------------------- */

@@ -208,3 +208,91 @@ def test_reupload_keeps_state_and_order():
     ra, rb = a.get_particles(), b.get_particles()
     for k in ("positions", "velocities", "affine_momenta", "elastic_deformation_gradients", "plastic"):
         assert np.array_equal(ra[k], rb[k]), k
+
+
+def test_incremental_ordering_matches_full_sort():
+    """The incremental ordering (movers partitioned out, ranked, merged) against the
+    full radix sort every step: same particles, results equal up to the FP32
+    rounding of the per-run sums (equal keys may be ordered differently)."""
+    sc = perturbed(scenes.sand_column(n=40000, res=32, seed=12), seed=13, vscale=2.0)
+    runs = {}
+    for full in (0, 1):
+        prm = capi.aep_params.from_buffer_copy(sc.params)
+        prm.full_sort = full
+        s = HybridSolver(sc.particles, sc.grid, prm)
+        s.set_level_set(sc.levelset)
+        s.init_volumes()
+        movers = []
+        for _ in range(12):
+            s.step(sc.dt)
+            movers.append(s.stats()["sort_movers"])
+        runs[full] = (s.get_particles(), movers, s.stats()["total_mass"])
+    inc, full = runs[0], runs[1]
+    assert inc[1][0] == -1 and all(0 <= m < 40000 // 4 for m in inc[1][1:])  # first step: full sort
+    assert any(m > 0 for m in inc[1][1:]) and all(m == -1 for m in full[1])
+    assert inc[2] == full[2]  # exact fixed-point mass
+    assert np.abs(inc[0]["positions"] - full[0]["positions"]).max() < 1e-6
+    assert max_rel(inc[0]["velocities"], full[0]["velocities"]) < 1e-4
+
+
+@pytest.mark.parametrize("where", ["pinned", "device"])
+def test_upload_and_readback_from_pinned_and_device_memory(where):
+    """aep_set_particles / aep_get_particles read and write page-locked host memory
+    and device memory directly (no staging copy); the results equal the pageable
+    path bit for bit, including a re-upload that keeps the device order."""
+    import ctypes as C
+
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.solver import mats_to_ref, rows_to_ref, vec_to_ref
+
+    sc = perturbed(scenes.snow_sand_collision(n=12000, res=32, seed=21), seed=22)
+    ps = sc.particles
+    n = len(ps)
+    ref = HybridSolver(ps, sc.grid, sc.params)
+    ref.set_level_set(sc.levelset)
+    ref.init_volumes()
+    for _ in range(3):
+        ref.step(sc.dt)
+    want = ref.get_particles()
+
+    def buf(a):
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        return t.pin_memory() if where == "pinned" else t.cuda()
+
+    host = [vec_to_ref(ps.positions), vec_to_ref(ps.velocities), rows_to_ref(ps.affine_momenta),
+            mats_to_ref(ps.elastic_deformation_gradients), mats_to_ref(ps.plastic_deformation_gradients),
+            np.ascontiguousarray(ps.masses, float), np.ascontiguousarray(ps.volumes, float),
+            np.ascontiguousarray(ps.plastic_amount, float)]
+    bufs = [buf(a) for a in host]
+    mat = buf(np.ascontiguousarray(ps.material, np.uint8))
+    s = HybridSolver(None, sc.grid, sc.params)
+    s._np = n
+    lib, h = s._lib, s._h
+    dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+    assert lib.aep_set_particles(h, n, *[dp(t) for t in bufs], C.cast(C.c_void_p(mat.data_ptr()),
+                                                                     C.POINTER(C.c_uint8))) == 0
+    s.set_level_set(sc.levelset)
+    s.init_volumes()
+    for _ in range(3):
+        s.step(sc.dt)
+    outs = [buf(np.zeros(k * n)) for k in (3, 3, 9, 9, 1, 1)]
+    assert lib.aep_get_particles(h, n, dp(outs[0]), dp(outs[1]), dp(outs[2]), dp(outs[3]), None, dp(outs[4]),
+                                 dp(outs[5])) == 0
+    torch.cuda.synchronize()
+    got = [o.cpu().numpy() for o in outs]
+    wants = [vec_to_ref(want["positions"]), vec_to_ref(want["velocities"]), rows_to_ref(want["affine_momenta"]),
+             mats_to_ref(want["elastic_deformation_gradients"]), want["volumes"], want["plastic"]]
+    for g, w in zip(got, wants):
+        assert np.array_equal(g, np.ravel(w))
+    # re-upload of the read-back state (keeps the device order) and one more step
+    for t, g in zip((bufs[0], bufs[1], bufs[2], bufs[3], bufs[6], bufs[7]), outs):
+        t.copy_(g)
+    assert lib.aep_set_particles(h, n, *[dp(t) for t in bufs[:5]], dp(bufs[5]), dp(bufs[6]), dp(bufs[7]),
+                                 C.cast(C.c_void_p(mat.data_ptr()), C.POINTER(C.c_uint8))) == 0
+    s.step(sc.dt)
+    ref.set_particle_system(ps.__class__(want["positions"], want["velocities"], ps.masses, want["volumes"],
+                                         want["elastic_deformation_gradients"], ps.plastic_deformation_gradients,
+                                         want["affine_momenta"], want["plastic"], ps.material))
+    ref.step(sc.dt)
+    a, b = s.get_particles(), ref.get_particles()
+    assert np.array_equal(a["positions"], b["positions"]) and np.array_equal(a["velocities"], b["velocities"])
