@@ -1008,127 +1008,224 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
     if (clamped) atomicAdd(&st->out_of_domain, 1ull);
 }
 
+// F_E = U diag(sn) V^T into the new order, the plastic scalar and (with
+// track_plastic_F) F_P = V diag(1/sn) U^T F_tr F_P (HybridSolver.cpp:675-677);
+// sprod = prod(s_trial / sn) updates J_P of snow without F_P.
+__device__ __forceinline__ void finish_return_map(const KParams& P, const PArrays& nxt, const PArrays& cur, int j,
+                                                  int pj, int mat, const float Ftr[9], const float U[9],
+                                                  const float V[9], const float s[3], const float sn[3], float q,
+                                                  float sprod) {
+    float US[9], Fe[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) US[3 * r + c] = U[3 * r + c] * sn[c];
+    mat_mul_bt(US, V, Fe);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) nxt.F[k][j] = Fe[k];
+    if (P.track_fp) {
+        float Fp[9], Ft[9], VS[9], M[9], Fpn[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
+        mat_mul(Ftr, Fp, Ft);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) VS[3 * r + c] = V[3 * r + c] / sn[c];
+        mat_mul_bt(VS, U, M);
+        mat_mul(M, Ft, Fpn);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = Fpn[k];
+        if (mat == kSnow) q = mat_det(Fpn);
+    } else if (mat == kSnow) {
+        q *= sprod;  // J_P = det F_P = det(F_tr) det(F_P) / det(S_new)
+    }
+    nxt.plastic[j] = q;
+}
+
+// the whole return mapping in FP64 (the FP32 SVD met a near-degenerate F_tr)
+__device__ __forceinline__ void return_map_fp64(const KParams& P, const PArrays& nxt, const PArrays& cur, int j,
+                                                int pj, int mat, const float Ftr[9], float q, DevStats* st) {
+    double Fd[9], Ud[9], sd[3], Vd[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Fd[k] = Ftr[k];
+    svd3<double>(Fd, Ud, sd, Vd, 40, 1e-15, 0.0);
+    svd3_complete(Ud, sd);
+    const double s0[3] = {sd[0], sd[1], sd[2]};
+    double qd = q;
+    return_map<double>(P, mat, sd, qd);
+    double US[9], Fed[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) US[3 * r + c] = Ud[3 * r + c] * sd[c];
+    mat_mul_bt(US, Vd, Fed);
+    for (int k = 0; k < 9; ++k) nxt.F[k][j] = (float)Fed[k];
+    float qn = (float)qd;
+    if (P.track_fp) {
+        double Fp[9], Ft[9], Ftd[9], VS[9], M[9], Fpn[9];
+        for (int k = 0; k < 9; ++k) {
+            Fp[k] = cur.Fp[k][pj];
+            Ftd[k] = Ftr[k];
+        }
+        mat_mul(Ftd, Fp, Ft);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) VS[3 * r + c] = Vd[3 * r + c] / sd[c];
+        mat_mul_bt(VS, Ud, M);
+        mat_mul(M, Ft, Fpn);
+        for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = (float)Fpn[k];
+        if (mat == kSnow) qn = (float)mat_det(Fpn);
+    } else if (mat == kSnow) {
+        qn = (float)(q * ((s0[0] / sd[0]) * (s0[1] / sd[1]) * (s0[2] / sd[2])));
+    }
+    nxt.plastic[j] = qn;
+    atomicAdd(&st->fallbacks, 1ull);
+}
+
 // ===================================================================================
 // G2P with the learned return map: as k_g2p, but the singular-value return mapping
 // of plastic snow and sand states is predicted by the MLP (aep_mlp.cuh) on the
-// tensor cores, 32 particles per warp.  The yield check (the exact mapping,
-// HybridSolver.cpp:626-674) decides whether a state is plastic; elastic states
-// keep their trial values.  Each plastic prediction is checked against the exact
+// tensor cores.  The yield check (the exact mapping, HybridSolver.cpp:626-674)
+// runs first and decides whether a state is plastic; elastic states keep their
+// trial values and never reach the network.  The plastic rows of a block are
+// compacted (in thread order) into 32-row tiles and the block's warps run the
+// MLP on those tiles only.  Each prediction is checked against the exact
 // projection: if the projected log singular values differ by more than `tol`
 // relative to their largest magnitude (absolute floor 1e-5), the exact value is
-// used instead and counted as a fallback.  No lane leaves before the warp-wide
-// MLP call.
-__global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PArrays nxt,
-                                                     const int32_t* __restrict__ perm, int n, GArrays G, float dt,
-                                                     uint32_t* __restrict__ keys_next, DevStats* st, MlpParams mlp,
-                                                     float tol) {
+// used instead and counted as a fallback.  Persistent: the weights are loaded
+// once per block, which then walks chunks of kLrnThreads particles; every thread
+// runs every chunk, so the block barriers are reached uniformly.
+constexpr int kLrnThreads = 128;
+constexpr int kLrnWarps = kLrnThreads / 32;
+constexpr int kLrnSmemBytes = kMlpSmemBytes + kLrnThreads * kStrideIn * 2 + kLrnThreads * kMlpOut * 4 +
+                              kLrnWarps * 2 * kMlpWarpH * 2;
+
+__global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArrays cur, PArrays nxt,
+                                                             const int32_t* __restrict__ perm, int n, GArrays G,
+                                                             float dt, uint32_t* __restrict__ keys_next,
+                                                             DevStats* st, MlpParams mlp, float tol) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_cnt[kLrnWarps];
     dt = step_dt(P, dt, 1);
     const MlpSmem W = mlp_smem_carve(smem_raw);
     mlp_load_smem(mlp, W, threadIdx.x, blockDim.x);
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned char* wbase = smem_raw + kMlpSmemBytes + warp * kMlpWarpBytes;
-    __nv_bfloat16* MX = reinterpret_cast<__nv_bfloat16*>(wbase);
-    __nv_bfloat16* MH0 = MX + kMlpWarpX;
-    __nv_bfloat16* MH1 = MH0 + kMlpWarpH;
-    float* MY = reinterpret_cast<float*>(MH1 + kMlpWarpH);
+    __nv_bfloat16* CX = reinterpret_cast<__nv_bfloat16*>(smem_raw + kMlpSmemBytes);  // compacted feature rows
+    float* CY = reinterpret_cast<float*>(CX + kLrnThreads * kStrideIn);             // their outputs
+    __nv_bfloat16* H0 = reinterpret_cast<__nv_bfloat16*>(CY + kLrnThreads * kMlpOut) + warp * 2 * kMlpWarpH;
+    __nv_bfloat16* H1 = H0 + kMlpWarpH;
+    __syncthreads();
 
-    // persistent: the weights are loaded once per block, which then walks chunks of
-    // blockDim.x particles (all threads run the same number of iterations)
-    for (long chunk = blockIdx.x; chunk * blockDim.x < n; chunk += gridDim.x) {
-    const int j = (int)(chunk * blockDim.x) + threadIdx.x;
-    const bool live = j < n;
-    const int pj = live ? perm[j] : 0;
-    const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
-    const bool active = live && mat != kClothElement;
-    const bool rm = active && mat <= kSand;
-    float xn[3] = {0, 0, 0}, vp[3] = {0, 0, 0}, Bn[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Ftr[9];
-    float U[9], s[3] = {1, 1, 1}, V[9];
-    bool ok = false;
-    float q = 0.0f;
-    if (active) {
-        float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
-        int cell[3];
-        float f[3], w[3][4], dw[3][4];
-        locate(P, xp[0], xp[1], xp[2], cell, f);
-        const bool truncated = particle_weights(P, cell, f, w, dw);
-        int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
-        uint32_t X[4], Y[4], Z[4];
-        stencil_offsets(P, base, X, Y, Z);
-        float xi[3][4];
+    for (long chunk = blockIdx.x; chunk * kLrnThreads < n; chunk += gridDim.x) {
+        const int j = (int)(chunk * kLrnThreads) + threadIdx.x;
+        const bool live = j < n;
+        const int pj = live ? perm[j] : 0;
+        const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
+        const bool active = live && mat != kClothElement;
+        // --- phase A: gather, advection, APIC, F update, SVD, yield check ------------
+        bool need = false;  // plastic state whose projection the MLP predicts
+        float U[9], V[9], s[3], srt[3], ex[3], lns[3];
+        int pm[3] = {0, 1, 2};
+        float q = 0.0f, qe = 0.0f, osc = 1.0f;
+        float Ftr[9];
+        if (active) {
+            const float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
+            int cell[3];
+            float f[3], w[3][4], dw[3][4];
+            locate(P, xp[0], xp[1], xp[2], cell, f);
+            const bool truncated = particle_weights(P, cell, f, w, dw);
+            int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+            uint32_t X[4], Y[4], Z[4];
+            stencil_offsets(P, base, X, Y, Z);
+            float xi[3][4];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+            for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
-        float xs[3], C[9], Gb[9];
-        g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+                for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
+            float vp[3], xs[3], C[9], Gb[9], xn[3], Bn[9];
+            g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) xn[a] = xp[a] + dt * xs[a];
-        if (truncated) {
-            float s0[3], s1[3];
+            for (int a = 0; a < 3; ++a) xn[a] = xp[a] + dt * xs[a];
+            if (truncated) {
+                float s0[3], s1[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    s0[a] = w[a][0] + w[a][1] + w[a][2] + w[a][3];
+                    s1[a] = w[a][0] * xi[a][0] + w[a][1] * xi[a][1] + w[a][2] * xi[a][2] + w[a][3] * xi[a][3];
+                }
+                const float sw = s0[0] * s0[1] * s0[2];
+                const float swx[3] = {s1[0] * s0[1] * s0[2], s0[0] * s1[1] * s0[2], s0[0] * s0[1] * s1[2]};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) xn[a] += xp[a] * (sw - 1.0f) + swx[a];
+            }
+            apic_damp(C, mat == kClothVertex ? P.mesh_damp : P.particle_damp, Bn);
+            // everything but F and the plastic scalar is final here
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                s0[a] = w[a][0] + w[a][1] + w[a][2] + w[a][3];
-                s1[a] = w[a][0] * xi[a][0] + w[a][1] * xi[a][1] + w[a][2] * xi[a][2] + w[a][3] * xi[a][3];
+                nxt.x[a][j] = xn[a];
+                nxt.v[a][j] = vp[a];
             }
-            const float sw = s0[0] * s0[1] * s0[2];
-            const float swx[3] = {s1[0] * s0[1] * s0[2], s0[0] * s1[1] * s0[2], s0[0] * s0[1] * s1[2]};
 #pragma unroll
-            for (int a = 0; a < 3; ++a) xn[a] += xp[a] * (sw - 1.0f) + swx[a];
+            for (int k = 0; k < 9; ++k) nxt.B[k][j] = Bn[k];
+            nxt.mat[j] = (uint8_t)mat;
+            nxt.m[j] = cur.m[pj];
+            nxt.vol[j] = cur.vol[pj];
+            nxt.id[j] = cur.id[pj];
+            int ncell[3];
+            float nfr[3];
+            const bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nfr);
+            keys_next[j] = make_key(P, ncell);
+            if (clamped) atomicAdd(&st->out_of_domain, 1ull);
+            if (mat == kClothVertex) {
+#pragma unroll
+                for (int k = 0; k < 9; ++k) nxt.F[k][j] = cur.F[k][pj];
+                nxt.plastic[j] = cur.plastic[pj];
+            } else {
+                float F[9], GF[9];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
+                mat_mul(Gb, F, GF);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
+                q = cur.plastic[pj];
+                if (svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f)) {
+                    ex[0] = s[0]; ex[1] = s[1]; ex[2] = s[2];
+                    qe = q;
+                    return_map<float>(P, mat, ex, qe);
+                    need = ex[0] != s[0] || ex[1] != s[1] || ex[2] != s[2];
+                    if (need) {
+                        lns[0] = logf(s[0]); lns[1] = logf(s[1]); lns[2] = logf(s[2]);
+                        sort3_desc(lns, srt, pm);
+                    } else {  // elastic: F_E = F_tr, q unchanged (snow J_P too)
+                        finish_return_map(P, nxt, cur, j, pj, mat, Ftr, U, V, s, s, q, 1.0f);
+                    }
+                } else {
+                    return_map_fp64(P, nxt, cur, j, pj, mat, Ftr, q, st);
+                }
+            }
         }
-        apic_damp(C, mat == kClothVertex ? P.mesh_damp : P.particle_damp, Bn);
-        if (rm) {
-            float F[9], GF[9];
+        // --- phase B: the MLP on the block's plastic rows, compacted -----------------
+        const unsigned bal = __ballot_sync(0xffffffffu, need);
+        if (lane == 0) s_cnt[warp] = __popc(bal);
+        __syncthreads();
+        int row = 0, total = 0;
 #pragma unroll
-            for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
-            mat_mul(Gb, F, GF);
-#pragma unroll
-            for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
-            q = cur.plastic[pj];
-            ok = svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
+        for (int w = 0; w < kLrnWarps; ++w) {
+            row += w < warp ? s_cnt[w] : 0;
+            total += s_cnt[w];
         }
-    }
-    // features: sorted trial log singular values (zero rows for lanes without a map)
-    float lns[3] = {0, 0, 0}, srt[3] = {0, 0, 0};
-    int pm[3] = {0, 1, 2};
-    if (rm && ok) {
-        lns[0] = logf(s[0]); lns[1] = logf(s[1]); lns[2] = logf(s[2]);
-        sort3_desc(lns, srt, pm);
-    }
-    const float osc = mlp_features(srt, q, (rm && ok) ? mat : 0, MX + lane * kStrideIn);
-    mlp_forward_warp(W, MX, MH0, MH1, MY, lane);
-
-    if (!active) continue;
-    if (mat == kClothVertex) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            nxt.x[a][j] = xn[a];
-            nxt.v[a][j] = vp[a];
-        }
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            nxt.B[k][j] = Bn[k];
-            nxt.F[k][j] = cur.F[k][pj];
-        }
-        nxt.plastic[j] = cur.plastic[pj];
-    } else {
-        float Fe[9], sn[3], sprod = 1.0f;
-        double Ud[9], sd[3], Vd[9];
-        bool used_fp64 = false;
-        if (ok) {
-            // the exact mapping decides whether the state is plastic (the yield check)
-            // and is the reference of the residual check
-            float ex[3] = {s[0], s[1], s[2]};
-            float qe = q;
-            return_map<float>(P, mat, ex, qe);
-            const bool plastic = ex[0] != s[0] || ex[1] != s[1] || ex[2] != s[2];
+        row += __popc(bal & ((1u << lane) - 1u));
+        const int tiles = (total + 31) >> 5;
+        if (need) osc = mlp_features(srt, q, mat, CX + row * kStrideIn);
+        if ((int)threadIdx.x >= total && (int)threadIdx.x < 32 * tiles)
+            mlp_features(srt, 0.0f, 0, CX + threadIdx.x * kStrideIn);  // zero rows of the last tile
+        __syncthreads();
+        for (int t = warp; t < tiles; t += kLrnWarps)
+            mlp_forward_warp(W, CX + 32 * t * kStrideIn, H0, H1, CY + 32 * t * kMlpOut, lane);
+        __syncthreads();
+        // --- phase C: check the prediction, F_E = U diag(s_new) V^T ------------------
+        if (need) {
             float pred_ln[3];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int src = pm[k];
-                pred_ln[src] = srt[k] + MY[lane * kMlpOut + k] / osc;
-            }
+            for (int k = 0; k < 3; ++k) pred_ln[pm[k]] = srt[k] + CY[row * kMlpOut + k] / osc;
             // relative residual of the projected log singular values: the stress is
             // nearly linear in them, so this bounds the relative stress error
             float err = 0.0f, ref = 0.0f;
@@ -1138,13 +1235,11 @@ __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PAr
                 err = fmaxf(err, fabsf(pred_ln[a] - le));
                 ref = fmaxf(ref, fabsf(le));
             }
-            const bool accept = plastic && err <= tol * fmaxf(ref, 1e-5f);
-            if (!plastic) {  // elastic: the mapping is the identity, nothing to predict
-                sn[0] = s[0]; sn[1] = s[1]; sn[2] = s[2];
-            } else if (accept) {
+            float sn[3];
+            if (err <= tol * fmaxf(ref, 1e-5f)) {
 #pragma unroll
                 for (int a = 0; a < 3; ++a) sn[a] = expf(pred_ln[a]);
-                if (mat == kSand && qe != q) {  // plastic: q grows by the projection distance
+                if (mat == kSand && qe != q) {  // q grows by the projection distance
                     const float d0 = pred_ln[0] - lns[0], d1 = pred_ln[1] - lns[1], d2 = pred_ln[2] - lns[2];
                     q += sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
                 }
@@ -1154,80 +1249,9 @@ __global__ void __launch_bounds__(128) k_g2p_learned(KParams P, PArrays cur, PAr
                 q = qe;
                 atomicAdd(&st->learned_rejected, 1ull);
             }
-            sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
-            float US[9];
-#pragma unroll
-            for (int r = 0; r < 3; ++r)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) US[3 * r + c] = U[3 * r + c] * sn[c];
-            mat_mul_bt(US, V, Fe);
-        } else {
-            used_fp64 = true;
-            double Fd[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) Fd[k] = Ftr[k];
-            svd3<double>(Fd, Ud, sd, Vd, 40, 1e-15, 0.0);
-            svd3_complete(Ud, sd);
-            double s0[3] = {sd[0], sd[1], sd[2]};
-            double qd = q;
-            return_map<double>(P, mat, sd, qd);
-            q = (float)qd;
-            sprod = (float)((s0[0] / sd[0]) * (s0[1] / sd[1]) * (s0[2] / sd[2]));
-            double US[9], Fed[9];
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) US[3 * r + c] = Ud[3 * r + c] * sd[c];
-            mat_mul_bt(US, Vd, Fed);
-#pragma unroll
-            for (int k = 0; k < 9; ++k) Fe[k] = (float)Fed[k];
-            atomicAdd(&st->fallbacks, 1ull);
+            finish_return_map(P, nxt, cur, j, pj, mat, Ftr, U, V, s, sn, q,
+                              (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]));
         }
-        if (P.track_fp) {
-            float Fp[9], Ft[9], M[9], Fpn[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
-            mat_mul(Ftr, Fp, Ft);
-            if (!used_fp64) {
-                float VS[9];
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) VS[3 * r + c] = V[3 * r + c] / sn[c];
-                mat_mul_bt(VS, U, M);
-            } else {
-                double VSd[9], Md[9];
-                for (int r = 0; r < 3; ++r)
-                    for (int c = 0; c < 3; ++c) VSd[3 * r + c] = Vd[3 * r + c] / sd[c];
-                mat_mul_bt(VSd, Ud, Md);
-                for (int k = 0; k < 9; ++k) M[k] = (float)Md[k];
-            }
-            mat_mul(M, Ft, Fpn);
-#pragma unroll
-            for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = Fpn[k];
-            if (mat == kSnow) q = mat_det(Fpn);
-        } else if (mat == kSnow) {
-            q *= sprod;
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            nxt.x[a][j] = xn[a];
-            nxt.v[a][j] = vp[a];
-        }
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            nxt.B[k][j] = Bn[k];
-            nxt.F[k][j] = Fe[k];
-        }
-        nxt.plastic[j] = q;
-    }
-    nxt.mat[j] = (uint8_t)mat;
-    nxt.m[j] = cur.m[pj];
-    nxt.vol[j] = cur.vol[pj];
-    nxt.id[j] = cur.id[pj];
-    int ncell[3];
-    float nf[3];
-    const bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nf);
-    keys_next[j] = make_key(P, ncell);
-    if (clamped) atomicAdd(&st->out_of_domain, 1ull);
     }
 }
 
@@ -1501,14 +1525,15 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
                 const Harvest& H, const MlpParams* mlp, float learned_tol) {
     if (n > 0) {
         if (mlp) {
-            const int smem = kMlpSmemBytes + 4 * kMlpWarpBytes;
+            const int smem = kLrnSmemBytes;
             cudaFuncSetAttribute(k_g2p_learned, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             int dev = 0, sms = 0, per_sm = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_g2p_learned, 128, smem);
-            const int blocks = std::min(blocks_for(n, 128), std::max(1, sms * std::max(per_sm, 1)));
-            k_g2p_learned<<<blocks, 128, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp, learned_tol);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_g2p_learned, kLrnThreads, smem);
+            const int blocks = std::min(blocks_for(n, kLrnThreads), std::max(1, sms * std::max(per_sm, 1)));
+            k_g2p_learned<<<blocks, kLrnThreads, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp,
+                                                            learned_tol);
         } else {
             k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H);
         }

@@ -79,7 +79,7 @@ struct TrainSmem {
 };
 
 __device__ __forceinline__ float dsilu(float z) {
-    const float s = 1.0f / (1.0f + __expf(-z));
+    const float s = __frcp_rn(1.0f + __expf(-z));
     return s * (1.0f + z * (1.0f - s));
 }
 

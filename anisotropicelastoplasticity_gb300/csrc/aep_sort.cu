@@ -43,27 +43,24 @@ struct MoverOp {
 
 constexpr int kRankThreads = 256;
 
-// rank of mover i among all movers by (key, partition index); partition order is
-// slot order, so ties keep slot order
+// rank of mover i among all movers by (key, partition index), one warp per mover;
+// partition order is slot order, so ties keep slot order
 __global__ void __launch_bounds__(kRankThreads) k_rank_movers(const uint32_t* __restrict__ keys,
                                                               const int32_t* __restrict__ part, int m,
                                                               uint32_t* __restrict__ mkeys, int32_t* __restrict__ mslot) {
-    __shared__ unsigned long long tile[kRankThreads];
-    const int i = blockIdx.x * kRankThreads + threadIdx.x;
-    const int ji = i < m ? part[i] : 0;
-    const unsigned long long ci = i < m ? ((unsigned long long)keys[ji] << 32) | (unsigned)i : ~0ull;
+    const int i = (int)(((long)blockIdx.x * kRankThreads + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= m) return;
+    const int ji = part[i];
+    const uint32_t ki = keys[ji];
     int rank = 0;
-    for (int t0 = 0; t0 < m; t0 += kRankThreads) {
-        const int k = t0 + threadIdx.x;
-        tile[threadIdx.x] = k < m ? ((unsigned long long)keys[part[k]] << 32) | (unsigned)k : ~0ull;
-        __syncthreads();
-        const int cnt = min(kRankThreads, m - t0);
-#pragma unroll 8
-        for (int q = 0; q < cnt; ++q) rank += tile[q] < ci;
-        __syncthreads();
+    for (int k = lane; k < m; k += 32) {
+        const uint32_t kk = keys[part[k]];
+        rank += (kk < ki) | ((kk == ki) & (k < i));
     }
-    if (i < m) {
-        mkeys[rank] = (uint32_t)(ci >> 32);
+    rank = __reduce_add_sync(0xffffffffu, rank);
+    if (lane == 0) {
+        mkeys[rank] = ki;
         mslot[rank] = ji;
     }
 }
@@ -129,7 +126,9 @@ cudaError_t sort_movers(void* temp, size_t temp_bytes, const uint32_t* keys, con
                         cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
     if (m <= kBruteMovers) {
-        k_rank_movers<<<(m + kRankThreads - 1) / kRankThreads, kRankThreads, 0, s>>>(keys, part, m, mkeys, mslot);
+        const long threads = 32l * m;
+        k_rank_movers<<<(unsigned)((threads + kRankThreads - 1) / kRankThreads), kRankThreads, 0, s>>>(keys, part, m,
+                                                                                                     mkeys, mslot);
         return cudaGetLastError();
     }
     k_gather_movers<<<(m + 255) / 256, 256, 0, s>>>(keys, part, m, mk_tmp, mj_tmp);

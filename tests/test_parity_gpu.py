@@ -286,7 +286,7 @@ def test_upload_and_readback_from_pinned_and_device_memory(where):
         assert np.array_equal(g, np.ravel(w))
     # re-upload of the read-back state (keeps the device order) and one more step
     for t, g in zip((bufs[0], bufs[1], bufs[2], bufs[3], bufs[6], bufs[7]), outs):
-        t.copy_(g)
+        t.view(-1).copy_(g)
     assert lib.aep_set_particles(h, n, *[dp(t) for t in bufs[:5]], dp(bufs[5]), dp(bufs[6]), dp(bufs[7]),
                                  C.cast(C.c_void_p(mat.data_ptr()), C.POINTER(C.c_uint8))) == 0
     s.step(sc.dt)
