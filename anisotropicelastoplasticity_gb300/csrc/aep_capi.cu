@@ -72,7 +72,9 @@ struct aep_solver {
     void* part_tmp = nullptr;
     size_t part_bytes = 0;
     bool prev_sorted = false;  // keys_sorted holds an ascending array of the current n
-    int64_t last_movers = -1;  // movers of the last incremental ordering (-1: full sort)
+    void* order_graph = nullptr;  // the incremental ordering, captured (aep_sort.cu)
+    int order_graph_n = -1;
+    cudaStream_t capture_stream = nullptr;
     GArrays G{};
     size_t nnodes = 0;
     int nblocks = 0;
@@ -245,6 +247,9 @@ void free_particles(aep_solver* s) {
     cudaFree(s->perm);
     cudaFree(s->sort_tmp);
     cudaFree(s->staging);
+    order_graph_destroy(s->order_graph);
+    s->order_graph = nullptr;
+    s->order_graph_n = -1;
     cudaFree(s->part);
     cudaFree(s->part_tmp);
     cudaFree(s->inv);
@@ -413,30 +418,30 @@ inline void mark(aep_solver* s, int boundary) {
 }
 
 // Order the current particles by key into keys_sorted / perm: incrementally from
-// the last sorted keys when few particles changed cell, else a full radix sort.
-// The incremental path reads the mover count back (one stream synchronisation).
+// the last sorted keys (a captured graph whose branch is chosen on the device,
+// aep_sort.cu), or a full radix sort when there are no sorted keys yet.
 cudaError_t order_particles(aep_solver* s) {
     const int n = (int)s->n;
-    s->last_movers = -1;
     if (!s->prm.full_sort && s->prev_sorted && n >= 4096) {
-        cudaError_t e = partition_movers(s->part_tmp, s->part_bytes, s->keys, s->keys_sorted, s->iota, s->part,
-                                         s->nmov, n, s->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(s->nmov_host, s->nmov, sizeof(int32_t), cudaMemcpyDeviceToHost,
-                                                  s->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-        if (e != cudaSuccess) return e;
-        const int m = *s->nmov_host;
-        if (m >= 0 && m <= n / 4) {
-            e = sort_movers(s->sort_tmp, s->sort_bytes, s->keys, s->part, m, s->mk_tmp, s->mj_tmp, s->mkeys,
-                            s->mslot, s->key_bits, s->stream);
-            if (e == cudaSuccess)
-                e = merge_movers(s->keys, s->part, n, m, s->mkeys, s->mslot, s->keys_sorted, s->perm, s->stream);
-            s->last_movers = m;
-            return e;
+        if (!s->order_graph || s->order_graph_n != n) {
+            order_graph_destroy(s->order_graph);
+            s->order_graph = nullptr;
+            if (!s->capture_stream) {
+                cudaError_t e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking);
+                if (e != cudaSuccess) return e;
+            }
+            OrderBuffers b{s->keys, s->keys_sorted, s->perm, s->iota, s->part, s->nmov, s->mk_tmp, s->mj_tmp,
+                           s->mkeys, s->mslot, s->part_tmp, s->part_bytes, s->sort_tmp, s->sort_bytes, n, n / 4,
+                           s->key_bits, s->dstats};
+            cudaError_t e = order_graph_build(&s->order_graph, s->capture_stream, b);
+            if (e != cudaSuccess) return e;
+            s->order_graph_n = n;
         }
+        return order_graph_launch(s->order_graph, s->stream);
     }
     cudaError_t e = sort_pairs(s->sort_tmp, s->sort_bytes, s->keys, s->keys_sorted, s->iota, s->perm, n,
                                s->key_bits, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&s->dstats->movers, 0xFF, sizeof(long long), s->stream);  // -1
     if (e == cudaSuccess) s->prev_sorted = true;
     return e;
 }
@@ -573,6 +578,7 @@ aep_status aep_solver_destroy(aep_solver* s) {
         for (int p = 0; p <= AEP_NUM_PHASES; ++p)
             if (s->ev[r][p]) cudaEventDestroy(s->ev[r][p]);
     cudaStreamDestroy(s->own_stream);
+    if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
     delete s;
     return AEP_OK;
 }
@@ -1306,7 +1312,7 @@ aep_status aep_get_stats(aep_solver* s, aep_stats* out) {
     out->active_nodes = (int64_t)h.nodes;
     out->learned_accepted = (int64_t)h.learned_ok;
     out->learned_fallbacks = (int64_t)h.learned_rejected;
-    out->sort_movers = s->last_movers;
+    out->sort_movers = (int64_t)h.movers;
     double im = std::ldexp(s->m_max, -s->prm.mass_bits), ip = std::ldexp(s->m_max, -s->prm.momentum_bits);
     out->total_mass = (double)(long long)h.mass * im;
     for (int a = 0; a < 3; ++a) out->total_momentum[a] = (double)(long long)h.mom[a] * ip;

@@ -129,6 +129,7 @@ struct DevStats {
     unsigned long long nodes;      // nodes with mass after P2G
     unsigned long long learned_ok;      // learned return maps accepted
     unsigned long long learned_rejected;  // learned outputs replaced by the exact mapping
+    long long movers;              // particles that changed key (incremental ordering), -1: full sort
 };
 
 // Training-pair harvest from the exact return mapping (plain G2P): records of 8
@@ -525,26 +526,33 @@ __device__ __forceinline__ void cloth_normal_stress(const float D[9], const floa
         for (int b = 0; b < 3; ++b) S[3 * a + b] = vol * dF3[a] * D[3 * b + 2];
 }
 
+// Cloth return mapping on the third column r = (r13, r23, r33) of the QR factor
+// (HybridSolver.cpp:701-717): no tension (r33 <= 1, else r = e3) and a frictional
+// cap of the shear by the normal force.
+__device__ __forceinline__ void cloth_project(float r[3], float shear, float stiffness, float friction) {
+    if (r[2] > 1.0f) {
+        r[2] = 1.0f;
+        r[0] = r[1] = 0.0f;
+    } else {
+        const float nf = stiffness * (r[2] - 1.0f) * (r[2] - 1.0f);
+        const float sf = shear * sqrtf(r[0] * r[0] + r[1] * r[1]);
+        if (sf > friction * nf) {
+            const float sc = friction * nf / sf;
+            r[0] *= sc;
+            r[1] *= sc;
+        }
+    }
+}
+
 // Cloth return mapping (HybridSolver.cpp:695-719): new d3 from the QR of [d1 d2 d3].
 __device__ __forceinline__ void cloth_return_map(const float D[9], float shear, float stiffness, float friction,
                                                  float d3[3]) {
     float Q[9], R[9];
     gram_schmidt(D, Q, R);
-    float r13 = R[2], r23 = R[5], r33 = R[8];
-    if (r33 > 1.0f) {
-        r33 = 1.0f;
-        r13 = r23 = 0.0f;
-    } else {
-        const float nf = stiffness * (r33 - 1.0f) * (r33 - 1.0f);
-        const float sf = shear * sqrtf(r13 * r13 + r23 * r23);
-        if (sf > friction * nf) {
-            const float sc = friction * nf / sf;
-            r13 *= sc;
-            r23 *= sc;
-        }
-    }
+    float r[3] = {R[2], R[5], R[8]};
+    cloth_project(r, shear, stiffness, friction);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) d3[a] = Q[3 * a] * r13 + Q[3 * a + 1] * r23 + Q[3 * a + 2] * r33;
+    for (int a = 0; a < 3; ++a) d3[a] = Q[3 * a] * r[0] + Q[3 * a + 1] * r[1] + Q[3 * a + 2] * r[2];
 }
 
 __device__ __forceinline__ unsigned long long to_fixed(float v, float scale) {

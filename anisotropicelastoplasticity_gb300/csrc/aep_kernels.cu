@@ -1261,74 +1261,138 @@ __global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArra
 // velocities (HS:749-756), position = centroid of the new vertex positions
 // (LagrangianMesh.cpp:371-380), directions d1, d2 from the vertices and
 // d3 += dt grad v^bf d3 (HS:584-607), then the QR return mapping (HS:686-720).
-__global__ void k_cloth_g2p(KParams P, PArrays cur, PArrays nxt, GArrays G, MeshArrays M, float dt,
-                            uint32_t* __restrict__ keys_next, DevStats* st) {
+// With an MLP (use_mlp), the cloth return mapping of plastic elements is predicted
+// by the learned map (cloth rows of the same network) and checked against the
+// exact projection as in k_g2p_learned; the warp runs the network when any of its
+// elements is plastic.  With a harvest buffer, plastic elements record
+// [r13, r23, r33 - 1, 0, 2, projected - trial (3)].
+__global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArrays nxt, GArrays G, MeshArrays M,
+                                                   float dt, uint32_t* __restrict__ keys_next, DevStats* st,
+                                                   Harvest H, MlpParams mlp, int use_mlp, float tol) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= M.nf) return;
+    const bool live = e < M.nf;
     dt = step_dt(P, dt, 1);
-    const int id = M.ebase + e;
-    const int j = M.slot_of[id];
-    const int pc = M.curidx_of[id];
-    float xp[3] = {cur.x[0][pc], cur.x[1][pc], cur.x[2][pc]};
-    int cell[3];
-    float f[3], w[3][4], dw[3][4];
-    locate(P, xp[0], xp[1], xp[2], cell, f);
-    particle_weights(P, cell, f, w, dw);
-    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
-    uint32_t X[4], Y[4], Z[4];
-    stencil_offsets(P, base, X, Y, Z);
-    float xi[3][4];
+    MlpSmem W{};
+    if (use_mlp) {  // block-uniform
+        W = mlp_smem_carve(smem_raw);
+        mlp_load_smem(mlp, W, threadIdx.x, blockDim.x);
+        __syncthreads();
+    }
+    float Q[9], r[3] = {0, 0, 1}, rp[3] = {0, 0, 1};
+    bool plastic = false;
+    int j = 0, pc = 0;
+    if (live) {
+        const int id = M.ebase + e;
+        j = M.slot_of[id];
+        pc = M.curidx_of[id];
+        float xp[3] = {cur.x[0][pc], cur.x[1][pc], cur.x[2][pc]};
+        int cell[3];
+        float f[3], w[3][4], dw[3][4];
+        locate(P, xp[0], xp[1], xp[2], cell, f);
+        particle_weights(P, cell, f, w, dw);
+        int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+        uint32_t X[4], Y[4], Z[4];
+        stencil_offsets(P, base, X, Y, Z);
+        float xi[3][4];
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
-    float vp[3], xs[3], C[9], Gb[9];
-    g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
-    float Bn[9];
-    apic_damp(C, P.mesh_damp, Bn);
-    float xv[3][3], vv[3][3];
+            for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
+        float vp[3], xs[3], C[9], Gb[9];
+        g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+        float Bn[9];
+        apic_damp(C, P.mesh_damp, Bn);
+        float xv[3][3], vv[3][3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const int sv = M.slot_of[M.vbase + M.faces[3 * e + c]];
+        for (int c = 0; c < 3; ++c) {
+            const int sv = M.slot_of[M.vbase + M.faces[3 * e + c]];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                xv[c][a] = nxt.x[a][sv];
+                vv[c][a] = nxt.v[a][sv];
+            }
+        }
+        float D[9];
+        const float d3o[3] = {cur.F[2][pc], cur.F[5][pc], cur.F[8][pc]};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            xv[c][a] = nxt.x[a][sv];
-            vv[c][a] = nxt.v[a][sv];
+            D[3 * a + 0] = xv[1][a] - xv[0][a];
+            D[3 * a + 1] = xv[2][a] - xv[0][a];
+            D[3 * a + 2] = dt * (Gb[3 * a] * d3o[0] + Gb[3 * a + 1] * d3o[1] + Gb[3 * a + 2] * d3o[2]) + d3o[a];
+        }
+        float R[9];
+        gram_schmidt(D, Q, R);
+        r[0] = R[2]; r[1] = R[5]; r[2] = R[8];
+        rp[0] = r[0]; rp[1] = r[1]; rp[2] = r[2];
+        cloth_project(rp, M.shear, M.stiffness, M.friction);
+        plastic = rp[0] != r[0] || rp[1] != r[1] || rp[2] != r[2];
+        if (H.buf && plastic && (e % H.stride) == 0) {
+            const unsigned long long slot = atomicAdd(H.count, 1ull);
+            if ((long long)slot < H.capacity) {
+                float* o = H.buf + 8ull * slot;
+                o[0] = r[0]; o[1] = r[1]; o[2] = r[2] - 1.0f; o[3] = 0.0f; o[4] = (float)kMlpCloth;
+                o[5] = rp[0] - r[0]; o[6] = rp[1] - r[1]; o[7] = rp[2] - r[2];
+            }
+        }
+        float xn[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            xn[a] = (xv[0][a] + xv[1][a] + xv[2][a]) / 3.0f;
+            nxt.x[a][j] = xn[a];
+            nxt.v[a][j] = (vv[0][a] + vv[1][a] + vv[2][a]) / 3.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) nxt.B[k][j] = Bn[k];
+        nxt.F[0][j] = D[0]; nxt.F[1][j] = D[1];
+        nxt.F[3][j] = D[3]; nxt.F[4][j] = D[4];
+        nxt.F[6][j] = D[6]; nxt.F[7][j] = D[7];
+        nxt.plastic[j] = cur.plastic[pc];
+        nxt.mat[j] = (uint8_t)kClothElement;
+        nxt.m[j] = cur.m[pc];
+        nxt.vol[j] = cur.vol[pc];
+        nxt.id[j] = id;
+        int nc[3];
+        float nf[3];
+        const bool clamped = locate(P, xn[0], xn[1], xn[2], nc, nf);
+        keys_next[j] = make_key(P, nc);
+        if (clamped) atomicAdd(&st->out_of_domain, 1ull);
+    }
+    if (use_mlp) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        unsigned char* wbase = smem_raw + kMlpSmemBytes + warp * kMlpWarpBytes;
+        __nv_bfloat16* MX = reinterpret_cast<__nv_bfloat16*>(wbase);
+        __nv_bfloat16* MH0 = MX + kMlpWarpX;
+        __nv_bfloat16* MH1 = MH0 + kMlpWarpH;
+        float* MY = reinterpret_cast<float*>(MH1 + kMlpWarpH);
+        if (__any_sync(0xffffffffu, plastic)) {  // warp-uniform
+            const float in[3] = {r[0], r[1], r[2] - 1.0f};
+            const float sc = mlp_features(in, 0.0f, plastic ? kMlpCloth : 0, MX + lane * kStrideIn);
+            mlp_forward_warp(W, MX, MH0, MH1, MY, lane);
+            if (plastic) {
+                // residual relative to the projected shear and normal strain
+                // (r13, r23, r33 - 1), whose size sets the cloth stresses
+                float pred[3], err = 0.0f;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    pred[a] = r[a] + MY[lane * kMlpOut + a] / sc;
+                    err = fmaxf(err, fabsf(pred[a] - rp[a]));
+                }
+                const float ref = fmaxf(fmaxf(fabsf(rp[0]), fabsf(rp[1])), fabsf(rp[2] - 1.0f));
+                if (err <= tol * fmaxf(ref, 1e-5f)) {
+                    rp[0] = pred[0]; rp[1] = pred[1]; rp[2] = pred[2];
+                    atomicAdd(&st->learned_ok, 1ull);
+                } else {
+                    atomicAdd(&st->learned_rejected, 1ull);
+                }
+            }
         }
     }
-    float D[9];
-    float d3o[3] = {cur.F[2][pc], cur.F[5][pc], cur.F[8][pc]};
+    if (live) {
+        // d3 = Q r (HybridSolver.cpp:718-719)
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        D[3 * a + 0] = xv[1][a] - xv[0][a];
-        D[3 * a + 1] = xv[2][a] - xv[0][a];
-        D[3 * a + 2] = dt * (Gb[3 * a] * d3o[0] + Gb[3 * a + 1] * d3o[1] + Gb[3 * a + 2] * d3o[2]) + d3o[a];
+        for (int a = 0; a < 3; ++a) nxt.F[3 * a + 2][j] = Q[3 * a] * rp[0] + Q[3 * a + 1] * rp[1] + Q[3 * a + 2] * rp[2];
     }
-    float d3[3];
-    cloth_return_map(D, M.shear, M.stiffness, M.friction, d3);
-    D[2] = d3[0]; D[5] = d3[1]; D[8] = d3[2];
-    float xn[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        xn[a] = (xv[0][a] + xv[1][a] + xv[2][a]) / 3.0f;
-        nxt.x[a][j] = xn[a];
-        nxt.v[a][j] = (vv[0][a] + vv[1][a] + vv[2][a]) / 3.0f;
-    }
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        nxt.B[k][j] = Bn[k];
-        nxt.F[k][j] = D[k];
-    }
-    nxt.plastic[j] = cur.plastic[pc];
-    nxt.mat[j] = (uint8_t)kClothElement;
-    nxt.m[j] = cur.m[pc];
-    nxt.vol[j] = cur.vol[pc];
-    nxt.id[j] = id;
-    int nc[3];
-    float nf[3];
-    const bool clamped = locate(P, xn[0], xn[1], xn[2], nc, nf);
-    keys_next[j] = make_key(P, nc);
-    if (clamped) atomicAdd(&st->out_of_domain, 1ull);
 }
 
 // ===================================================================================
@@ -1538,7 +1602,12 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
             k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H);
         }
     }
-    if (M.nf > 0) k_cloth_g2p<<<blocks_for(M.nf, 128), 128, 0, s>>>(P, cur, nxt, G, M, dt, keys_next, st);
+    if (M.nf > 0) {
+        const int smem = mlp ? kMlpSmemBytes + 4 * kMlpWarpBytes : 0;
+        if (mlp) cudaFuncSetAttribute(k_cloth_g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        k_cloth_g2p<<<blocks_for(M.nf, 128), 128, smem, s>>>(P, cur, nxt, G, M, dt, keys_next, st, H,
+                                                             mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, learned_tol);
+    }
 }
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s) {

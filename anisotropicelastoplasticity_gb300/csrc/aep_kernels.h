@@ -42,16 +42,31 @@ void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double*
 MlpParams mlp_device_params(const aep_mlp* m);
 
 // incremental ordering (aep_sort.cu): partition of the slots into movers and
-// stayers, sort of the movers, merge
-constexpr int kBruteMovers = 16384;  // movers ranked by brute force up to this count
+// stayers, sort of the movers, merge; captured as a CUDA graph whose branch
+// (brute-force rank, radix sort of the movers, full sort) is chosen on the device
+constexpr int kBruteMovers = 8192;  // movers ranked by brute force up to this count
+struct OrderBuffers {
+    const uint32_t* keys;  // new keys in the current order
+    uint32_t* keys_sorted; // in: the last sorted keys (ascending); out: this ordering's keys
+    int32_t* perm;         // out: current slot of each sorted position
+    const int32_t* iota;
+    int32_t* part;         // partition: movers first (slot order), stayers last (reversed)
+    int32_t* nmov;         // device mover count
+    uint32_t* mk_tmp;      // cap padded mover keys / slots, and the sorted ones
+    int32_t* mj_tmp;
+    uint32_t* mkeys;
+    int32_t* mslot;
+    void* part_tmp;
+    size_t part_bytes;
+    void* sort_tmp;
+    size_t sort_bytes;
+    int n, cap, key_bits;
+    DevStats* st;
+};
 size_t partition_temp_bytes(int n);
-cudaError_t partition_movers(void* temp, size_t temp_bytes, const uint32_t* keys, const uint32_t* prev,
-                             const int32_t* iota, int32_t* part, int32_t* num_movers, int n, cudaStream_t s);
-cudaError_t sort_movers(void* temp, size_t temp_bytes, const uint32_t* keys, const int32_t* part, int m,
-                        uint32_t* mk_tmp, int32_t* mj_tmp, uint32_t* mkeys, int32_t* mslot, int key_bits,
-                        cudaStream_t s);
-cudaError_t merge_movers(const uint32_t* keys, const int32_t* part, int n, int m, const uint32_t* mkeys,
-                         const int32_t* mslot, uint32_t* keys_out, int32_t* perm_out, cudaStream_t s);
+cudaError_t order_graph_build(void** out, cudaStream_t capture_stream, const OrderBuffers& b);
+cudaError_t order_graph_launch(void* graph, cudaStream_t s);
+void order_graph_destroy(void* graph);
 
 // radix sort of (key, index) pairs; implemented with CUB in aep_sort.cu
 size_t sort_temp_bytes(int n, int key_bits);

@@ -1,10 +1,11 @@
-// aep_mlp.cuh -- the learned return map: a 6 -> 64 -> 64 -> 64 -> 3 MLP with SiLU,
+// aep_mlp.cuh -- the learned return map: a 7 -> 64 -> 64 -> 64 -> 3 MLP with SiLU,
 // BF16 weights on the tensor cores (mma.sync m16n8k16, FP32 accumulation).
 //
 // Input features (one row per particle): the trial log singular values of F_E^tr
 // sorted descending (3; normalised for sand, scaled by kLnScale for snow, see
 // mlp_features), the sand plastic amount q (1), and the material one-hot (snow,
-// sand) (2); padded to 16 columns.  Output: the correction (ln s_projected -
+// sand, cloth) (3); padded to 16 columns.  Cloth elements use the same network
+// on (r13, r23, r33 - 1) of their QR factor.  Output: the correction (ln s_projected -
 // ln s_trial) in the same order and the same scaling (3 of 8).
 // The return mappings it stands in for (HybridSolver.cpp:626-674) are invariant
 // under permutations of the singular values, so sorting canonicalises the input.
@@ -169,14 +170,20 @@ __device__ __forceinline__ void mlp_forward_warp(const MlpSmem& W, __nv_bfloat16
     __syncwarp();
 }
 
+constexpr int kMlpCloth = 2;        // material code of cloth element records
+constexpr float kClothScale = 50.0f;  // cloth features and outputs are R entries times this
+
 // Feature row of one particle and the scale of its output.  Sand: the Drucker-Prager
 // projection onto a cone is positively homogeneous in ln s, so the sorted trial
 // log singular values are normalised by their norm r and the network predicts the
 // correction divided by r.  Snow: the clamp bounds are absolute, so ln s and the
 // correction are scaled by kLnScale.  Returns the factor that maps a correction to
 // the network's output (sand: 1/r, snow: kLnScale).
+// Cloth (mat == kMlpCloth): the input is (r13, r23, r33 - 1) of the QR factor of the
+// element directions, the output the change of (r13, r23, r33) by the cloth return
+// mapping (HybridSolver.cpp:701-717), both scaled by kClothScale; one-hot column 6.
 __device__ __forceinline__ float mlp_features(const float ln_sorted[3], float q, int mat, __nv_bfloat16* row) {
-    float sc = kLnScale;
+    float sc = mat == kMlpCloth ? kClothScale : kLnScale;
     if (mat == 1) {
         const float r = sqrtf(ln_sorted[0] * ln_sorted[0] + ln_sorted[1] * ln_sorted[1] + ln_sorted[2] * ln_sorted[2]);
         sc = 1.0f / fmaxf(r, 1e-20f);
@@ -187,8 +194,9 @@ __device__ __forceinline__ float mlp_features(const float ln_sorted[3], float q,
     row[3] = __float2bfloat16(mat == 1 ? q : 0.0f);
     row[4] = __float2bfloat16(mat == 0 ? 1.0f : 0.0f);
     row[5] = __float2bfloat16(mat == 1 ? 1.0f : 0.0f);
+    row[6] = __float2bfloat16(mat == kMlpCloth ? 1.0f : 0.0f);
 #pragma unroll
-    for (int k = 6; k < kMlpIn; ++k) row[k] = __float2bfloat16(0.0f);
+    for (int k = 7; k < kMlpIn; ++k) row[k] = __float2bfloat16(0.0f);
     return sc;
 }
 

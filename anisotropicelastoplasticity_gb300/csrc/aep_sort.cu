@@ -44,10 +44,13 @@ struct MoverOp {
 constexpr int kRankThreads = 256;
 
 // rank of mover i among all movers by (key, partition index), one warp per mover;
-// partition order is slot order, so ties keep slot order
+// partition order is slot order, so ties keep slot order.  m is read on the device.
 __global__ void __launch_bounds__(kRankThreads) k_rank_movers(const uint32_t* __restrict__ keys,
-                                                              const int32_t* __restrict__ part, int m,
+                                                              const int32_t* __restrict__ part,
+                                                              const int32_t* __restrict__ nmov, int cap,
                                                               uint32_t* __restrict__ mkeys, int32_t* __restrict__ mslot) {
+    const int m = *nmov;
+    if (m > cap) return;  // not this branch (the decision kernel never sends it here)
     const int i = (int)(((long)blockIdx.x * kRankThreads + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= m) return;
@@ -65,21 +68,31 @@ __global__ void __launch_bounds__(kRankThreads) k_rank_movers(const uint32_t* __
     }
 }
 
-__global__ void k_gather_movers(const uint32_t* __restrict__ keys, const int32_t* __restrict__ part, int m,
-                                uint32_t* __restrict__ mk, int32_t* __restrict__ mj) {
+// movers into `cap` sort slots; slots past m get the largest key of the sorted
+// bits (`pad`) and, coming last, stay after any mover with that key (stable sort)
+__global__ void k_gather_movers(const uint32_t* __restrict__ keys, const int32_t* __restrict__ part,
+                                const int32_t* __restrict__ nmov, int cap, uint32_t pad, uint32_t* __restrict__ mk,
+                                int32_t* __restrict__ mj) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < m) {
+    if (r >= cap) return;
+    if (r < *nmov) {
         const int j = part[r];
         mk[r] = keys[j];
         mj[r] = j;
+    } else {
+        mk[r] = pad;
+        mj[r] = -1;
     }
 }
 
 // merge of the stayers (partition tail, reversed: stayer q is part[n-1-q]) and the
 // sorted movers; stayers go before movers with an equal key
-__global__ void k_merge_movers(const uint32_t* __restrict__ keys, const int32_t* __restrict__ part, int n, int m,
-                               const uint32_t* __restrict__ mkeys, const int32_t* __restrict__ mslot,
-                               uint32_t* __restrict__ keys_out, int32_t* __restrict__ perm_out) {
+__global__ void k_merge_movers(const uint32_t* __restrict__ keys, const int32_t* __restrict__ part, int n, int cap,
+                               const int32_t* __restrict__ nmov, const uint32_t* __restrict__ mkeys,
+                               const int32_t* __restrict__ mslot, uint32_t* __restrict__ keys_out,
+                               int32_t* __restrict__ perm_out) {
+    const int m = *nmov;
+    if (m > cap || m > n) return;  // not this branch
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int ns = n - m;
     if (t < ns) {
@@ -107,6 +120,34 @@ __global__ void k_merge_movers(const uint32_t* __restrict__ keys, const int32_t*
     }
 }
 
+// the branch of the ordering graph: 0 rank (m <= kBruteMovers), 1 radix sort of the
+// movers (m <= cap), 2 full sort
+__global__ void k_order_decide(const int32_t* __restrict__ nmov, int cap, cudaGraphConditionalHandle h,
+                               DevStats* st) {
+    const int m = *nmov;
+    // the mover arrays hold `cap` entries: more movers take the full sort
+    const unsigned branch = m > cap ? 2u : (m <= kBruteMovers ? 0u : 1u);
+    cudaGraphSetConditional(h, branch);
+    st->movers = branch == 2u ? -1ll : (long long)m;
+}
+
+struct OrderGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+#define OG_CK(x)                                 \
+    do {                                         \
+        cudaError_t e_ = (x);                    \
+        if (e_ != cudaSuccess) {                 \
+            cudaGraph_t open_ = nullptr;         \
+            cudaStreamEndCapture(cs, &open_);    \
+            cudaGetLastError();                  \
+            cudaGraphDestroy(g);                 \
+            return e_;                           \
+        }                                        \
+    } while (0)
+
 }  // namespace
 
 size_t partition_temp_bytes(int n) {
@@ -116,33 +157,87 @@ size_t partition_temp_bytes(int n) {
     return bytes;
 }
 
-cudaError_t partition_movers(void* temp, size_t temp_bytes, const uint32_t* keys, const uint32_t* prev,
-                             const int32_t* iota, int32_t* part, int32_t* num_movers, int n, cudaStream_t s) {
-    return cub::DevicePartition::If(temp, temp_bytes, iota, part, num_movers, n, MoverOp{keys, prev}, s);
-}
-
-cudaError_t sort_movers(void* temp, size_t temp_bytes, const uint32_t* keys, const int32_t* part, int m,
-                        uint32_t* mk_tmp, int32_t* mj_tmp, uint32_t* mkeys, int32_t* mslot, int key_bits,
-                        cudaStream_t s) {
-    if (m <= 0) return cudaSuccess;
-    if (m <= kBruteMovers) {
-        const long threads = 32l * m;
-        k_rank_movers<<<(unsigned)((threads + kRankThreads - 1) / kRankThreads), kRankThreads, 0, s>>>(keys, part, m,
-                                                                                                     mkeys, mslot);
-        return cudaGetLastError();
-    }
-    k_gather_movers<<<(m + 255) / 256, 256, 0, s>>>(keys, part, m, mk_tmp, mj_tmp);
-    cudaError_t e = cudaGetLastError();
+// Capture the incremental ordering into a graph: partition (CUB), the branch
+// decision on the device, and a three-way switch (rank + merge | radix sort of
+// the movers + merge | full radix sort).  No host synchronisation per step.
+cudaError_t order_graph_build(void** out, cudaStream_t cs, const OrderBuffers& b) {
+    *out = nullptr;
+    cudaGraph_t g = nullptr, dummy = nullptr;  // dummy receives the graph a capture ended into
+    cudaError_t e = cudaGraphCreate(&g, 0);
     if (e != cudaSuccess) return e;
-    // stable radix sort: ties keep partition (= slot) order
-    return cub::DeviceRadixSort::SortPairs(temp, temp_bytes, mk_tmp, mkeys, mj_tmp, mslot, m, 0, key_bits, s);
+    cudaGraphConditionalHandle h;
+    OG_CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    OG_CK(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    size_t part_bytes = b.part_bytes, sort_bytes = b.sort_bytes;  // CUB takes them by reference
+    OG_CK(cub::DevicePartition::If(b.part_tmp, part_bytes, b.iota, b.part, b.nmov, b.n,
+                                   MoverOp{b.keys, b.keys_sorted}, cs));
+    k_order_decide<<<1, 1, 0, cs>>>(b.nmov, b.cap, h, b.st);
+    OG_CK(cudaGetLastError());
+    cudaStreamCaptureStatus status;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    OG_CK(cudaStreamGetCaptureInfo(cs, &status, nullptr, nullptr, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeSwitch;
+    cp.conditional.size = 3;
+    cudaGraphNode_t cnode;
+    OG_CK(cudaGraphAddNode(&cnode, g, deps, nullptr, ndeps, &cp));
+    OG_CK(cudaStreamEndCapture(cs, &dummy));
+    dummy = nullptr;
+    cudaGraph_t* body = cp.conditional.phGraph_out;
+    const int n = b.n;
+    // case 0: brute-force rank of at most kBruteMovers movers, merge
+    OG_CK(cudaStreamBeginCaptureToGraph(cs, body[0], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    k_rank_movers<<<(unsigned)((32l * kBruteMovers + kRankThreads - 1) / kRankThreads), kRankThreads, 0, cs>>>(
+        b.keys, b.part, b.nmov, b.cap, b.mkeys, b.mslot);
+    k_merge_movers<<<(n + 255) / 256, 256, 0, cs>>>(b.keys, b.part, n, b.cap, b.nmov, b.mkeys, b.mslot,
+                                                     b.keys_sorted, b.perm);
+    OG_CK(cudaGetLastError());
+    OG_CK(cudaStreamEndCapture(cs, &dummy));
+    dummy = nullptr;
+    // case 1: radix sort of the movers in `cap` padded slots (stable: ties keep slot order), merge
+    OG_CK(cudaStreamBeginCaptureToGraph(cs, body[1], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    const uint32_t pad = b.key_bits >= 32 ? 0xFFFFFFFFu : ((1u << b.key_bits) - 1u);
+    k_gather_movers<<<(b.cap + 255) / 256, 256, 0, cs>>>(b.keys, b.part, b.nmov, b.cap, pad, b.mk_tmp, b.mj_tmp);
+    OG_CK(cudaGetLastError());
+    OG_CK(cub::DeviceRadixSort::SortPairs(b.sort_tmp, sort_bytes, b.mk_tmp, b.mkeys, b.mj_tmp, b.mslot, b.cap, 0,
+                                          b.key_bits, cs));
+    k_merge_movers<<<(n + 255) / 256, 256, 0, cs>>>(b.keys, b.part, n, b.cap, b.nmov, b.mkeys, b.mslot,
+                                                     b.keys_sorted, b.perm);
+    OG_CK(cudaGetLastError());
+    OG_CK(cudaStreamEndCapture(cs, &dummy));
+    dummy = nullptr;
+    // case 2: full radix sort
+    OG_CK(cudaStreamBeginCaptureToGraph(cs, body[2], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    sort_bytes = b.sort_bytes;
+    OG_CK(cub::DeviceRadixSort::SortPairs(b.sort_tmp, sort_bytes, b.keys, b.keys_sorted, b.iota, b.perm, n, 0,
+                                          b.key_bits, cs));
+    OG_CK(cudaStreamEndCapture(cs, &dummy));
+    dummy = nullptr;
+    OrderGraph* og = new OrderGraph();
+    og->graph = g;
+    e = cudaGraphInstantiate(&og->exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        delete og;
+        return e;
+    }
+    *out = og;
+    return cudaSuccess;
 }
 
-cudaError_t merge_movers(const uint32_t* keys, const int32_t* part, int n, int m, const uint32_t* mkeys,
-                         const int32_t* mslot, uint32_t* keys_out, int32_t* perm_out, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    k_merge_movers<<<(n + 255) / 256, 256, 0, s>>>(keys, part, n, m, mkeys, mslot, keys_out, perm_out);
-    return cudaGetLastError();
+cudaError_t order_graph_launch(void* og, cudaStream_t s) {
+    return cudaGraphLaunch(static_cast<OrderGraph*>(og)->exec, s);
+}
+
+void order_graph_destroy(void* og) {
+    if (!og) return;
+    OrderGraph* o = static_cast<OrderGraph*>(og);
+    if (o->exec) cudaGraphExecDestroy(o->exec);
+    if (o->graph) cudaGraphDestroy(o->graph);
+    delete o;
 }
 
 }  // namespace aep

@@ -139,6 +139,29 @@ def cloth_drape(nside: int = 256, res: int = 128, seed: int = 2, shear_stiffness
                  f"element volume", mesh)
 
 
+def sand_cloth(nside: int = 512, n_sand: int = 7604222, res: int = 512, seed: int = 4) -> Scene:
+    """Sand and cloth at scale: 7,604,222 sand particles in a cylinder r=0.12, height
+    0.16 on the ground at 0.05 (about 8 per cell at 512^3), under a 512x512-vertex
+    sheet (262,144 vertices, 522,242 triangles) of side 0.6 at height 0.3 that falls
+    onto the pile; sand as in the sand column, cloth as in the drape (in-plane E=1e4,
+    volume-weighted in-plane forces); grid 512^3, dt=2e-5, 500 steps."""
+    rng = np.random.default_rng(seed)
+    r = 0.12 * np.sqrt(rng.random(n_sand))
+    th = 2.0 * np.pi * rng.random(n_sand)
+    z = 0.05 + 0.16 * rng.random(n_sand)
+    x = np.stack([0.5 + r * np.cos(th), 0.5 + r * np.sin(th), z], axis=1)
+    vol_total = np.pi * 0.12 ** 2 * 0.16
+    m = np.full(n_sand, 2200.0 * vol_total / n_sand)
+    ps = _particles(x, np.zeros((n_sand, 3)), m, m / 2200.0, capi.AEP_SAND)
+    V, F = sheet(nside, 0.6, (0.5, 0.5), 0.3, 1e-4, rng)
+    thickness = 1.0 / res
+    mesh = LagrangianMesh.from_triangles(V, F, density=0.2 / thickness, thickness=thickness, youngs_modulus=1e4,
+                                         poisson_ratio=0.3, shear_stiffness=1e3, stiffness=1e3, friction_coeff=0.3)
+    prm = make_params(friction=0.5, cloth_volume_weighting=1)
+    return Scene("sand_cloth", RegularGrid([0, 0, 0], [1, 1, 1], [res] * 3), ps, LevelSet.ground(0.05), prm, 2e-5,
+                 500, f"{n_sand / (vol_total * res ** 3):.1f} sand particles per cell; cloth as in the drape", mesh)
+
+
 # --- the reference's particle factories (ParticleSystem.cpp:119-401), seeded ---------
 # Rejection sampling of the unit ball / disk, the total mass spread evenly, volumes 1
 # (the first P2G of solve recomputes them), F_E = F_P = I.  The C++ facade
@@ -192,4 +215,4 @@ def sand_cylinder(base_center, radius: float, height: float, n: int, seed: int =
     return _particles(x, v, np.full(n, 1300.0 * np.pi * radius ** 2 * height / n), np.ones(n), capi.AEP_SAND)
 
 
-CONFIGS = {0: snow_block, 1: sand_column, 2: cloth_drape, 3: snow_sand_collision}
+CONFIGS = {0: snow_block, 1: sand_column, 2: cloth_drape, 3: snow_sand_collision, 4: sand_cloth}

@@ -9,8 +9,10 @@ pin against central finite differences.
 
 Packed parameters (9928 floats): W1^T [64][16], W2^T [64][64], W3^T [64][64],
 W4^T [8][64], b1 [64], b2 [64], b3 [64], b4 [8].  Records: [ln s0, ln s1, ln s2,
-q, material, d0, d1, d2]; features and targets are scaled per record (sand by
-1/|ln s|, snow by 50), as the kernels do.
+q, material, d0, d1, d2] (material 0 snow, 1 sand); cloth records (material 2)
+carry [r13, r23, r33 - 1, 0, 2, change of (r13, r23, r33)].  Features and targets
+are scaled per record (sand by 1/|ln s|, snow and cloth by 50), as the kernels do
+(aep_mlp.cuh mlp_features).
 """
 from __future__ import annotations
 
@@ -64,6 +66,7 @@ def features(rec, rnd=True):
     X[:, 3] = np.where(mat == 1, rec[:, 3].astype(np.float32), 0.0)
     X[:, 4] = (mat == 0)
     X[:, 5] = (mat == 1)
+    X[:, 6] = (mat == 2)
     return bf16(X) if rnd else X
 
 

@@ -19,7 +19,7 @@ def random_records(n, seed=0):
     ln = np.sort(rng.normal(0, 0.02, (n, 3)), axis=1)[:, ::-1]
     rec[:, 0:3] = ln
     rec[:, 3] = rng.random(n) * 0.5
-    rec[:, 4] = rng.integers(0, 2, n)
+    rec[:, 4] = rng.integers(0, 3, n)  # snow, sand, cloth rows
     rec[:, 5:8] = -0.3 * np.maximum(ln, 0) + 0.01 * rng.normal(size=(n, 3))
     return rec
 
@@ -28,7 +28,7 @@ def random_params(seed=1):
     rng = np.random.default_rng(seed)
     p = np.zeros(NP, np.float32)
     d = mo.unpack(p.astype(np.float64))
-    d["w1t"][:, :6] = rng.normal(0, np.sqrt(2 / 6), (64, 6))
+    d["w1t"][:, :7] = rng.normal(0, np.sqrt(2 / 7), (64, 7))
     d["w2t"][:] = rng.normal(0, np.sqrt(2 / 64), (64, 64))
     d["w3t"][:] = rng.normal(0, np.sqrt(2 / 64), (64, 64))
     d["w4t"][:3] = rng.normal(0, 0.1 * np.sqrt(2 / 64), (3, 64))
@@ -50,7 +50,7 @@ def test_oracle_backward_matches_finite_differences():
     p = random_params(4).astype(np.float64)
     loss, g = mo.loss_and_grad(p, rec, bf=False)
     rng = np.random.default_rng(5)
-    idx = np.concatenate([rng.choice(np.arange(0, 64 * 16).reshape(64, 16)[:, :6].ravel(), 10),
+    idx = np.concatenate([rng.choice(np.arange(0, 64 * 16).reshape(64, 16)[:, :7].ravel(), 10),
                           rng.integers(1024, 9728, 40), rng.integers(9728, 9728 + 195, 10)])
     for i in idx:
         h = 1e-6 * max(1.0, abs(p[i]))
@@ -78,7 +78,7 @@ def test_gpu_gradient_matches_oracle():
     for name, _ in mo.LAYOUT:
         ref = go[name]
         if name == "w1t":
-            ref, got = ref[:, :6], gg[name][:, :6]
+            ref, got = ref[:, :7], gg[name][:, :7]
         elif name in ("w4t", "b4"):
             ref, got = ref[:3], gg[name][:3]
         else:
@@ -174,3 +174,47 @@ def test_learned_step_matches_oracle_and_training_gains():
     gp, op = s_tr.get_particles(), o.get_particles()
     assert np.abs(gp["positions"] - op["positions"]).max() < 2e-6
     assert np.abs(gp["elastic_deformation_gradients"] - op["elastic_deformation_gradients"]).max() < 5e-4
+
+
+@pytest.mark.gpu
+def test_learned_cloth_return_map():
+    """Cloth rows of the network: harvested (trial, projected) QR columns of plastic
+    elements train the map; with it attached the elements' return mapping is
+    predicted and checked, and the mesh stays within the cloth tolerances of the
+    FP64 oracle."""
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP
+    from oracle.oracle import Oracle
+
+    from .test_cloth_gpu import _compare_mesh, pair, small_cloth
+
+    grid, ps, mesh, ls, prm = small_cloth(False, seed=6, E=1e4, weighting=1)
+    gpu, _ = pair(grid, ps, mesh, ls, prm)
+    buf = torch.zeros((200000, 8), dtype=torch.float32, device="cuda")
+    gpu.set_harvest(buf.data_ptr(), len(buf), 1)
+    for _ in range(40):
+        gpu.step(2e-5)
+    nrec = min(gpu.harvest_count(), len(buf))
+    gpu.set_harvest(0, 0, 1)
+    rec = buf[:nrec].contiguous()
+    assert nrec > 500 and torch.all(rec[:, 4] == 2)
+    m = ReturnMapMLP(seed=4)
+    _, loss0 = m.gradient(rec.data_ptr(), nrec)
+    m.train(rec.data_ptr(), nrec, steps=1500, batch=4096, lr=2e-3, lr_final=2e-5)
+    _, loss1 = m.gradient(rec.data_ptr(), nrec)
+    assert loss1 < 0.2 * loss0
+    g2, orc = pair(grid, ps, mesh, ls, prm)
+    g2.set_return_map(m, 1e-3)
+    acc = fb = 0
+    orc.init(volumes=False)
+    for _ in range(10):
+        g2.step(2e-5)
+        orc.step(2e-5)
+        st = g2.stats()
+        acc += st["learned_accepted"]
+        fb += st["learned_fallbacks"]
+    assert acc + fb > 0
+    # an accepted prediction may differ from the exact projection by up to the
+    # tolerance (1e-3) relative to the projected strain, per step; the directions
+    # get the matching bound, the rest keeps the exact-path tolerances
+    _compare_mesh(g2.get_mesh(), orc.get_mesh(), 2e-6, 1e-3, 1e-3, 5e-3)
