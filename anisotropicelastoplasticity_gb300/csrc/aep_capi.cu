@@ -60,17 +60,15 @@ struct aep_solver {
     void* sort_tmp = nullptr;
     size_t sort_bytes = 0;
     int key_bits = 0;
-    // incremental ordering: partition of the slots, sorted movers, mover count
-    int32_t* part = nullptr;
-    uint32_t* mk_tmp = nullptr;
-    int32_t* mj_tmp = nullptr;
+    // incremental ordering (aep_sort.cu): mover list, sorted mover keys, scratch
+    uint32_t* order_mem = nullptr;  // one allocation for the arrays below
+    uint32_t* mk = nullptr;
+    int32_t* mj = nullptr;
     uint32_t* mkeys = nullptr;
     int32_t* mslot = nullptr;
-    int32_t* nmov = nullptr;       // device
-    int32_t* nmov_host = nullptr;  // pinned
-    unsigned long long* nmov_host_check = nullptr;  // pinned, 2 words: upload validation result
-    void* part_tmp = nullptr;
-    size_t part_bytes = 0;
+    int32_t* mpos = nullptr;
+    uint32_t* order_scratch = nullptr;
+    unsigned long long* check_host = nullptr;  // pinned, 2 words: upload validation result
     bool prev_sorted = false;  // keys_sorted holds an ascending array of the current n
     void* order_graph = nullptr;  // the incremental ordering, captured (aep_sort.cu)
     int order_graph_n = -1;
@@ -250,18 +248,15 @@ void free_particles(aep_solver* s) {
     order_graph_destroy(s->order_graph);
     s->order_graph = nullptr;
     s->order_graph_n = -1;
-    cudaFree(s->part);
-    cudaFree(s->part_tmp);
+    cudaFree(s->order_mem);
     cudaFree(s->inv);
     s->inv = nullptr;
     s->keys = s->keys_sorted = nullptr;
     s->iota = s->perm = nullptr;
     s->sort_tmp = nullptr;
     s->staging = nullptr;
-    s->part = nullptr;  // the mover arrays live in the same allocation
-    s->mk_tmp = s->mkeys = nullptr;
-    s->mj_tmp = s->mslot = nullptr;
-    s->part_tmp = nullptr;
+    s->order_mem = s->mk = s->mkeys = s->order_scratch = nullptr;
+    s->mj = s->mslot = s->mpos = nullptr;
     s->prev_sorted = false;
     s->cap = 0;
 }
@@ -298,20 +293,17 @@ aep_status ensure_capacity(aep_solver* s, int64_t n, int64_t keep = 0) {
     CK(cudaMalloc(&s->inv, sizeof(int32_t) * (size_t)n));
     s->sort_bytes = sort_temp_bytes((int)n, s->key_bits);
     CK(cudaMalloc(&s->sort_tmp, s->sort_bytes));
-    // partition (n) + four mover arrays (n / 4 + 1 each: larger counts take the full sort)
+    // mover list and sorted mover keys (n / 4 + 1 each: more movers take the full sort)
+    // and the ordering scratch
     const size_t mcap = (size_t)n / 4 + 1;
-    CK(cudaMalloc(&s->part, sizeof(int32_t) * ((size_t)n + 4 * mcap)));
-    s->mk_tmp = reinterpret_cast<uint32_t*>(s->part + n);
-    s->mj_tmp = s->part + n + mcap;
-    s->mkeys = reinterpret_cast<uint32_t*>(s->part + n + 2 * mcap);
-    s->mslot = s->part + n + 3 * mcap;
-    s->part_bytes = partition_temp_bytes((int)n);
-    CK(cudaMalloc(&s->part_tmp, s->part_bytes));
-    if (!s->nmov) {
-        CK(cudaMalloc(&s->nmov, sizeof(int32_t)));
-        CK(cudaMallocHost(&s->nmov_host, sizeof(int32_t)));
-        CK(cudaMallocHost(&s->nmov_host_check, 2 * sizeof(unsigned long long)));
-    }
+    CK(cudaMalloc(&s->order_mem, sizeof(uint32_t) * (5 * mcap + order_scratch_words((int)n))));
+    s->mk = s->order_mem;
+    s->mj = reinterpret_cast<int32_t*>(s->order_mem + mcap);
+    s->mkeys = s->order_mem + 2 * mcap;
+    s->mslot = reinterpret_cast<int32_t*>(s->order_mem + 3 * mcap);
+    s->mpos = reinterpret_cast<int32_t*>(s->order_mem + 4 * mcap);
+    s->order_scratch = s->order_mem + 5 * mcap;
+    if (!s->check_host) CK(cudaMallocHost(&s->check_host, 2 * sizeof(unsigned long long)));
     s->prev_sorted = false;
     s->staging_bytes = sizeof(double) * 36 * (size_t)n;  // every field of one particle set at once
     CK(cudaMalloc(&s->staging, s->staging_bytes));
@@ -430,9 +422,8 @@ cudaError_t order_particles(aep_solver* s) {
                 cudaError_t e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking);
                 if (e != cudaSuccess) return e;
             }
-            OrderBuffers b{s->keys, s->keys_sorted, s->perm, s->iota, s->part, s->nmov, s->mk_tmp, s->mj_tmp,
-                           s->mkeys, s->mslot, s->part_tmp, s->part_bytes, s->sort_tmp, s->sort_bytes, n, n / 4,
-                           s->key_bits, s->dstats};
+            OrderBuffers b{s->keys, s->keys_sorted, s->perm, s->iota, s->mk, s->mj, s->mkeys, s->mslot, s->mpos,
+                           s->order_scratch, s->sort_tmp, s->sort_bytes, n, n / 4, s->key_bits, s->dstats};
             cudaError_t e = order_graph_build(&s->order_graph, s->capture_stream, b);
             if (e != cudaSuccess) return e;
             s->order_graph_n = n;
@@ -568,9 +559,7 @@ aep_status aep_solver_destroy(aep_solver* s) {
     cudaFree(s->dforce);
     cudaFree(s->harvest_count);
     cudaFree(s->check);
-    cudaFree(s->nmov);
-    cudaFreeHost(s->nmov_host);
-    cudaFreeHost(s->nmov_host_check);
+    cudaFreeHost(s->check_host);
     cudaFree(s->solve);
     cudaFreeHost(s->solve_host);
     cudaFreeHost(s->stats_host);
@@ -658,7 +647,7 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
         launch_snow_jp((int)n, P, dFp, s->stream, map);
         CKLAUNCH();
     }
-    unsigned long long* chk = reinterpret_cast<unsigned long long*>(s->nmov_host_check);
+    unsigned long long* chk = s->check_host;
     CK(cudaMemcpyAsync(chk, s->check, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     double mm = 0.0;

@@ -41,29 +41,27 @@ void launch_grid_dense(const KParams& P, const GArrays& G, double* mass, double*
 // device view of a trained MLP (aep_mlp.cu)
 MlpParams mlp_device_params(const aep_mlp* m);
 
-// incremental ordering (aep_sort.cu): partition of the slots into movers and
-// stayers, sort of the movers, merge; captured as a CUDA graph whose branch
-// (brute-force rank, radix sort of the movers, full sort) is chosen on the device
-constexpr int kBruteMovers = 8192;  // movers ranked by brute force up to this count
+// incremental ordering (aep_sort.cu): movers flagged and listed, placed by their
+// (key, slot) rank, stayers placed from block offsets; captured as a CUDA graph
+// whose if/else node runs the full sort when the movers are too many
+constexpr int kBruteMovers = 8192;  // movers placed by brute-force rank up to this count
 struct OrderBuffers {
     const uint32_t* keys;  // new keys in the current order
     uint32_t* keys_sorted; // in: the last sorted keys (ascending); out: this ordering's keys
     int32_t* perm;         // out: current slot of each sorted position
     const int32_t* iota;
-    int32_t* part;         // partition: movers first (slot order), stayers last (reversed)
-    int32_t* nmov;         // device mover count
-    uint32_t* mk_tmp;      // cap padded mover keys / slots, and the sorted ones
-    int32_t* mj_tmp;
-    uint32_t* mkeys;
+    uint32_t* mk;          // mover list: keys and slots (cap entries)
+    int32_t* mj;
+    uint32_t* mkeys;       // movers sorted by (key, slot): keys, slots, final positions
     int32_t* mslot;
-    void* part_tmp;
-    size_t part_bytes;
+    int32_t* mpos;
+    uint32_t* scratch;     // order_scratch_words(n) words
     void* sort_tmp;
     size_t sort_bytes;
     int n, cap, key_bits;
     DevStats* st;
 };
-size_t partition_temp_bytes(int n);
+size_t order_scratch_words(int n);
 cudaError_t order_graph_build(void** out, cudaStream_t capture_stream, const OrderBuffers& b);
 cudaError_t order_graph_launch(void* graph, cudaStream_t s);
 void order_graph_destroy(void* graph);

@@ -5,16 +5,28 @@
 // the permutation is close to the identity from step to step and the permuted
 // reads of the particle arrays stay nearly coalesced.
 //
-// Incremental sort: from one step to the next only the particles that crossed a
-// cell boundary change key (about 1% at the workloads' time steps).  With `prev`
-// any ascending key array of the same length (the last sorted keys), the slots
-// whose new key equals prev[j] form an ascending subsequence.  So: partition the
-// slots into movers (key != prev) and stayers, keeping slot order (CUB
-// DevicePartition); sort the few movers by (key, slot) (a brute-force rank for
-// small counts, the radix sort otherwise); merge the two ascending lists, stayers
-// before movers on equal keys.  The result is an ascending key order; it is a
-// deterministic function of the keys, so steps repeat bit for bit.
-#include <cub/device/device_partition.cuh>
+// Incremental ordering: from one step to the next only the particles that
+// crossed a cell boundary change key (well under 1% at the workloads' time
+// steps).  With `prev` any ascending key array of the same length (the last
+// sorted keys), the slots whose new key equals prev[j] ("stayers") form an
+// ascending subsequence; the others are "movers".  The result is the merge of
+// the stayers (slot order) with the movers sorted by (key, slot), stayers first
+// on equal keys:
+//   position of stayer j  = (stayers before slot j) + (movers with key < key_j)
+//   position of mover r   = (movers before it by (key, slot))
+//                           + (stayers with key <= its key)
+// where "stayers with key <= k" = upper_bound(prev, k) - (movers whose prev key
+// is <= k), since a stayer's key is its prev key.  Kernels:
+//   k_flag_movers   mover bitmask, per-block mover counts and the mover list
+//                   (appended in any order: placement depends only on (key,
+//                   slot)); the last block to finish scans the block counts,
+//                   places up to kSmallMovers movers itself and picks the branch
+//   k_place_movers  the same placement for up to kBruteMovers movers, one warp each
+//   k_place_stayers each stayer's position from the block offsets and bitmask,
+//                   and the movers' entries
+// captured in a CUDA graph whose switch node runs (stayers | movers + stayers |
+// full sort).  The ordering is a deterministic function of the keys, so steps
+// repeat bit for bit, and no host synchronisation is needed.
 #include <cub/device/device_radix_sort.cuh>
 
 #include "aep_kernels.h"
@@ -35,100 +47,181 @@ cudaError_t sort_pairs(void* temp, size_t temp_bytes, const uint32_t* keys_in, u
 
 namespace {
 
-struct MoverOp {
-    const uint32_t* keys;
-    const uint32_t* prev;
-    __device__ __forceinline__ bool operator()(const int32_t& j) const { return keys[j] != prev[j]; }
-};
-
+constexpr int kFlagThreads = 1024;  // slots per block of the flag and stayer kernels
 constexpr int kRankThreads = 256;
+constexpr int kSmallMovers = 512;   // movers placed by the last flag block
 
-// rank of mover i among all movers by (key, partition index), one warp per mover;
-// partition order is slot order, so ties keep slot order.  m is read on the device.
-__global__ void __launch_bounds__(kRankThreads) k_rank_movers(const uint32_t* __restrict__ keys,
-                                                              const int32_t* __restrict__ part,
-                                                              const int32_t* __restrict__ nmov, int cap,
-                                                              uint32_t* __restrict__ mkeys, int32_t* __restrict__ mslot) {
-    const int m = *nmov;
-    if (m > cap) return;  // not this branch (the decision kernel never sends it here)
-    const int i = (int)(((long)blockIdx.x * kRankThreads + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (i >= m) return;
-    const int ji = part[i];
-    const uint32_t ki = keys[ji];
-    int rank = 0;
+// first index i of the ascending a[0, n) with a[i] > k, found by one warp with
+// 32-way probes (about four dependent loads for a million entries)
+__device__ __forceinline__ int warp_upper_bound(const uint32_t* __restrict__ a, int n, uint32_t k, int lane) {
+    int lo = 0, hi = n;  // a[lo - 1] <= k (or lo = 0); the answer is in [lo, hi]
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) >> 5;
+        const int idx = lo + lane * step;
+        const unsigned above = __ballot_sync(0xffffffffu, idx >= hi || a[idx] > k);
+        if (above == 0u) {
+            lo += 31 * step + 1;
+        } else {
+            const int f = __ffs(above) - 1;
+            if (f == 0) return lo;
+            hi = min(hi, lo + f * step);
+            lo += (f - 1) * step + 1;
+        }
+    }
+    const int idx = lo + lane;
+    return lo + __popc(__ballot_sync(0xffffffffu, idx < hi && a[idx] <= k));
+}
+
+// placement of mover i (one warp): its (key, slot) rank among the m movers and
+// the number of stayers with a key <= its key
+__device__ __forceinline__ void place_mover(int i, int m, const uint32_t* __restrict__ prev, int n,
+                                            const uint32_t* __restrict__ mk, const int32_t* __restrict__ mj,
+                                            uint32_t* __restrict__ mkeys, int32_t* __restrict__ mslot,
+                                            int32_t* __restrict__ mpos, int lane) {
+    // the list was written by other blocks of the flag kernel: read it from L2
+    const uint32_t ki = __ldcg(&mk[i]);
+    const int ji = __ldcg(&mj[i]);
+    int rank = 0, prev_le = 0;
     for (int k = lane; k < m; k += 32) {
-        const uint32_t kk = keys[part[k]];
-        rank += (kk < ki) | ((kk == ki) & (k < i));
+        const uint32_t kk = __ldcg(&mk[k]);
+        const int jk = __ldcg(&mj[k]);
+        rank += (kk < ki) | ((kk == ki) & (jk < ji));
+        prev_le += prev[jk] <= ki;
     }
     rank = __reduce_add_sync(0xffffffffu, rank);
+    prev_le = __reduce_add_sync(0xffffffffu, prev_le);
+    const int ub = warp_upper_bound(prev, n, ki, lane);
     if (lane == 0) {
         mkeys[rank] = ki;
         mslot[rank] = ji;
+        mpos[rank] = rank + ub - prev_le;
     }
 }
 
-// movers into `cap` sort slots; slots past m get the largest key of the sorted
-// bits (`pad`) and, coming last, stay after any mover with that key (stable sort)
-__global__ void k_gather_movers(const uint32_t* __restrict__ keys, const int32_t* __restrict__ part,
-                                const int32_t* __restrict__ nmov, int cap, uint32_t pad, uint32_t* __restrict__ mk,
-                                int32_t* __restrict__ mj) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= cap) return;
-    if (r < *nmov) {
-        const int j = part[r];
-        mk[r] = keys[j];
-        mj[r] = j;
-    } else {
-        mk[r] = pad;
-        mj[r] = -1;
-    }
-}
-
-// merge of the stayers (partition tail, reversed: stayer q is part[n-1-q]) and the
-// sorted movers; stayers go before movers with an equal key
-__global__ void k_merge_movers(const uint32_t* __restrict__ keys, const int32_t* __restrict__ part, int n, int cap,
-                               const int32_t* __restrict__ nmov, const uint32_t* __restrict__ mkeys,
-                               const int32_t* __restrict__ mslot, uint32_t* __restrict__ keys_out,
-                               int32_t* __restrict__ perm_out) {
-    const int m = *nmov;
-    if (m > cap || m > n) return;  // not this branch
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ns = n - m;
-    if (t < ns) {
-        const int j = part[n - 1 - t];
+// counters: [0] movers, [1] finished flag blocks
+__global__ void __launch_bounds__(kFlagThreads) k_flag_movers(const uint32_t* __restrict__ keys,
+                                                              const uint32_t* __restrict__ prev, int n, int cap,
+                                                              uint32_t* __restrict__ mask, int32_t* __restrict__ blk,
+                                                              uint32_t* __restrict__ mk, int32_t* __restrict__ mj,
+                                                              uint32_t* __restrict__ mkeys, int32_t* __restrict__ mslot,
+                                                              int32_t* __restrict__ mpos,
+                                                              int32_t* __restrict__ counters,
+                                                              cudaGraphConditionalHandle h, DevStats* st) {
+    __shared__ bool last;
+    __shared__ int warp_sum[kFlagThreads / 32];
+    const int j = blockIdx.x * kFlagThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool mover = false;
+    if (j < n) {
         const uint32_t k = keys[j];
-        int lo = 0, hi = m;  // movers with key < k
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (mkeys[mid] < k) lo = mid + 1;
-            else hi = mid;
+        mover = k != prev[j];
+        if (mover) {
+            const int idx = atomicAdd(&counters[0], 1);
+            if (idx < cap) {
+                mk[idx] = k;
+                mj[idx] = j;
+            }
         }
-        keys_out[t + lo] = k;
-        perm_out[t + lo] = j;
-    } else if (t < n) {
-        const int r = t - ns;
-        const uint32_t k = mkeys[r];
-        int lo = 0, hi = ns;  // stayers with key <= k
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (keys[part[n - 1 - mid]] <= k) lo = mid + 1;
-            else hi = mid;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, mover);
+    if (lane == 0 && j < n) mask[j >> 5] = bal;
+    const int cnt = __syncthreads_count(mover);
+    if (threadIdx.x == 0) {
+        blk[blockIdx.x] = cnt;
+        __threadfence();
+        last = atomicAdd(&counters[1], 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    // last block: exclusive scan of the block counts in place
+    __threadfence();
+    const int nb = gridDim.x;
+    int carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += kFlagThreads) {
+        const int b = b0 + threadIdx.x;
+        const int v = b < nb ? __ldcg(&blk[b]) : 0;  // written by other blocks: read from L2
+        int x = v;  // inclusive warp scan
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        keys_out[r + lo] = k;
-        perm_out[r + lo] = mslot[r];
+        if (lane == 31) warp_sum[threadIdx.x >> 5] = x;
+        __syncthreads();
+        int woff = 0;
+        for (int w = 0; w < (int)(threadIdx.x >> 5); ++w) woff += warp_sum[w];
+        int total = 0;
+        for (int w = 0; w < kFlagThreads / 32; ++w) total += warp_sum[w];
+        if (b < nb) blk[b] = carry + woff + x - v;  // this thread alone read blk[b] (as v)
+        carry += total;
+        __syncthreads();
+    }
+    const int m = carry;  // the movers
+    const unsigned branch = (m > cap || m > kBruteMovers) ? 2u : (m > kSmallMovers ? 1u : 0u);
+    if (branch == 0u) {  // place the few movers here; all flag blocks are done with prev
+        __threadfence();
+        for (int i = threadIdx.x >> 5; i < m; i += kFlagThreads / 32)
+            place_mover(i, m, prev, n, mk, mj, mkeys, mslot, mpos, lane);
+    }
+    if (threadIdx.x == 0) {
+        cudaGraphSetConditional(h, branch);
+        st->movers = branch == 2u ? -1ll : (long long)m;
+        counters[0] = m;
+        counters[1] = 0;
     }
 }
 
-// the branch of the ordering graph: 0 rank (m <= kBruteMovers), 1 radix sort of the
-// movers (m <= cap), 2 full sort
-__global__ void k_order_decide(const int32_t* __restrict__ nmov, int cap, cudaGraphConditionalHandle h,
-                               DevStats* st) {
-    const int m = *nmov;
-    // the mover arrays hold `cap` entries: more movers take the full sort
-    const unsigned branch = m > cap ? 2u : (m <= kBruteMovers ? 0u : 1u);
-    cudaGraphSetConditional(h, branch);
-    st->movers = branch == 2u ? -1ll : (long long)m;
+// placement of up to kBruteMovers movers, one warp each
+__global__ void __launch_bounds__(kRankThreads) k_place_movers(const uint32_t* __restrict__ prev, int n, int cap,
+                                                               const uint32_t* __restrict__ mk,
+                                                               const int32_t* __restrict__ mj,
+                                                               const int32_t* __restrict__ counters,
+                                                               uint32_t* __restrict__ mkeys, int32_t* __restrict__ mslot,
+                                                               int32_t* __restrict__ mpos) {
+    const int m = counters[0];
+    if (m > cap || m > kBruteMovers) return;  // the full-sort branch (never launched with these)
+    const int i = (int)(((long)blockIdx.x * kRankThreads + threadIdx.x) >> 5);
+    if (i >= m) return;
+    place_mover(i, m, prev, n, mk, mj, mkeys, mslot, mpos, threadIdx.x & 31);
+}
+
+// stayer j: (stayers before j) + (movers with key < key_j); threads t < m also
+// write the movers' entries
+__global__ void __launch_bounds__(kFlagThreads) k_place_stayers(const uint32_t* __restrict__ keys, int n, int cap,
+                                                                const uint32_t* __restrict__ mask,
+                                                                const int32_t* __restrict__ blk,
+                                                                const uint32_t* __restrict__ mkeys,
+                                                                const int32_t* __restrict__ mslot,
+                                                                const int32_t* __restrict__ mpos,
+                                                                const int32_t* __restrict__ counters,
+                                                                uint32_t* __restrict__ keys_out,
+                                                                int32_t* __restrict__ perm_out) {
+    __shared__ int warp_movers[kFlagThreads / 32];
+    const int j = blockIdx.x * kFlagThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m = counters[0];
+    if (m > cap || m > kBruteMovers) return;  // the full-sort branch (never launched with these); block-uniform
+    const unsigned bal = j - lane < n ? mask[j >> 5] : 0u;
+    if (lane == 0) warp_movers[warp] = __popc(bal);
+    __syncthreads();
+    if (j < m) {
+        const int p = mpos[j];
+        keys_out[p] = mkeys[j];
+        perm_out[p] = mslot[j];
+    }
+    if (j >= n || ((bal >> lane) & 1u)) return;
+    int before = blk[blockIdx.x] + __popc(bal & ((1u << lane) - 1u));
+    for (int w = 0; w < warp; ++w) before += warp_movers[w];
+    const uint32_t k = keys[j];
+    int lo = 0, hi = m;  // movers with key < k
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (mkeys[mid] < k) lo = mid + 1;
+        else hi = mid;
+    }
+    const int pos = j - before + lo;
+    keys_out[pos] = k;
+    perm_out[pos] = j;
 }
 
 struct OrderGraph {
@@ -150,28 +243,31 @@ struct OrderGraph {
 
 }  // namespace
 
-size_t partition_temp_bytes(int n) {
-    size_t bytes = 0;
-    cub::DevicePartition::If(nullptr, bytes, (const int32_t*)nullptr, (int32_t*)nullptr, (int32_t*)nullptr, n,
-                             MoverOp{nullptr, nullptr});
-    return bytes;
+size_t order_scratch_words(int n) {
+    const size_t nb = ((size_t)n + kFlagThreads - 1) / kFlagThreads;
+    // mask (n/32 + 1), block offsets (nb), counters (2)
+    return (size_t)n / 32 + 1 + nb + 2;
 }
 
-// Capture the incremental ordering into a graph: partition (CUB), the branch
-// decision on the device, and a three-way switch (rank + merge | radix sort of
-// the movers + merge | full radix sort).  No host synchronisation per step.
 cudaError_t order_graph_build(void** out, cudaStream_t cs, const OrderBuffers& b) {
     *out = nullptr;
-    cudaGraph_t g = nullptr, dummy = nullptr;  // dummy receives the graph a capture ended into
+    cudaGraph_t g = nullptr, ended = nullptr;
     cudaError_t e = cudaGraphCreate(&g, 0);
     if (e != cudaSuccess) return e;
+    const int n = b.n;
+    const int nb = (n + kFlagThreads - 1) / kFlagThreads;
+    uint32_t* mask = b.scratch;
+    int32_t* blk = reinterpret_cast<int32_t*>(mask + n / 32 + 1);
+    int32_t* counters = blk + nb;
+    // counters[1] is reset by the last flag block; zero both once here
+    OG_CK(cudaMemsetAsync(counters, 0, 2 * sizeof(int32_t), cs));
+    OG_CK(cudaStreamSynchronize(cs));
     cudaGraphConditionalHandle h;
     OG_CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
     OG_CK(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    size_t part_bytes = b.part_bytes, sort_bytes = b.sort_bytes;  // CUB takes them by reference
-    OG_CK(cub::DevicePartition::If(b.part_tmp, part_bytes, b.iota, b.part, b.nmov, b.n,
-                                   MoverOp{b.keys, b.keys_sorted}, cs));
-    k_order_decide<<<1, 1, 0, cs>>>(b.nmov, b.cap, h, b.st);
+    OG_CK(cudaMemsetAsync(counters, 0, sizeof(int32_t), cs));
+    k_flag_movers<<<nb, kFlagThreads, 0, cs>>>(b.keys, b.keys_sorted, n, b.cap, mask, blk, b.mk, b.mj, b.mkeys,
+                                               b.mslot, b.mpos, counters, h, b.st);
     OG_CK(cudaGetLastError());
     cudaStreamCaptureStatus status;
     const cudaGraphNode_t* deps = nullptr;
@@ -181,41 +277,26 @@ cudaError_t order_graph_build(void** out, cudaStream_t cs, const OrderBuffers& b
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
     cp.conditional.type = cudaGraphCondTypeSwitch;
-    cp.conditional.size = 3;
+    cp.conditional.size = 3;  // 0: stayers, 1: movers + stayers, 2: full sort
     cudaGraphNode_t cnode;
     OG_CK(cudaGraphAddNode(&cnode, g, deps, nullptr, ndeps, &cp));
-    OG_CK(cudaStreamEndCapture(cs, &dummy));
-    dummy = nullptr;
+    OG_CK(cudaStreamEndCapture(cs, &ended));
     cudaGraph_t* body = cp.conditional.phGraph_out;
-    const int n = b.n;
-    // case 0: brute-force rank of at most kBruteMovers movers, merge
-    OG_CK(cudaStreamBeginCaptureToGraph(cs, body[0], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    k_rank_movers<<<(unsigned)((32l * kBruteMovers + kRankThreads - 1) / kRankThreads), kRankThreads, 0, cs>>>(
-        b.keys, b.part, b.nmov, b.cap, b.mkeys, b.mslot);
-    k_merge_movers<<<(n + 255) / 256, 256, 0, cs>>>(b.keys, b.part, n, b.cap, b.nmov, b.mkeys, b.mslot,
+    for (int c = 0; c < 2; ++c) {
+        OG_CK(cudaStreamBeginCaptureToGraph(cs, body[c], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        if (c == 1)
+            k_place_movers<<<(unsigned)((32l * kBruteMovers + kRankThreads - 1) / kRankThreads), kRankThreads, 0,
+                             cs>>>(b.keys_sorted, n, b.cap, b.mk, b.mj, counters, b.mkeys, b.mslot, b.mpos);
+        k_place_stayers<<<nb, kFlagThreads, 0, cs>>>(b.keys, n, b.cap, mask, blk, b.mkeys, b.mslot, b.mpos, counters,
                                                      b.keys_sorted, b.perm);
-    OG_CK(cudaGetLastError());
-    OG_CK(cudaStreamEndCapture(cs, &dummy));
-    dummy = nullptr;
-    // case 1: radix sort of the movers in `cap` padded slots (stable: ties keep slot order), merge
-    OG_CK(cudaStreamBeginCaptureToGraph(cs, body[1], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    const uint32_t pad = b.key_bits >= 32 ? 0xFFFFFFFFu : ((1u << b.key_bits) - 1u);
-    k_gather_movers<<<(b.cap + 255) / 256, 256, 0, cs>>>(b.keys, b.part, b.nmov, b.cap, pad, b.mk_tmp, b.mj_tmp);
-    OG_CK(cudaGetLastError());
-    OG_CK(cub::DeviceRadixSort::SortPairs(b.sort_tmp, sort_bytes, b.mk_tmp, b.mkeys, b.mj_tmp, b.mslot, b.cap, 0,
-                                          b.key_bits, cs));
-    k_merge_movers<<<(n + 255) / 256, 256, 0, cs>>>(b.keys, b.part, n, b.cap, b.nmov, b.mkeys, b.mslot,
-                                                     b.keys_sorted, b.perm);
-    OG_CK(cudaGetLastError());
-    OG_CK(cudaStreamEndCapture(cs, &dummy));
-    dummy = nullptr;
-    // case 2: full radix sort
+        OG_CK(cudaGetLastError());
+        OG_CK(cudaStreamEndCapture(cs, &ended));
+    }
+    size_t sort_bytes = b.sort_bytes;  // CUB takes it by reference
     OG_CK(cudaStreamBeginCaptureToGraph(cs, body[2], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    sort_bytes = b.sort_bytes;
     OG_CK(cub::DeviceRadixSort::SortPairs(b.sort_tmp, sort_bytes, b.keys, b.keys_sorted, b.iota, b.perm, n, 0,
                                           b.key_bits, cs));
-    OG_CK(cudaStreamEndCapture(cs, &dummy));
-    dummy = nullptr;
+    OG_CK(cudaStreamEndCapture(cs, &ended));
     OrderGraph* og = new OrderGraph();
     og->graph = g;
     e = cudaGraphInstantiate(&og->exec, g, 0);
