@@ -56,7 +56,8 @@ struct aep_solver {
     uint32_t* keys_sorted = nullptr;
     int32_t* iota = nullptr;
     int32_t* perm = nullptr;
-    int32_t* inv = nullptr;  // id -> slot of the current order (readback)
+    int32_t* inv = nullptr;  // id -> slot of the current order (readback); during a step, the
+                             // force pass's list of particles redone in FP64
     void* sort_tmp = nullptr;
     size_t sort_bytes = 0;
     int key_bits = 0;
@@ -305,7 +306,7 @@ aep_status ensure_capacity(aep_solver* s, int64_t n, int64_t keep = 0) {
     s->order_scratch = s->order_mem + 5 * mcap;
     if (!s->check_host) CK(cudaMallocHost(&s->check_host, 2 * sizeof(unsigned long long)));
     s->prev_sorted = false;
-    s->staging_bytes = sizeof(double) * 36 * (size_t)n;  // every field of one particle set at once
+    s->staging_bytes = sizeof(double) * 37 * (size_t)n;  // every field of one particle set at once
     CK(cudaMalloc(&s->staging, s->staging_bytes));
     if (!s->check) CK(cudaMalloc(&s->check, 2 * sizeof(unsigned long long)));
     std::vector<int32_t> io((size_t)n);
@@ -601,52 +602,29 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     s->n = s->np = n;
     PArrays& P = s->P[s->cur];
     // Arrays in page-locked host or device memory are read by the conversion
-    // kernels directly; pageable ones are staged (doubles): x 0, v 3n, B 6n (F_P
-    // reuses it after B's conversion), Fe 15n, m 27n, vol 28n, plastic 29n,
-    // material bytes at 35n.
+    // kernel directly; pageable ones are staged first (doubles): x 0, v 3n, B 6n,
+    // Fe 15n, Fp 24n, m 33n, vol 34n, plastic 35n, material bytes at 36n.
     const size_t N = (size_t)n;
     cudaError_t e = cudaSuccess;
-    const double* dm = static_cast<const double*>(device_source(s, m, sizeof(double) * N, 27 * N, &e));
+    auto dsrc = [&](const void* p, size_t bytes, size_t off) -> const void* {
+        if (!p || e != cudaSuccess) return nullptr;
+        return device_source(s, p, bytes, off, &e);
+    };
+    UploadSrc src{static_cast<const double*>(dsrc(x, sizeof(double) * 3 * N, 0)),
+                  static_cast<const double*>(dsrc(v, sizeof(double) * 3 * N, 3 * N)),
+                  static_cast<const double*>(dsrc(B, sizeof(double) * 9 * N, 6 * N)),
+                  static_cast<const double*>(dsrc(Fe, sizeof(double) * 9 * N, 15 * N)),
+                  static_cast<const double*>(dsrc(Fp, sizeof(double) * 9 * N, 24 * N)),
+                  static_cast<const double*>(dsrc(m, sizeof(double) * N, 33 * N)),
+                  static_cast<const double*>(dsrc(vol, sizeof(double) * N, 34 * N)),
+                  static_cast<const double*>(dsrc(plastic, sizeof(double) * N, 35 * N)),
+                  static_cast<const uint8_t*>(dsrc(material, N, 36 * N))};
     CK(e);
-    const uint8_t* dmat =
-        material ? static_cast<const uint8_t*>(device_source(s, material, N, 35 * N, &e)) : nullptr;
-    CK(e);
-    // validation on the device (largest mass, bad masses, unknown tags), read back
-    // with the final synchronisation
+    // the whole upload and its validation (bad masses, unknown tags, largest mass)
+    // in one launch, read back with the final synchronisation
     CK(cudaMemsetAsync(s->check, 0, 2 * sizeof(unsigned long long), s->stream));
-    launch_check_upload((int)n, dm, dmat, s->check, s->stream);
+    launch_upload_particles((int)n, src, P, map, s->prm.track_plastic_F, s->check, s->stream);
     CKLAUNCH();
-    aep_status st = upload(s, x, 3, 0, P.x, -1, 0, map, 0);
-    if (st) return st;
-    if (v) { st = upload(s, v, 3, 0, P.v, -1, 0, map, 3 * N); if (st) return st; }
-    else for (int a = 0; a < 3; ++a) CK(cudaMemsetAsync(P.v[a], 0, sizeof(float) * n, s->stream));
-    if (B) { st = upload(s, B, 9, 1, P.B, -1, 0, map, 6 * N); if (st) return st; }
-    else for (int a = 0; a < 9; ++a) CK(cudaMemsetAsync(P.B[a], 0, sizeof(float) * n, s->stream));
-    st = upload(s, Fe, 9, 2, P.F, -1, 0, map, 15 * N);
-    if (st) return st;
-    st = upload(s, dm, 1, 3, &P.m, -1, 0, map, 27 * N);
-    if (st) return st;
-    if (vol) { st = upload(s, vol, 1, 3, &P.vol, -1, 0, map, 28 * N); if (st) return st; }
-    else CK(cudaMemsetAsync(P.vol, 0, sizeof(float) * n, s->stream));
-    if (plastic) { st = upload(s, plastic, 1, 3, &P.plastic, -1, 0, map, 29 * N); if (st) return st; }
-    else CK(cudaMemsetAsync(P.plastic, 0, sizeof(float) * n, s->stream));
-    // material tags and ids
-    launch_init_particles((int)n, P, dmat, Fp != nullptr, s->prm.track_plastic_F, s->stream, 0, -1, map);
-    CKLAUNCH();
-    // F_P: full copy with track_plastic_F; snow particles get J_P = det F_P
-    const double* dFp = nullptr;
-    if (Fp) {
-        dFp = static_cast<const double*>(device_source(s, Fp, sizeof(double) * 9 * N, 6 * N, &e));
-        CK(e);
-        if (s->prm.track_plastic_F) {
-            st = upload(s, dFp, 9, 2, P.Fp, -1, 0, map, 6 * N);
-            if (st) return st;
-        }
-    }
-    if (!s->prm.track_plastic_F && (Fp || !plastic)) {  // else J_P of snow comes from `plastic`
-        launch_snow_jp((int)n, P, dFp, s->stream, map);
-        CKLAUNCH();
-    }
     unsigned long long* chk = s->check_host;
     CK(cudaMemcpyAsync(chk, s->check, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -888,7 +866,7 @@ aep_status step_impl(aep_solver* s, double dt_force, double dt, int32_t stage, b
     const float dtf = (float)dt_force;
     const PArrays& P = s->P[s->cur];
     const MeshArrays M = mesh_arrays(s);
-    launch_force(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, dtf, s->dstats, M, s->stream);
+    launch_force(s->kp, P, s->keys_sorted, s->perm, (int)s->n, s->G, dtf, s->dstats, M, s->stream, s->inv);
     CKLAUNCH();
     if (timed) mark(s, AEP_PHASE_GRID);
     if (stage == AEP_STAGE_FORCES) {
@@ -1244,13 +1222,23 @@ aep_status aep_get_particles(aep_solver* s, int64_t n, double* x, double* v, dou
     const int64_t np = s->np;
     const size_t N = (size_t)np;
     if ((st = prepare_download(s))) return st;
-    if (x && (st = download(s, x, 3, 0, P.x, 0, np, 0, false))) return st;
-    if (v && (st = download(s, v, 3, 0, P.v, 0, np, 3 * N, false))) return st;
-    if (B && (st = download(s, B, 9, 1, P.B, 0, np, 6 * N, false))) return st;
-    if (Fe && (st = download(s, Fe, 9, 2, P.F, 0, np, 15 * N, false))) return st;
-    if (Fp && (st = download(s, Fp, 9, 2, P.Fp, 0, np, 24 * N, false))) return st;
-    if (vol && (st = download(s, vol, 1, 3, &P.vol, 0, np, 33 * N, false))) return st;
-    if (plastic && (st = download(s, plastic, 1, 3, &P.plastic, 0, np, 34 * N, false))) return st;
+    // one conversion launch for all requested fields: straight into page-locked or
+    // device destinations, through staging (doubles: x 0, v 3N, B 6N, Fe 15N,
+    // Fp 24N, vol 33N, plastic 34N) and one copy each for pageable ones
+    double* const req[7] = {x, v, B, Fe, Fp, vol, plastic};
+    const size_t cnt[7] = {3, 3, 9, 9, 9, 1, 1}, off[7] = {0, 3, 6, 15, 24, 33, 34};
+    double* dev[7] = {};
+    for (int f = 0; f < 7; ++f)
+        if (req[f]) {
+            double* a = static_cast<double*>(const_cast<void*>(device_alias(req[f])));
+            dev[f] = a ? a : s->staging + off[f] * N;
+        }
+    DownloadDst dst{dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], dev[6]};
+    launch_download_particles((int)np, dst, P, s->inv, s->stream);
+    CKLAUNCH();
+    for (int f = 0; f < 7; ++f)
+        if (req[f] && dev[f] == s->staging + off[f] * N)
+            CK(cudaMemcpyAsync(req[f], dev[f], sizeof(double) * cnt[f] * N, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return AEP_OK;
 }

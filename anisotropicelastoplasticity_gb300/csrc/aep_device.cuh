@@ -130,6 +130,8 @@ struct DevStats {
     unsigned long long learned_ok;      // learned return maps accepted
     unsigned long long learned_rejected;  // learned outputs replaced by the exact mapping
     long long movers;              // particles that changed key (incremental ordering), -1: full sort
+    unsigned int force_fp64;       // entries of the force pass's FP64 list (k_force_fp64)
+    unsigned int pad;
 };
 
 // Training-pair harvest from the exact return mapping (plain G2P): records of 8

@@ -320,8 +320,13 @@ constexpr int kFrcRec = 11;
 constexpr int kFrcWarpBuf = 32 * kFrcRec + 1;
 __device__ __forceinline__ int frc_slot(int p) { return p * kFrcRec + (p >= 16 ? 1 : 0); }
 
+// The FP32 stress impulse of one particle; a near-degenerate F-hat (a singular
+// value under 2% of the largest) gives S = 0 here and the particle is listed for
+// k_force_fp64, which redoes it in FP64 and scatters it on its own (keeping the
+// FP64 code, and its registers, out of k_force).
 __device__ void particle_stress_impulse(const KParams& P, const GArrays& G, const PArrays& cur, int pj, float dt_force,
-                                        float S[9], float w[3][4], float dw[3][4], int cell[3], DevStats* st) {
+                                        float S[9], float w[3][4], float dw[3][4], int cell[3], DevStats* st,
+                                        int32_t* fp64_list, int fp64_cap) {
     float f[3];
     locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
     particle_weights(P, cell, f, w, dw);
@@ -388,24 +393,85 @@ __device__ void particle_stress_impulse(const KParams& P, const GArrays& G, cons
     if (ok) {
         stress_from_svd<float>(P, mat, Fh, F, U, s, V, Jp, vol, out);
     } else {
-        double Fd[9], Fhd[9], Ud[9], sd[3], Vd[9], od[9];
+        const unsigned k = atomicAdd(&st->force_fp64, 1u);
+        if ((int)k < fp64_cap) fp64_list[k] = pj;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) { Fd[k] = F[k]; Fhd[k] = Fh[k]; }
-        svd3<double>(Fhd, Ud, sd, Vd, 40, 1e-15, 0.0);
-        svd3_complete(Ud, sd);
-        stress_from_svd<double>(P, mat, Fhd, Fd, Ud, sd, Vd, (double)Jp, (double)vol, od);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) out[k] = (float)od[k];
-        atomicAdd(&st->fallbacks, 1ull);
+        for (int k2 = 0; k2 < 9; ++k2) out[k2] = 0.0f;
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) S[k] = -dt_force * out[k];
 }
 
+// FP64 stress impulses of the particles k_force listed, each scattered to its 64
+// stencil nodes with its own fixed-point atomics (integer sums: the order does
+// not matter).  Grid-stride over the list; usually empty.
+__global__ void k_force_fp64(KParams P, PArrays cur, GArrays G, float dt_force, DevStats* st,
+                             const int32_t* __restrict__ fp64_list, int fp64_cap) {
+    dt_force = step_dt(P, dt_force, 0);
+    const int count = min((int)st->force_fp64, fp64_cap);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
+        const int pj = fp64_list[q];
+        float f[3], w[3][4], dw[3][4];
+        int cell[3];
+        locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
+        particle_weights(P, cell, f, w, dw);
+        int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+        uint32_t X[4], Y[4], Z[4];
+        stencil_offsets(P, base, X, Y, Z);
+        float Gm[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // grad v (HS:269-271), as in particle_stress_impulse
+        for (int oz = 0; oz < 4; ++oz)
+            for (int oy = 0; oy < 4; ++oy)
+                for (int ox = 0; ox < 4; ++ox) {
+                    const float4 v = __ldg(&G.vel[Y[oy] + Z[oz] + X[ox]]);
+                    const float g[3] = {dw[0][ox] * w[1][oy] * w[2][oz], w[0][ox] * dw[1][oy] * w[2][oz],
+                                        w[0][ox] * w[1][oy] * dw[2][oz]};
+                    const float vv[3] = {v.x, v.y, v.z};
+                    for (int c = 0; c < 3; ++c)
+                        for (int b = 0; b < 3; ++b) Gm[3 * c + b] = fmaf(vv[c], g[b], Gm[3 * c + b]);
+                }
+        float F[9], GF[9], Fh[9];
+        for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
+        mat_mul(Gm, F, GF);
+        for (int k = 0; k < 9; ++k) Fh[k] = F[k] + dt_force * GF[k];
+        const int mat = cur.mat[pj];
+        float Jp = 1.0f;
+        if (mat == kSnow) {
+            if (P.track_fp) {
+                float Fp[9];
+                for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
+                Jp = mat_det(Fp);
+            } else {
+                Jp = cur.plastic[pj];
+            }
+        }
+        double Fd[9], Fhd[9], Ud[9], sd[3], Vd[9], od[9];
+        for (int k = 0; k < 9; ++k) { Fd[k] = F[k]; Fhd[k] = Fh[k]; }
+        svd3<double>(Fhd, Ud, sd, Vd, 40, 1e-15, 0.0);
+        svd3_complete(Ud, sd);
+        stress_from_svd<double>(P, mat, Fhd, Fd, Ud, sd, Vd, (double)Jp, (double)cur.vol[pj], od);
+        float S[9];
+        for (int k = 0; k < 9; ++k) S[k] = -dt_force * (float)od[k];
+        for (int oz = 0; oz < 4; ++oz)
+            for (int oy = 0; oy < 4; ++oy)
+                for (int ox = 0; ox < 4; ++ox) {
+                    const float g[3] = {dw[0][ox] * w[1][oy] * w[2][oz], w[0][ox] * dw[1][oy] * w[2][oz],
+                                        w[0][ox] * w[1][oy] * dw[2][oz]};
+                    if (g[0] == 0.0f && g[1] == 0.0f && g[2] == 0.0f) continue;
+                    unsigned long long* a = G.acc + 4ull * node_index(P, base[0] + ox, base[1] + oy, base[2] + oz);
+                    for (int c = 0; c < 3; ++c) {
+                        const float fc = S[3 * c] * g[0] + S[3 * c + 1] * g[1] + S[3 * c + 2] * g[2];
+                        atomicAdd(a + 1 + c, to_fixed(fc, P.mom_scale));
+                    }
+                }
+        atomicAdd(&st->fallbacks, 1ull);
+    }
+}
+
 // impulse scatter: f_i -= sum_p stress_p grad w_ip (HS:356-366), stored as dt * f_i
-__global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(kFrcThreads, 5) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                        const int32_t* __restrict__ perm, int n, GArrays G,
-                                                       float dt_force, DevStats* st, MeshArrays M) {
+                                                       float dt_force, DevStats* st, MeshArrays M,
+                                                       int32_t* fp64_list, int fp64_cap) {
     __shared__ float4 sm4[(kFrcThreads / 32) * kFrcWarpBuf];
     dt_force = step_dt(P, dt_force, 0);
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -421,7 +487,7 @@ __global__ void __launch_bounds__(kFrcThreads, 4) k_force(KParams P, PArrays cur
         int cell[3];
         const int mat = cur.mat[pj];
         if (mat <= kSand) {
-            particle_stress_impulse(P, G, cur, pj, dt_force, S, w, dw, cell, st);
+            particle_stress_impulse(P, G, cur, pj, dt_force, S, w, dw, cell, st, fp64_list, fp64_cap);
         } else {
             float f[3];
             locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
@@ -1453,6 +1519,105 @@ __global__ void k_upload(long total, int n, int mode, const double* __restrict__
     d[k][p] = (float)src[e];
 }
 
+// The whole particle upload of aep_set_particles in one launch: one thread per
+// source double, over the segments x (3n), v (3n), B (9n), Fe (9n), Fp (9n, with
+// track_plastic_F and a given F_P) and one thread per item for m, vol, plastic,
+// material, id and snow J_P.  Consecutive threads read consecutive doubles, so a
+// source in page-locked host memory streams over the host link without gaps
+// between kernels.  Item q goes to slot map[q] (or q).  check = {max mass bits,
+// bad mass or tag}.
+__global__ void k_upload_particles(int n, UploadSrc src, PArrays P, const int32_t* __restrict__ map, int track_fp,
+                                   unsigned long long* check) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long N = n;
+    const long nF = (track_fp && src.Fp) ? 9 * N : 0;
+    const long total = 24 * N + nF + N;
+    unsigned long long mx = 0ull, bad = 0ull;
+    if (e < total) {
+        long r = e;
+        if (r < 3 * N) {  // x: N x 3 column-major
+            const int a = (int)(r / N), q = (int)(r % N);
+            P.x[a][map ? map[q] : q] = (float)src.x[r];
+        } else if ((r -= 3 * N) < 3 * N) {  // v
+            const int a = (int)(r / N), q = (int)(r % N);
+            P.v[a][map ? map[q] : q] = src.v ? (float)src.v[r] : 0.0f;
+        } else if ((r -= 3 * N) < 9 * N) {  // B: block a of N x 3 = row a
+            const int t = (int)(r / N), q = (int)(r % N);
+            P.B[t][map ? map[q] : q] = src.B ? (float)src.B[r] : 0.0f;
+        } else if ((r -= 9 * N) < 9 * N) {  // Fe: 3x3 column-major per item
+            const int q = (int)(r / 9), c = (int)(r % 9);
+            P.F[3 * (c % 3) + c / 3][map ? map[q] : q] = (float)src.Fe[r];
+        } else if ((r -= 9 * N) < nF) {  // F_P, same layout
+            const int q = (int)(r / 9), c = (int)(r % 9);
+            P.Fp[3 * (c % 3) + c / 3][map ? map[q] : q] = (float)src.Fp[r];
+        } else {  // item fields
+            const int q = (int)(r - nF);
+            const int p = map ? map[q] : q;
+            const double m = src.m[q];
+            if (!(m >= 0.0) || !isfinite(m)) bad = 1ull;
+            else if (m > 0.0) mx = (unsigned long long)__double_as_longlong(m);
+            const int mat = src.mat ? (int)src.mat[q] : kSand;
+            if (mat > kSand) bad = 1ull;
+            P.m[p] = (float)m;
+            P.vol[p] = src.vol ? (float)src.vol[q] : 0.0f;
+            P.mat[p] = (uint8_t)mat;
+            P.id[p] = q;
+            float pl = src.plastic ? (float)src.plastic[q] : 0.0f;
+            if (track_fp && !src.Fp)
+#pragma unroll
+                for (int c = 0; c < 9; ++c) P.Fp[c][p] = (c % 4 == 0) ? 1.0f : 0.0f;
+            if (!track_fp && mat == kSnow) {  // J_P = det F_P, else the given scalar, else 1
+                if (src.Fp) {
+                    double A[9];
+#pragma unroll
+                    for (int c = 0; c < 9; ++c) A[3 * (c % 3) + c / 3] = src.Fp[9l * q + c];
+                    pl = (float)mat_det(A);
+                } else if (!src.plastic) {
+                    pl = 1.0f;
+                }
+            }
+            P.plastic[p] = pl;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (mx) atomicMax(check, mx);
+        if (bad) atomicOr(check + 1, bad);
+    }
+}
+
+// The particle readback of aep_get_particles in one launch: one thread per
+// destination double over the requested fields (coalesced writes into
+// page-locked host memory); inv[id] = slot.
+__global__ void k_download_particles(int n, DownloadDst dst, PArrays P, const int32_t* __restrict__ inv) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long N = n;
+    long r = e;
+    const long sx = dst.x ? 3 * N : 0, sv = dst.v ? 3 * N : 0, sB = dst.B ? 9 * N : 0, sF = dst.Fe ? 9 * N : 0,
+               sP = dst.Fp ? 9 * N : 0, sV = dst.vol ? N : 0, sQ = dst.plastic ? N : 0;
+    if (r < sx) {
+        dst.x[r] = (double)P.x[r / N][inv[r % N]];
+    } else if ((r -= sx) < sv) {
+        dst.v[r] = (double)P.v[r / N][inv[r % N]];
+    } else if ((r -= sv) < sB) {
+        dst.B[r] = (double)P.B[r / N][inv[r % N]];
+    } else if ((r -= sB) < sF) {
+        const int c = (int)(r % 9);
+        dst.Fe[r] = (double)P.F[3 * (c % 3) + c / 3][inv[r / 9]];
+    } else if ((r -= sF) < sP) {
+        const int c = (int)(r % 9);
+        dst.Fp[r] = (double)P.Fp[3 * (c % 3) + c / 3][inv[r / 9]];
+    } else if ((r -= sP) < sV) {
+        dst.vol[r] = (double)P.vol[inv[r]];
+    } else if ((r -= sV) < sQ) {
+        dst.plastic[r] = (double)P.plastic[inv[r]];
+    }
+}
+
 // FP32 SoA -> host-layout doubles for ids [id_lo, id_lo + count), one thread per
 // destination double (coalesced writes into pinned host memory); inv[id] = slot.
 __global__ void k_download(long total, int count, int mode, const int32_t* __restrict__ inv, int id_lo,
@@ -1571,11 +1736,15 @@ void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid
     k_normalize<<<grid_blocks, 256, 0, s>>>(P, G, st);
 }
 void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
-                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s) {
+                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s,
+                  int32_t* fp64_list) {
     long warps = (n + 31) / 32;
     if (M.nf > 0) k_cloth_force<<<blocks_for(M.nf, 128), 128, 0, s>>>(P, cur, M, dt_force);
-    if (n > 0)
-        k_force<<<blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s>>>(P, cur, keys, perm, n, G, dt_force, st, M);
+    if (n > 0) {
+        k_force<<<blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s>>>(P, cur, keys, perm, n, G, dt_force, st, M,
+                                                                            fp64_list, n);
+        k_force_fp64<<<8, 128, 0, s>>>(P, cur, G, dt_force, st, fp64_list, n);
+    }
 }
 void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
                  int grid_blocks, cudaStream_t s) {
@@ -1619,6 +1788,17 @@ void launch_upload(int n, int mode, const double* src, float* const* dst, cudaSt
     if (total > 0)
         k_upload<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(total, n, mode, src, dst[0], dst[1], dst[2], dst[3],
                                                                  dst[4], dst[5], dst[6], dst[7], dst[8], map);
+}
+void launch_upload_particles(int n, const UploadSrc& src, const PArrays& P, const int32_t* map, int track_fp,
+                             unsigned long long* check, cudaStream_t s) {
+    const long total = 25l * n + ((track_fp && src.Fp) ? 9l * n : 0);
+    if (n > 0)
+        k_upload_particles<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n, src, P, map, track_fp, check);
+}
+void launch_download_particles(int n, const DownloadDst& dst, const PArrays& P, const int32_t* inv, cudaStream_t s) {
+    const long total = (long)n * ((dst.x ? 3 : 0) + (dst.v ? 3 : 0) + (dst.B ? 9 : 0) + (dst.Fe ? 9 : 0) +
+                                  (dst.Fp ? 9 : 0) + (dst.vol ? 1 : 0) + (dst.plastic ? 1 : 0));
+    if (total > 0) k_download_particles<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n, dst, P, inv);
 }
 void launch_fixed_vertices(const KParams& P, const PArrays& cur, const GArrays& G, const MeshArrays& M,
                            const int32_t* fixed, int nfixed, cudaStream_t s) {

@@ -12,7 +12,8 @@ void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, cons
                 const GArrays& G, int32_t* slot_of, int32_t* curidx_of, cudaStream_t s);
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s);
 void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
-                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s);
+                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s,
+                  int32_t* fp64_list);
 void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
                  int grid_blocks, cudaStream_t s);
 void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s);
@@ -24,6 +25,17 @@ void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, i
 void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s,
                    const int32_t* map = nullptr);
 void launch_inverse_ids(int n, const int32_t* id, int32_t* inv, cudaStream_t s);
+// one-launch particle upload / readback (device-usable source / destination pointers)
+struct UploadSrc {
+    const double *x, *v, *B, *Fe, *Fp, *m, *vol, *plastic;
+    const uint8_t* mat;
+};
+struct DownloadDst {
+    double *x, *v, *B, *Fe, *Fp, *vol, *plastic;
+};
+void launch_upload_particles(int n, const UploadSrc& src, const PArrays& P, const int32_t* map, int track_fp,
+                             unsigned long long* check, cudaStream_t s);
+void launch_download_particles(int n, const DownloadDst& dst, const PArrays& P, const int32_t* inv, cudaStream_t s);
 void launch_fixed_vertices(const KParams& P, const PArrays& cur, const GArrays& G, const MeshArrays& M,
                            const int32_t* fixed, int nfixed, cudaStream_t s);
 void launch_solve_dt(SolveState* S, int phase, cudaStream_t s);

@@ -296,3 +296,33 @@ def test_upload_and_readback_from_pinned_and_device_memory(where):
     ref.step(sc.dt)
     a, b = s.get_particles(), ref.get_particles()
     assert np.array_equal(a["positions"], b["positions"]) and np.array_equal(a["velocities"], b["velocities"])
+
+
+@pytest.mark.parametrize("kind", ["snow", "sand"])
+def test_fp64_fallbacks_match_oracle(kind):
+    """Near-degenerate deformation gradients (a singular value at 1% of the largest)
+    take the FP64 path: in the force pass a separate kernel (k_force_fp64) redoes
+    their stress and scatters it, in G2P the return mapping is redone in FP64.
+    Forces and the stepped particles match the oracle at the usual tolerances."""
+    sc = perturbed(small_scene(kind), seed=31)
+    ps = sc.particles
+    rng = np.random.default_rng(32)
+    sel = rng.random(len(ps)) < 0.05
+    q, _ = np.linalg.qr(rng.standard_normal((int(sel.sum()), 3, 3)))
+    ps.elastic_deformation_gradients[sel] = q @ np.diag([1.0, 0.9, 0.01]) @ q.transpose(0, 2, 1)
+    gpu, orc = make_pair(sc)
+    gpu.step_stage(sc.dt, capi.AEP_STAGE_FORCES)
+    assert gpu.stats()["fp64_fallbacks"] >= sel.sum()
+    g = gpu.get_grid()
+    orc.init(volumes=False)
+    orc.step(sc.dt, stage=capi.AEP_STAGE_FORCES)
+    o = orc.get_grid()
+    f_orc = o["forces"] - o["masses"][:, None] * np.array(list(sc.params.gravity))
+    assert max_rel(g["forces"], f_orc) < 2e-4
+    gpu2, orc2 = make_pair(sc)
+    gpu2.step(sc.dt)
+    assert gpu2.stats()["fp64_fallbacks"] >= sel.sum()
+    orc2.init(volumes=False)
+    orc2.step(sc.dt)
+    _compare_particles(gpu2.get_particles(), orc2.get_particles(), pos_tol=5e-7, vel_tol=1e-4, F_tol=2e-6,
+                       B_tol=1e-3, q_tol=2e-6, h=float(sc.grid.h.min()))
