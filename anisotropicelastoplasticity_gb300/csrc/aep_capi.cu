@@ -895,7 +895,7 @@ aep_status step_impl(aep_solver* s, double dt_force, double dt, int32_t stage, b
     MlpParams mp{};
     if (s->mlp) mp = mlp_device_params(s->mlp);
     launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, (float)dt, s->keys, s->dstats, M, s->stream, H,
-               s->mlp ? &mp : nullptr, (float)s->learned_tol);
+               s->mlp ? &mp : nullptr, (float)s->learned_tol, s->keys_sorted);
     CKLAUNCH();
     if (timed) {
         mark(s, AEP_NUM_PHASES);

@@ -221,6 +221,48 @@ __device__ __forceinline__ void stencil_offsets(const KParams& P, const int base
     }
 }
 
+// Grid tile of a block of sorted particles: the 2x2x2 node blocks (512 nodes)
+// starting at the base-node block of the block's first particle.  Particles are
+// ordered by base-node block, so almost every particle of the block has its
+// whole 4x4x4 stencil inside; their gathers read shared memory instead of L1/L2.
+constexpr int kTileNodes = 512;
+
+__device__ __forceinline__ void tile_origin(const KParams& P, uint32_t key, int org[3]) {
+    const uint32_t blk = key >> 6;
+    org[0] = (int)(blk % (uint32_t)P.nb[0]);
+    const uint32_t r = blk / (uint32_t)P.nb[0];
+    org[1] = (int)(r % (uint32_t)P.nb[1]);
+    org[2] = (int)(r / (uint32_t)P.nb[1]);
+}
+
+// cooperative copy of the tile (all threads of the block); src2 / dst2 may be null
+__device__ __forceinline__ void load_tile(const KParams& P, const int org[3], const float4* __restrict__ src,
+                                          const float4* __restrict__ src2, float4* dst, float4* dst2) {
+    for (int i = threadIdx.x; i < kTileNodes; i += blockDim.x) {
+        const int t = i >> 6;
+        const uint32_t gblk = (uint32_t)(((org[2] + (t >> 2)) * P.nb[1] + org[1] + ((t >> 1) & 1)) * P.nb[0] + org[0] +
+                                         (t & 1));
+        const uint32_t node = (gblk << 6) | (uint32_t)(i & 63);
+        dst[i] = src[node];
+        if (dst2) dst2[i] = src2[node];
+    }
+}
+
+// stencil offsets inside the tile when the stencil's base block is the tile's
+// origin (returns false otherwise); the same additive form as stencil_offsets
+__device__ __forceinline__ bool tile_offsets(const int base[3], const int org[3], uint32_t X[4], uint32_t Y[4],
+                                             uint32_t Z[4]) {
+    if ((base[0] >> 2) != org[0] || (base[1] >> 2) != org[1] || (base[2] >> 2) != org[2]) return false;
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const int x = base[0] + o - 4 * org[0], y = base[1] + o - 4 * org[1], z = base[2] + o - 4 * org[2];
+        X[o] = (uint32_t)((x >> 2) * 64 + (x & 3));
+        Y[o] = (uint32_t)((y >> 2) * 128 + ((y & 3) << 2));
+        Z[o] = (uint32_t)((z >> 2) * 256 + ((z & 3) << 4));
+    }
+    return true;
+}
+
 // weights of one particle with the reference's out-of-grid node drop (HS:44-46)
 __device__ __forceinline__ bool particle_weights(const KParams& P, const int cell[3], const float f[3],
                                                  float w[3][4], float dw[3][4]) {

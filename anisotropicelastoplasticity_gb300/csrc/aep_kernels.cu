@@ -324,15 +324,12 @@ __device__ __forceinline__ int frc_slot(int p) { return p * kFrcRec + (p >= 16 ?
 // value under 2% of the largest) gives S = 0 here and the particle is listed for
 // k_force_fp64, which redoes it in FP64 and scatters it on its own (keeping the
 // FP64 code, and its registers, out of k_force).
-__device__ void particle_stress_impulse(const KParams& P, const GArrays& G, const PArrays& cur, int pj, float dt_force,
-                                        float S[9], float w[3][4], float dw[3][4], int cell[3], DevStats* st,
-                                        int32_t* fp64_list, int fp64_cap) {
-    float f[3];
-    locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
-    particle_weights(P, cell, f, w, dw);
-    int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
-    uint32_t X[4], Y[4], Z[4];
-    stencil_offsets(P, base, X, Y, Z);
+// vel: the grid velocities (global) or the block's tile; X, Y, Z the stencil
+// offsets into it; w, dw the particle's weights
+__device__ void particle_stress_impulse(const KParams& P, const float4* vel, const uint32_t X[4], const uint32_t Y[4],
+                                        const uint32_t Z[4], const PArrays& cur, int pj, float dt_force, float S[9],
+                                        const float w[3][4], const float dw[3][4], DevStats* st, int32_t* fp64_list,
+                                        int fp64_cap) {
     // velocity gradient of the P2G velocity (the three SpMVs of HS:269-271),
     // contracted one axis at a time: Gm = sum v (grad w)^T with
     // grad w = (dwx wy wz, wx dwy wz, wx wy dwz)
@@ -346,7 +343,7 @@ __device__ void particle_stress_impulse(const KParams& P, const GArrays& G, cons
             float Ad[3] = {0, 0, 0}, Aw[3] = {0, 0, 0};
 #pragma unroll
             for (int ox = 0; ox < 4; ++ox) {
-                const float4 v = __ldg(&G.vel[yz + X[ox]]);
+                const float4 v = vel[yz + X[ox]];
                 const float a = w[0][ox], d = dw[0][ox];
                 Ad[0] = fmaf(d, v.x, Ad[0]); Ad[1] = fmaf(d, v.y, Ad[1]); Ad[2] = fmaf(d, v.z, Ad[2]);
                 Aw[0] = fmaf(a, v.x, Aw[0]); Aw[1] = fmaf(a, v.y, Aw[1]); Aw[2] = fmaf(a, v.z, Aw[2]);
@@ -473,25 +470,41 @@ __global__ void __launch_bounds__(kFrcThreads, 5) k_force(KParams P, PArrays cur
                                                        float dt_force, DevStats* st, MeshArrays M,
                                                        int32_t* fp64_list, int fp64_cap) {
     __shared__ float4 sm4[(kFrcThreads / 32) * kFrcWarpBuf];
+    __shared__ float4 tile_v[kTileNodes];
     dt_force = step_dt(P, dt_force, 0);
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const buf = sm4 + wid * kFrcWarpBuf;
     const long chunk0 = ((long)blockIdx.x * (kFrcThreads / 32) + wid) * 32;
-    if (chunk0 >= n) return;
     const long j = chunk0 + lane;
+    int org[3];
+    tile_origin(P, keys[(long)blockIdx.x * kFrcThreads], org);
+    load_tile(P, org, G.vel, nullptr, tile_v, nullptr);
+    // the particle's own loads and weights overlap the tile copy
+    const bool live = j < n;
+    const int pj = live ? perm[j] : 0;
+    const int mat = live ? (int)cur.mat[pj] : 0;
+    int cell[3];
+    float w[3][4], dw[3][4];
+    uint32_t X[4], Y[4], Z[4];
+    bool in_tile = false;
+    {
+        float f[3];
+        locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
+        particle_weights(P, cell, f, w, dw);
+        const int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+        in_tile = tile_offsets(base, org, X, Y, Z);
+        if (!in_tile) stencil_offsets(P, base, X, Y, Z);
+    }
+    __syncthreads();
+    if (chunk0 >= n) return;
     uint32_t my_key = kInvalidKey;
-    if (j < n) {
-        const int pj = perm[j];
-        float w[3][4], dw[3][4], S[9];
+    if (live) {
+        float S[9];
         float av[3] = {0.f, 0.f, 0.f};  // w-weighted impulse (cloth vertices)
-        int cell[3];
-        const int mat = cur.mat[pj];
         if (mat <= kSand) {
-            particle_stress_impulse(P, G, cur, pj, dt_force, S, w, dw, cell, st, fp64_list, fp64_cap);
+            particle_stress_impulse(P, in_tile ? tile_v : G.vel, X, Y, Z, cur, pj, dt_force, S, w, dw, st, fp64_list,
+                                    fp64_cap);
         } else {
-            float f[3];
-            locate(P, cur.x[0][pj], cur.x[1][pj], cur.x[2][pj], cell, f);
-            particle_weights(P, cell, f, w, dw);
             const int id = cur.id[pj];
             if (mat == kClothVertex) {
                 // rg.forces += vertexOmegas^T vertexInPlaneForces (HS:376-378)
@@ -826,9 +839,10 @@ __device__ __forceinline__ void return_map(const KParams& P, int mat, T s[3], T&
 // products: x first (A), then z (B), then y.
 //   A0 = sum_x wx v      A1 = sum_x wx xi_x v   A2 = sum_x dwx vbf   A3 = sum_x wx vbf
 //   vp = sum w v,  C = sum w v xi^T,  xs = sum w vbf,  Gb = sum vbf (grad w)^T
-__device__ __forceinline__ void g2p_gather(const GArrays& G, const float w[3][4], const float dw[3][4],
-                                           const float xi[3][4], const uint32_t X[4], const uint32_t Y[4],
-                                           const uint32_t Z[4], float vp[3], float C[9], float xs[3], float Gb[9]) {
+__device__ __forceinline__ void g2p_gather(const float4* vel, const float4* vbf, const float w[3][4],
+                                           const float dw[3][4], const float xi[3][4], const uint32_t X[4],
+                                           const uint32_t Y[4], const uint32_t Z[4], float vp[3], float C[9],
+                                           float xs[3], float Gb[9]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) vp[k] = xs[k] = 0.f;
 #pragma unroll
@@ -846,8 +860,8 @@ __device__ __forceinline__ void g2p_gather(const GArrays& G, const float w[3][4]
             float A0[3] = {0, 0, 0}, A1[3] = {0, 0, 0}, A2[3] = {0, 0, 0}, A3[3] = {0, 0, 0};
 #pragma unroll
             for (int ox = 0; ox < 4; ++ox) {
-                const float4 v = __ldg(&G.vel[yz + X[ox]]);
-                const float4 b = __ldg(&G.vbf[yz + X[ox]]);
+                const float4 v = vel[yz + X[ox]];
+                const float4 b = vbf[yz + X[ox]];
                 const float a = w[0][ox], ax_ = wxi[ox], d = dw[0][ox];
                 A0[0] = fmaf(a, v.x, A0[0]); A0[1] = fmaf(a, v.y, A0[1]); A0[2] = fmaf(a, v.z, A0[2]);
                 A1[0] = fmaf(ax_, v.x, A1[0]); A1[1] = fmaf(ax_, v.y, A1[1]); A1[2] = fmaf(ax_, v.z, A1[2]);
@@ -908,15 +922,18 @@ __device__ __forceinline__ void harvest_record(const Harvest& H, int mat, const 
     for (int k = 0; k < 3; ++k) r[5 + k] = logf(s_new[pm[k]]) - srt[k];
 }
 
-__global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
+__global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
                                              int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
-                                             DevStats* st, Harvest H) {
+                                             DevStats* st, Harvest H, const uint32_t* __restrict__ keys_sorted) {
+    __shared__ float4 tile_v[kTileNodes], tile_b[kTileNodes];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    dt = step_dt(P, dt, 1);
-    const int pj = perm[j];
-    const int mat = cur.mat[pj];
-    if (mat == kClothElement) return;  // elements follow their vertices (k_cloth_g2p)
+    int org[3];
+    tile_origin(P, keys_sorted[blockIdx.x * blockDim.x], org);
+    load_tile(P, org, G.vel, G.vbf, tile_v, tile_b);
+    // the particle's own loads and weights overlap the tile copy
+    const bool live = j < n;
+    const int pj = live ? perm[j] : 0;
+    const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
     float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
     int cell[3];
     float f[3], w[3][4], dw[3][4];
@@ -924,7 +941,12 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
     const bool truncated = particle_weights(P, cell, f, w, dw);
     int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
     uint32_t X[4], Y[4], Z[4];
-    stencil_offsets(P, base, X, Y, Z);
+    const bool in_tile = tile_offsets(base, org, X, Y, Z);
+    if (!in_tile) stencil_offsets(P, base, X, Y, Z);
+    __syncthreads();
+    // elements follow their vertices (k_cloth_g2p)
+    if (!live || mat == kClothElement) return;
+    dt = step_dt(P, dt, 1);
     float xi[3][4];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -932,7 +954,7 @@ __global__ void __launch_bounds__(128) k_g2p(KParams P, PArrays cur, PArrays nxt
         for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
 
     float vp[3], xs[3], C[9], Gb[9];
-    g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+    g2p_gather(in_tile ? tile_v : G.vel, in_tile ? tile_b : G.vbf, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
     // advection x = sum w (x_i + dt v^bf_i) (HS:944): exact linear reproduction for a
     // full stencil; a stencil cut by the grid boundary keeps its lost weight.
     float xn[3];
@@ -1207,7 +1229,7 @@ __global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArra
 #pragma unroll
                 for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
             float vp[3], xs[3], C[9], Gb[9], xn[3], Bn[9];
-            g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+            g2p_gather(G.vel, G.vbf, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
 #pragma unroll
             for (int a = 0; a < 3; ++a) xn[a] = xp[a] + dt * xs[a];
             if (truncated) {
@@ -1366,7 +1388,7 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
 #pragma unroll
             for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
         float vp[3], xs[3], C[9], Gb[9];
-        g2p_gather(G, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+        g2p_gather(G.vel, G.vbf, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
         float Bn[9];
         apic_damp(C, P.mesh_damp, Bn);
         float xv[3][3], vv[3][3];
@@ -1755,7 +1777,7 @@ void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s) {
 }
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
                 const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s,
-                const Harvest& H, const MlpParams* mlp, float learned_tol) {
+                const Harvest& H, const MlpParams* mlp, float learned_tol, const uint32_t* keys_sorted) {
     if (n > 0) {
         if (mlp) {
             const int smem = kLrnSmemBytes;
@@ -1768,7 +1790,7 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
             k_g2p_learned<<<blocks, kLrnThreads, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp,
                                                             learned_tol);
         } else {
-            k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H);
+            k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H, keys_sorted);
         }
     }
     if (M.nf > 0) {
