@@ -1185,11 +1185,15 @@ constexpr int kLrnThreads = 128;
 constexpr int kLrnWarps = kLrnThreads / 32;
 constexpr int kLrnSmemBytes = kMlpSmemBytes + kLrnThreads * kStrideIn * 2 + kLrnThreads * kMlpOut * 4 +
                               kLrnWarps * 2 * kMlpWarpH * 2;
+static_assert(kLrnWarps * 2 * kMlpWarpH * 2 >= 2 * kTileNodes * 16, "the grid tile must fit the hidden-layer buffers");
+static_assert((kMlpSmemBytes + kLrnThreads * kStrideIn * 2 + kLrnThreads * kMlpOut * 4) % 16 == 0,
+              "the grid tile must be 16-byte aligned");
 
 __global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArrays cur, PArrays nxt,
                                                              const int32_t* __restrict__ perm, int n, GArrays G,
                                                              float dt, uint32_t* __restrict__ keys_next,
-                                                             DevStats* st, MlpParams mlp, float tol) {
+                                                             DevStats* st, MlpParams mlp, float tol,
+                                                             const uint32_t* __restrict__ keys_sorted) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_cnt[kLrnWarps];
     dt = step_dt(P, dt, 1);
@@ -1198,8 +1202,12 @@ __global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArra
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __nv_bfloat16* CX = reinterpret_cast<__nv_bfloat16*>(smem_raw + kMlpSmemBytes);  // compacted feature rows
     float* CY = reinterpret_cast<float*>(CX + kLrnThreads * kStrideIn);             // their outputs
-    __nv_bfloat16* H0 = reinterpret_cast<__nv_bfloat16*>(CY + kLrnThreads * kMlpOut) + warp * 2 * kMlpWarpH;
+    unsigned char* const hbase = reinterpret_cast<unsigned char*>(CY + kLrnThreads * kMlpOut);
+    __nv_bfloat16* H0 = reinterpret_cast<__nv_bfloat16*>(hbase) + warp * 2 * kMlpWarpH;
     __nv_bfloat16* H1 = H0 + kMlpWarpH;
+    // the grid tile of phase A shares the memory of the hidden layers of phase B
+    float4* const tile_v = reinterpret_cast<float4*>(hbase);
+    float4* const tile_b = tile_v + kTileNodes;
     __syncthreads();
 
     for (long chunk = blockIdx.x; chunk * kLrnThreads < n; chunk += gridDim.x) {
@@ -1209,27 +1217,32 @@ __global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArra
         const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
         const bool active = live && mat != kClothElement;
         // --- phase A: gather, advection, APIC, F update, SVD, yield check ------------
+        int org[3];
+        tile_origin(P, keys_sorted[chunk * kLrnThreads], org);
+        load_tile(P, org, G.vel, G.vbf, tile_v, tile_b);  // after the last chunk's phase-B barrier
+        const float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
+        int cell[3];
+        float f[3], w[3][4], dw[3][4];
+        locate(P, xp[0], xp[1], xp[2], cell, f);
+        const bool truncated = particle_weights(P, cell, f, w, dw);
+        int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
+        uint32_t X[4], Y[4], Z[4];
+        const bool in_tile = tile_offsets(base, org, X, Y, Z);
+        if (!in_tile) stencil_offsets(P, base, X, Y, Z);
+        __syncthreads();
         bool need = false;  // plastic state whose projection the MLP predicts
         float U[9], V[9], s[3], srt[3], ex[3], lns[3];
         int pm[3] = {0, 1, 2};
         float q = 0.0f, qe = 0.0f, osc = 1.0f;
         float Ftr[9];
         if (active) {
-            const float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
-            int cell[3];
-            float f[3], w[3][4], dw[3][4];
-            locate(P, xp[0], xp[1], xp[2], cell, f);
-            const bool truncated = particle_weights(P, cell, f, w, dw);
-            int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
-            uint32_t X[4], Y[4], Z[4];
-            stencil_offsets(P, base, X, Y, Z);
             float xi[3][4];
 #pragma unroll
             for (int a = 0; a < 3; ++a)
 #pragma unroll
                 for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
             float vp[3], xs[3], C[9], Gb[9], xn[3], Bn[9];
-            g2p_gather(G.vel, G.vbf, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
+            g2p_gather(in_tile ? tile_v : G.vel, in_tile ? tile_b : G.vbf, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
 #pragma unroll
             for (int a = 0; a < 3; ++a) xn[a] = xp[a] + dt * xs[a];
             if (truncated) {
@@ -1788,7 +1801,7 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_g2p_learned, kLrnThreads, smem);
             const int blocks = std::min(blocks_for(n, kLrnThreads), std::max(1, sms * std::max(per_sm, 1)));
             k_g2p_learned<<<blocks, kLrnThreads, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp,
-                                                            learned_tol);
+                                                            learned_tol, keys_sorted);
         } else {
             k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H, keys_sorted);
         }
