@@ -254,8 +254,12 @@ def run_ours(args):
                    "l2": "flushed between timed steps (512 MB write)", "active_nodes": nodes,
                    "active_blocks": int(st["active_blocks"])},
         "roofline": roofline,
-        "gpu_launches": 5 * args.steps,
-        "library_launches_note": "plus the CUB radix-sort kernels of each step's particle ordering",
+        # per step: the ordering graph's k_flag_movers + k_place_stayers (+ k_place_movers
+        # when more than 512 particles change cell; CUB radix-sort kernels instead when
+        # more than 8,192 do), k_p2g, k_normalize, k_force, k_force_fp64, k_grid, k_g2p
+        "gpu_launches": 8 * args.steps + (args.steps if st["sort_movers"] > 512 else 0),
+        "launches_note": "8 library kernels per step on this workload (2 of them inside the ordering graph); "
+                         f"last step's ordering moved {st['sort_movers']} particles (-1: full CUB radix sort)",
         "fp64_fallbacks_last_step": int(st["fp64_fallbacks"]),
         "wall_s": wall,
     }
