@@ -103,6 +103,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest x over the ranks of the default process group (x itself alone)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(items_per_rank: int, steps: int, seconds: float, world: int, device: str = "cuda"):
+    """Whole-job items x steps per second: every rank's items over the slowest rank's time
+    (replicas: weak scaling).  Returns (value, slowest seconds)."""
+    slowest = max_over_ranks(seconds, world, device)
+    return world * items_per_rank * steps / slowest, slowest
+
+
 def make_scene(args):
     from anisotropicelastoplasticity_gb300 import scenes
 
@@ -210,13 +229,8 @@ def run_ours(args):
     phase_ms, timed = solver.phase_times()
     solver.set_profiling(False)
     st = solver.stats()
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n_p * args.steps / (ms * 1e-3)
+    value, sec = job_throughput(n_p, args.steps, ms * 1e-3, world)
+    ms = sec * 1e3
 
     # roofline of the dominant kernel (CUDA events on the launching stream)
     per_launch = {k: v / max(timed, 1) for k, v in phase_ms.items()}
@@ -243,7 +257,7 @@ def run_ours(args):
     # end to end through the C-ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, solver, sc, stream)
+        e2e = run_e2e(args, solver, sc, stream, world)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -450,7 +464,7 @@ def run_learned_vs_plain(args, torch, flush):
     }
 
 
-def run_e2e(args, solver, sc, stream):
+def run_e2e(args, solver, sc, stream, world=1):
     import torch
 
     n = len(sc.particles)
@@ -495,7 +509,8 @@ def run_e2e(args, solver, sc, stream):
                                    dp(bufs["vol"]), dp(bufs["q"]))
         assert st == 0, st
     el = time.perf_counter() - t0
-    return {"value": n * steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+    value, _ = job_throughput(n, steps, el, world)
+    return {"value": value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": steps, "path": "aep_set_particles + aep_step + aep_get_particles, pinned FP64 host arrays "
                                     "in the reference layouts"}
 
