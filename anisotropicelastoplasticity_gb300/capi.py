@@ -92,7 +92,8 @@ class aep_stats(C.Structure):
         ("learned_accepted", C.c_int64),
         ("learned_fallbacks", C.c_int64),
         ("sort_movers", C.c_int64),
-        ("reserved", C.c_double * 4),
+        ("learned_exact", C.c_int64),
+        ("reserved", C.c_double * 3),
     ]
 
 
@@ -161,6 +162,7 @@ SIGNATURES = {
     "aep_set_harvest": (C.c_int, [_solver_p, C.c_void_p, C.c_int64, C.c_int32]),
     "aep_get_harvest_count": (C.c_int, [_solver_p, C.POINTER(C.c_int64)]),
     "aep_set_return_map": (C.c_int, [_solver_p, C.c_void_p, C.c_double]),
+    "aep_set_return_map_bounds": (C.c_int, [_solver_p, C.c_double, C.c_double]),
 }
 
 AEP_MLP_NUM_PARAMS = 9928

@@ -48,7 +48,10 @@ struct aep_solver {
     int64_t harvest_cap = 0;
     int32_t harvest_stride = 1;
     const aep_mlp* mlp = nullptr;
-    double learned_tol = 1e-4;
+    double learned_tol = 1e-3;  // learned-map check: relative bound
+    double learned_abs = 0x1p-23;  // and absolute bound (ln-strain units)
+    void* queue_mem = nullptr;     // rows queued for the network (MlpQueue), one per particle
+    MlpQueue queue{};
     ParticleSet set[2];
     PArrays P[2];
     int cur = 0;
@@ -559,6 +562,7 @@ aep_status aep_solver_destroy(aep_solver* s) {
     cudaFree(s->dstats);
     cudaFree(s->dforce);
     cudaFree(s->harvest_count);
+    cudaFree(s->queue_mem);
     cudaFree(s->check);
     cudaFreeHost(s->check_host);
     cudaFree(s->solve);
@@ -893,9 +897,23 @@ aep_status step_impl(aep_solver* s, double dt_force, double dt, int32_t stage, b
     const int nx = 1 - s->cur;
     Harvest H{s->harvest, s->harvest_count, s->harvest_cap, s->harvest_stride};
     MlpParams mp{};
-    if (s->mlp) mp = mlp_device_params(s->mlp);
+    if (s->mlp) {
+        mp = mlp_device_params(s->mlp);
+        if (s->queue.cap < s->n) {  // room for every particle: (int32 j, pj, 35 floats) per row
+            CK(cudaStreamSynchronize(s->stream));
+            cudaFree(s->queue_mem);
+            s->queue_mem = nullptr;
+            s->queue = MlpQueue{};
+            const size_t cap = (size_t)s->n;
+            CK(cudaMalloc(&s->queue_mem, cap * (2 * sizeof(int32_t) + kQueueFields * sizeof(float))));
+            s->queue.j = static_cast<int32_t*>(s->queue_mem);
+            s->queue.pj = s->queue.j + cap;
+            s->queue.f = reinterpret_cast<float*>(s->queue.pj + cap);
+            s->queue.cap = (int)cap;
+        }
+    }
     launch_g2p(s->kp, P, s->P[nx], s->perm, (int)s->n, s->G, (float)dt, s->keys, s->dstats, M, s->stream, H,
-               s->mlp ? &mp : nullptr, (float)s->learned_tol, s->keys_sorted);
+               s->mlp ? &mp : nullptr, (float)s->learned_tol, (float)s->learned_abs, s->keys_sorted, s->queue);
     CKLAUNCH();
     if (timed) {
         mark(s, AEP_NUM_PHASES);
@@ -1290,6 +1308,7 @@ aep_status aep_get_stats(aep_solver* s, aep_stats* out) {
     out->learned_accepted = (int64_t)h.learned_ok;
     out->learned_fallbacks = (int64_t)h.learned_rejected;
     out->sort_movers = (int64_t)h.movers;
+    out->learned_exact = (int64_t)h.learned_exact;
     double im = std::ldexp(s->m_max, -s->prm.mass_bits), ip = std::ldexp(s->m_max, -s->prm.momentum_bits);
     out->total_mass = (double)(long long)h.mass * im;
     for (int a = 0; a < 3; ++a) out->total_momentum[a] = (double)(long long)h.mom[a] * ip;
@@ -1323,6 +1342,16 @@ aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance)
     if (m && !(tolerance >= 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_return_map: tolerance >= 0");
     s->mlp = m;
     s->learned_tol = tolerance;
+    s->learned_abs = std::ldexp(1.0, -23);
+    return AEP_OK;
+}
+
+aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_tol) {
+    if (!s) return AEP_INVALID_ARG;
+    if (!(rel_tol >= 0.0) || !(abs_tol >= 0.0))
+        return fail(s, AEP_INVALID_ARG, "aep_set_return_map_bounds: tolerances >= 0");
+    s->learned_tol = rel_tol;
+    s->learned_abs = abs_tol;
     return AEP_OK;
 }
 

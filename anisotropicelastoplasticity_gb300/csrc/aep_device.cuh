@@ -129,10 +129,23 @@ struct DevStats {
     unsigned long long nodes;      // nodes with mass after P2G
     unsigned long long learned_ok;      // learned return maps accepted
     unsigned long long learned_rejected;  // learned outputs replaced by the exact mapping
+    unsigned long long learned_exact;  // constant projections (sand apex, cloth tension) taken exactly
     long long movers;              // particles that changed key (incremental ordering), -1: full sort
     unsigned int force_fp64;       // entries of the force pass's FP64 list (k_force_fp64)
-    unsigned int pad;
+    unsigned int mlp_rows;         // rows queued for the learned return map (k_mlp_finish)
 };
+
+// Rows of the learned return map that the G2P pass queues for k_mlp_finish
+// (plastic snow and sand states whose projection is not a constant): field-major
+// float arrays of `cap` rows, the fields below.
+struct MlpQueue {
+    int32_t* j;   // slot in the new order
+    int32_t* pj;  // slot in the current order
+    float* f;     // [kQueueFields][cap]
+    int cap;
+};
+constexpr int kQU = 0, kQV = 9, kQS = 18, kQSx = 21, kQQ = 24, kQQx = 25, kQFtr = 26;  // U, V, s trial,
+constexpr int kQueueFields = 35;  // s exact, q trial, q exact, F_tr (with track_plastic_F)
 
 // Training-pair harvest from the exact return mapping (plain G2P): records of 8
 // floats [ln s trial sorted desc (3), q, material, ln s_new - ln s trial (3)].
@@ -586,6 +599,15 @@ __device__ __forceinline__ void cloth_project(float r[3], float shear, float sti
             r[1] *= sc;
         }
     }
+}
+
+// Ratio of the friction cap to the trial shear force in cloth_project, in [0, 1]
+// (1 when the shear is within the cap); the projected shear is the trial shear
+// times this ratio.
+__device__ __forceinline__ float cloth_cap_ratio(const float r[3], float shear, float stiffness, float friction) {
+    const float nf = stiffness * (r[2] - 1.0f) * (r[2] - 1.0f);
+    const float sf = shear * sqrtf(r[0] * r[0] + r[1] * r[1]);
+    return sf > friction * nf ? friction * nf / sf : 1.0f;
 }
 
 // Cloth return mapping (HybridSolver.cpp:695-719): new d3 from the QR of [d1 d2 d3].

@@ -24,9 +24,13 @@
 // batch of 16 particles.
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "aep_device.cuh"
 #include "aep_kernels.h"
 #include "aep_mlp.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace aep {
 
@@ -906,25 +910,46 @@ __device__ __forceinline__ void apic_damp(const float C[9], float damp, float Bn
         }
 }
 
-// G2P + APIC + advection + F update + return mapping, one thread per particle
-__device__ __forceinline__ void harvest_record(const Harvest& H, int mat, const float s_tr[3], const float s_new[3],
-                                               float q_old) {
-    const unsigned long long slot = atomicAdd(H.count, 1ull);
-    if ((long long)slot >= H.capacity) return;
-    float ln[3] = {logf(s_tr[0]), logf(s_tr[1]), logf(s_tr[2])}, srt[3];
+// One training record of a plastic state: [ln s (trial, sorted descending), q,
+// material, ln s_projected - ln s].  The sand projection is recomputed in log space
+// on the sorted values, so that the target carries no exp/log rounding; states it
+// sends to the apex (s = 1, a constant the network never predicts) are skipped, and
+// so are sand states within kHarvestMinLn of s = 1, whose ln s carry the FP32
+// rounding of s (2^-24 absolute) as more than 1e-3 of their size.
+constexpr float kHarvestMinLn = 1e-4f;
+__device__ __forceinline__ void harvest_record(const KParams& P, const Harvest& H, int mat, const float s_tr[3],
+                                               const float s_new[3], float q_old) {
+    float ln[3] = {logf(s_tr[0]), logf(s_tr[1]), logf(s_tr[2])}, srt[3], t[3];
     int pm[3];
     sort3_desc(ln, srt, pm);
+    if (mat == kSand) {
+        if (fmaxf(fabsf(srt[0]), fabsf(srt[2])) < kHarvestMinLn) return;
+        t[0] = srt[0]; t[1] = srt[1]; t[2] = srt[2];
+        float qq = q_old;
+        if (dp_project<float>(t, qq, P.sand_h0, P.sand_h1, P.sand_h2, P.sand_h3, P.sand_k) != 2) return;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) t[k] = logf(s_new[pm[k]]);
+    }
+    const unsigned long long slot = atomicAdd(H.count, 1ull);
+    if ((long long)slot >= H.capacity) return;
     float* r = H.buf + 8ull * slot;
     r[0] = srt[0]; r[1] = srt[1]; r[2] = srt[2];
     r[3] = q_old;
     r[4] = (float)mat;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) r[5 + k] = logf(s_new[pm[k]]) - srt[k];
+    for (int k = 0; k < 3; ++k) r[5 + k] = t[k] - srt[k];
 }
 
+// G2P + APIC + advection + F update + return mapping, one thread per particle.
+// kDefer (the learned return map): a plastic snow or sand state whose projection
+// is not a constant is queued with its SVD and exact projection for k_mlp_finish,
+// which writes its F_E, F_P and plastic scalar; the sand apex is taken exactly.
+template <bool kDefer>
 __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
                                              int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
-                                             DevStats* st, Harvest H, const uint32_t* __restrict__ keys_sorted) {
+                                             DevStats* st, Harvest H, const uint32_t* __restrict__ keys_sorted,
+                                             MlpQueue Qu) {
     __shared__ float4 tile_v[kTileNodes], tile_b[kTileNodes];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     int org[3];
@@ -1010,7 +1035,7 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
     float U[9], s[3], V[9];
     float Fe[9], sn[3];
     float sprod = 1.0f;  // prod(s_trial / s_new) for J_P
-    bool used_fp64 = false;
+    bool used_fp64 = false, deferred = false;
     double Ud[9], sd[3], Vd[9];
     bool ok = svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
     if (ok) {
@@ -1018,14 +1043,49 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         const float q_old = q;
         return_map<float>(P, mat, sn, q);
         if (H.buf && (j % H.stride) == 0 && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2]))
-            harvest_record(H, mat, s, sn, q_old);  // plastic states only
-        sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
-        float US[9];
+            harvest_record(P, H, mat, s, sn, q_old);  // plastic states only
+        if (kDefer && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2])) {
+            if (mat == kSand && sn[0] == 1.0f && sn[1] == 1.0f && sn[2] == 1.0f) {
+                cg::coalesced_group g = cg::coalesced_threads();  // the apex: exact, counted
+                if (g.thread_rank() == 0) atomicAdd(&st->learned_exact, (unsigned long long)g.size());
+            } else {
+                cg::coalesced_group g = cg::coalesced_threads();  // warp-aggregated queue append
+                unsigned base = 0;
+                if (g.thread_rank() == 0) base = atomicAdd(&st->mlp_rows, g.size());
+                const int r = (int)(g.shfl(base, 0) + g.thread_rank());
+                if (r < Qu.cap) {
+                    deferred = true;
+                    const long cap = Qu.cap;
+                    float* f = Qu.f + r;
+                    Qu.j[r] = j;
+                    Qu.pj[r] = pj;
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
+                    for (int k = 0; k < 9; ++k) {
+                        f[(kQU + k) * cap] = U[k];
+                        f[(kQV + k) * cap] = V[k];
+                    }
 #pragma unroll
-            for (int c = 0; c < 3; ++c) US[3 * r + c] = U[3 * r + c] * sn[c];
-        mat_mul_bt(US, V, Fe);
+                    for (int a = 0; a < 3; ++a) {
+                        f[(kQS + a) * cap] = s[a];
+                        f[(kQSx + a) * cap] = sn[a];
+                    }
+                    f[kQQ * cap] = q_old;
+                    f[kQQx * cap] = q;
+                    if (P.track_fp)
+#pragma unroll
+                        for (int k = 0; k < 9; ++k) f[(kQFtr + k) * cap] = Ftr[k];
+                }
+            }
+        }
+        if (!deferred) {
+            sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
+            float US[9];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) US[3 * r + c] = U[3 * r + c] * sn[c];
+            mat_mul_bt(US, V, Fe);
+        }
     } else {
         used_fp64 = true;
         double Fd[9];
@@ -1046,7 +1106,8 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         for (int k = 0; k < 9; ++k) Fe[k] = (float)Fed[k];
         atomicAdd(&st->fallbacks, 1ull);
     }
-    if (P.track_fp) {
+    if (deferred) {
+    } else if (P.track_fp) {
         // F_P = V S^-1 U^T F_tr F_P (HS:676)
         float Fp[9], Ft[9];
 #pragma unroll
@@ -1080,11 +1141,12 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         nxt.v[a][j] = vp[a];
     }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        nxt.B[k][j] = Bn[k];
-        nxt.F[k][j] = Fe[k];
+    for (int k = 0; k < 9; ++k) nxt.B[k][j] = Bn[k];
+    if (!deferred) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) nxt.F[k][j] = Fe[k];
+        nxt.plastic[j] = q;
     }
-    nxt.plastic[j] = q;
     nxt.mat[j] = (uint8_t)mat;
     nxt.m[j] = cur.m[pj];
     nxt.vol[j] = cur.vol[pj];
@@ -1131,228 +1193,96 @@ __device__ __forceinline__ void finish_return_map(const KParams& P, const PArray
     nxt.plastic[j] = q;
 }
 
-// the whole return mapping in FP64 (the FP32 SVD met a near-degenerate F_tr)
-__device__ __forceinline__ void return_map_fp64(const KParams& P, const PArrays& nxt, const PArrays& cur, int j,
-                                                int pj, int mat, const float Ftr[9], float q, DevStats* st) {
-    double Fd[9], Ud[9], sd[3], Vd[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Fd[k] = Ftr[k];
-    svd3<double>(Fd, Ud, sd, Vd, 40, 1e-15, 0.0);
-    svd3_complete(Ud, sd);
-    const double s0[3] = {sd[0], sd[1], sd[2]};
-    double qd = q;
-    return_map<double>(P, mat, sd, qd);
-    double US[9], Fed[9];
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) US[3 * r + c] = Ud[3 * r + c] * sd[c];
-    mat_mul_bt(US, Vd, Fed);
-    for (int k = 0; k < 9; ++k) nxt.F[k][j] = (float)Fed[k];
-    float qn = (float)qd;
-    if (P.track_fp) {
-        double Fp[9], Ft[9], Ftd[9], VS[9], M[9], Fpn[9];
-        for (int k = 0; k < 9; ++k) {
-            Fp[k] = cur.Fp[k][pj];
-            Ftd[k] = Ftr[k];
-        }
-        mat_mul(Ftd, Fp, Ft);
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) VS[3 * r + c] = Vd[3 * r + c] / sd[c];
-        mat_mul_bt(VS, Ud, M);
-        mat_mul(M, Ft, Fpn);
-        for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = (float)Fpn[k];
-        if (mat == kSnow) qn = (float)mat_det(Fpn);
-    } else if (mat == kSnow) {
-        qn = (float)(q * ((s0[0] / sd[0]) * (s0[1] / sd[1]) * (s0[2] / sd[2])));
-    }
-    nxt.plastic[j] = qn;
-    atomicAdd(&st->fallbacks, 1ull);
-}
-
 // ===================================================================================
-// G2P with the learned return map: as k_g2p, but the singular-value return mapping
-// of plastic snow and sand states is predicted by the MLP (aep_mlp.cuh) on the
-// tensor cores.  The yield check (the exact mapping, HybridSolver.cpp:626-674)
-// runs first and decides whether a state is plastic; elastic states keep their
-// trial values and never reach the network.  The plastic rows of a block are
-// compacted (in thread order) into 32-row tiles and the block's warps run the
-// MLP on those tiles only.  Each prediction is checked against the exact
-// projection: if the projected log singular values differ by more than `tol`
-// relative to their largest magnitude (absolute floor 1e-5), the exact value is
-// used instead and counted as a fallback.  Persistent: the weights are loaded
-// once per block, which then walks chunks of kLrnThreads particles; every thread
-// runs every chunk, so the block barriers are reached uniformly.
-constexpr int kLrnThreads = 128;
-constexpr int kLrnWarps = kLrnThreads / 32;
-constexpr int kLrnSmemBytes = kMlpSmemBytes + kLrnThreads * kStrideIn * 2 + kLrnThreads * kMlpOut * 4 +
-                              kLrnWarps * 2 * kMlpWarpH * 2;
-static_assert(kLrnWarps * 2 * kMlpWarpH * 2 >= 2 * kTileNodes * 16, "the grid tile must fit the hidden-layer buffers");
-static_assert((kMlpSmemBytes + kLrnThreads * kStrideIn * 2 + kLrnThreads * kMlpOut * 4) % 16 == 0,
-              "the grid tile must be 16-byte aligned");
+// The learned return map of the rows that k_g2p<true> queued: one warp per 32
+// consecutive rows runs the MLP (aep_mlp.cuh) on the tensor cores on the sorted
+// trial log singular values, and each prediction is checked against the exact
+// projection that the G2P pass computed (the point of the yield surface that the
+// flow rule reaches, HybridSolver.cpp:626-674): within max(tol_rel x its largest
+// magnitude, tol_abs) it is kept, otherwise the exact value is used and counted
+// as a fallback.  Then F_E = U diag(s_new) V^T, F_P and the plastic scalar into the
+// new order.  Persistent: the weights are loaded once per block.
+constexpr int kFinThreads = 128;
 
-__global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArrays cur, PArrays nxt,
-                                                             const int32_t* __restrict__ perm, int n, GArrays G,
-                                                             float dt, uint32_t* __restrict__ keys_next,
-                                                             DevStats* st, MlpParams mlp, float tol,
-                                                             const uint32_t* __restrict__ keys_sorted) {
+__global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays cur, PArrays nxt, MlpQueue Qu,
+                                                            DevStats* st, MlpParams mlp, float tol_rel,
+                                                            float tol_abs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_cnt[kLrnWarps];
-    dt = step_dt(P, dt, 1);
+    const int rows = (int)min(st->mlp_rows, (unsigned)Qu.cap);
+    if (rows == 0) return;  // block-uniform
     const MlpSmem W = mlp_smem_carve(smem_raw);
     mlp_load_smem(mlp, W, threadIdx.x, blockDim.x);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __nv_bfloat16* CX = reinterpret_cast<__nv_bfloat16*>(smem_raw + kMlpSmemBytes);  // compacted feature rows
-    float* CY = reinterpret_cast<float*>(CX + kLrnThreads * kStrideIn);             // their outputs
-    unsigned char* const hbase = reinterpret_cast<unsigned char*>(CY + kLrnThreads * kMlpOut);
-    __nv_bfloat16* H0 = reinterpret_cast<__nv_bfloat16*>(hbase) + warp * 2 * kMlpWarpH;
-    __nv_bfloat16* H1 = H0 + kMlpWarpH;
-    // the grid tile of phase A shares the memory of the hidden layers of phase B
-    float4* const tile_v = reinterpret_cast<float4*>(hbase);
-    float4* const tile_b = tile_v + kTileNodes;
     __syncthreads();
-
-    for (long chunk = blockIdx.x; chunk * kLrnThreads < n; chunk += gridDim.x) {
-        const int j = (int)(chunk * kLrnThreads) + threadIdx.x;
-        const bool live = j < n;
-        const int pj = live ? perm[j] : 0;
-        const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
-        const bool active = live && mat != kClothElement;
-        // --- phase A: gather, advection, APIC, F update, SVD, yield check ------------
-        int org[3];
-        tile_origin(P, keys_sorted[chunk * kLrnThreads], org);
-        load_tile(P, org, G.vel, G.vbf, tile_v, tile_b);  // after the last chunk's phase-B barrier
-        const float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
-        int cell[3];
-        float f[3], w[3][4], dw[3][4];
-        locate(P, xp[0], xp[1], xp[2], cell, f);
-        const bool truncated = particle_weights(P, cell, f, w, dw);
-        int base[3] = {cell[0] + 3, cell[1] + 3, cell[2] + 3};
-        uint32_t X[4], Y[4], Z[4];
-        const bool in_tile = tile_offsets(base, org, X, Y, Z);
-        if (!in_tile) stencil_offsets(P, base, X, Y, Z);
-        __syncthreads();
-        bool need = false;  // plastic state whose projection the MLP predicts
-        float U[9], V[9], s[3], srt[3], ex[3], lns[3];
-        int pm[3] = {0, 1, 2};
-        float q = 0.0f, qe = 0.0f, osc = 1.0f;
-        float Ftr[9];
-        if (active) {
-            float xi[3][4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wbase = smem_raw + kMlpSmemBytes + warp * kMlpWarpBytes;
+    __nv_bfloat16* X = reinterpret_cast<__nv_bfloat16*>(wbase);
+    __nv_bfloat16* H0 = X + kMlpWarpX;
+    __nv_bfloat16* H1 = H0 + kMlpWarpH;
+    float* Y = reinterpret_cast<float*>(H1 + kMlpWarpH);
+    const long cap = Qu.cap;
+    unsigned n_ok = 0, n_rej = 0;
+    const int nwarps = gridDim.x * (kFinThreads / 32);
+    for (int t = blockIdx.x * (kFinThreads / 32) + warp; t * 32 < rows; t += nwarps) {  // warp-uniform
+        const int r = t * 32 + lane;
+        const bool live = r < rows;
+        const int rr = live ? r : t * 32;  // a lane past the end repeats the tile's first row
+        const float* f = Qu.f + rr;
+        const int pj = Qu.pj[rr];
+        const int mat = (int)cur.mat[pj];
+        float s[3], lns[3], srt[3];
+        int pm[3];
 #pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-                for (int o = 0; o < 4; ++o) xi[a][o] = ((float)(o - 1) - f[a]) * P.h[a];
-            float vp[3], xs[3], C[9], Gb[9], xn[3], Bn[9];
-            g2p_gather(in_tile ? tile_v : G.vel, in_tile ? tile_b : G.vbf, w, dw, xi, X, Y, Z, vp, C, xs, Gb);
-#pragma unroll
-            for (int a = 0; a < 3; ++a) xn[a] = xp[a] + dt * xs[a];
-            if (truncated) {
-                float s0[3], s1[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    s0[a] = w[a][0] + w[a][1] + w[a][2] + w[a][3];
-                    s1[a] = w[a][0] * xi[a][0] + w[a][1] * xi[a][1] + w[a][2] * xi[a][2] + w[a][3] * xi[a][3];
-                }
-                const float sw = s0[0] * s0[1] * s0[2];
-                const float swx[3] = {s1[0] * s0[1] * s0[2], s0[0] * s1[1] * s0[2], s0[0] * s0[1] * s1[2]};
-#pragma unroll
-                for (int a = 0; a < 3; ++a) xn[a] += xp[a] * (sw - 1.0f) + swx[a];
-            }
-            apic_damp(C, mat == kClothVertex ? P.mesh_damp : P.particle_damp, Bn);
-            // everything but F and the plastic scalar is final here
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                nxt.x[a][j] = xn[a];
-                nxt.v[a][j] = vp[a];
-            }
-#pragma unroll
-            for (int k = 0; k < 9; ++k) nxt.B[k][j] = Bn[k];
-            nxt.mat[j] = (uint8_t)mat;
-            nxt.m[j] = cur.m[pj];
-            nxt.vol[j] = cur.vol[pj];
-            nxt.id[j] = cur.id[pj];
-            int ncell[3];
-            float nfr[3];
-            const bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nfr);
-            keys_next[j] = make_key(P, ncell);
-            if (clamped) atomicAdd(&st->out_of_domain, 1ull);
-            if (mat == kClothVertex) {
-#pragma unroll
-                for (int k = 0; k < 9; ++k) nxt.F[k][j] = cur.F[k][pj];
-                nxt.plastic[j] = cur.plastic[pj];
-            } else {
-                float F[9], GF[9];
-#pragma unroll
-                for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
-                mat_mul(Gb, F, GF);
-#pragma unroll
-                for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
-                q = cur.plastic[pj];
-                if (svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f)) {
-                    ex[0] = s[0]; ex[1] = s[1]; ex[2] = s[2];
-                    qe = q;
-                    return_map<float>(P, mat, ex, qe);
-                    need = ex[0] != s[0] || ex[1] != s[1] || ex[2] != s[2];
-                    if (need) {
-                        lns[0] = logf(s[0]); lns[1] = logf(s[1]); lns[2] = logf(s[2]);
-                        sort3_desc(lns, srt, pm);
-                    } else {  // elastic: F_E = F_tr, q unchanged (snow J_P too)
-                        finish_return_map(P, nxt, cur, j, pj, mat, Ftr, U, V, s, s, q, 1.0f);
-                    }
-                } else {
-                    return_map_fp64(P, nxt, cur, j, pj, mat, Ftr, q, st);
-                }
-            }
+        for (int a = 0; a < 3; ++a) {
+            s[a] = f[(kQS + a) * cap];
+            lns[a] = logf(s[a]);
         }
-        // --- phase B: the MLP on the block's plastic rows, compacted -----------------
-        const unsigned bal = __ballot_sync(0xffffffffu, need);
-        if (lane == 0) s_cnt[warp] = __popc(bal);
-        __syncthreads();
-        int row = 0, total = 0;
+        sort3_desc(lns, srt, pm);
+        float q = f[kQQ * cap];
+        const float osc = mlp_features(srt, q, mat, X + lane * kStrideIn);
+        mlp_forward_warp(W, X, H0, H1, Y, lane);
+        if (live) {
+            float pred_ln[3], ex[3];
 #pragma unroll
-        for (int w = 0; w < kLrnWarps; ++w) {
-            row += w < warp ? s_cnt[w] : 0;
-            total += s_cnt[w];
-        }
-        row += __popc(bal & ((1u << lane) - 1u));
-        const int tiles = (total + 31) >> 5;
-        if (need) osc = mlp_features(srt, q, mat, CX + row * kStrideIn);
-        if ((int)threadIdx.x >= total && (int)threadIdx.x < 32 * tiles)
-            mlp_features(srt, 0.0f, 0, CX + threadIdx.x * kStrideIn);  // zero rows of the last tile
-        __syncthreads();
-        for (int t = warp; t < tiles; t += kLrnWarps)
-            mlp_forward_warp(W, CX + 32 * t * kStrideIn, H0, H1, CY + 32 * t * kMlpOut, lane);
-        __syncthreads();
-        // --- phase C: check the prediction, F_E = U diag(s_new) V^T ------------------
-        if (need) {
-            float pred_ln[3];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) pred_ln[pm[k]] = srt[k] + CY[row * kMlpOut + k] / osc;
-            // relative residual of the projected log singular values: the stress is
-            // nearly linear in them, so this bounds the relative stress error
+            for (int k = 0; k < 3; ++k) pred_ln[pm[k]] = srt[k] + Y[lane * kMlpOut + k] / osc;
             float err = 0.0f, ref = 0.0f;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
+                ex[a] = f[(kQSx + a) * cap];
                 const float le = logf(ex[a]);
                 err = fmaxf(err, fabsf(pred_ln[a] - le));
                 ref = fmaxf(ref, fabsf(le));
             }
+            const float qe = f[kQQx * cap];
             float sn[3];
-            if (err <= tol * fmaxf(ref, 1e-5f)) {
+            if (err <= fmaxf(tol_rel * ref, tol_abs)) {
 #pragma unroll
                 for (int a = 0; a < 3; ++a) sn[a] = expf(pred_ln[a]);
                 if (mat == kSand && qe != q) {  // q grows by the projection distance
                     const float d0 = pred_ln[0] - lns[0], d1 = pred_ln[1] - lns[1], d2 = pred_ln[2] - lns[2];
                     q += sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
                 }
-                atomicAdd(&st->learned_ok, 1ull);
+                ++n_ok;
             } else {
                 sn[0] = ex[0]; sn[1] = ex[1]; sn[2] = ex[2];
                 q = qe;
-                atomicAdd(&st->learned_rejected, 1ull);
+                ++n_rej;
             }
-            finish_return_map(P, nxt, cur, j, pj, mat, Ftr, U, V, s, sn, q,
+            float U[9], V[9], Ftr[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                U[k] = f[(kQU + k) * cap];
+                V[k] = f[(kQV + k) * cap];
+                Ftr[k] = P.track_fp ? f[(kQFtr + k) * cap] : 0.0f;
+            }
+            finish_return_map(P, nxt, cur, Qu.j[r], pj, mat, Ftr, U, V, s, sn, q,
                               (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]));
         }
+    }
+    n_ok = __reduce_add_sync(0xffffffffu, n_ok);
+    n_rej = __reduce_add_sync(0xffffffffu, n_rej);
+    if (lane == 0) {
+        if (n_ok) atomicAdd(&st->learned_ok, (unsigned long long)n_ok);
+        if (n_rej) atomicAdd(&st->learned_rejected, (unsigned long long)n_rej);
     }
 }
 
@@ -1364,12 +1294,13 @@ __global__ void __launch_bounds__(kLrnThreads, 3) k_g2p_learned(KParams P, PArra
 // d3 += dt grad v^bf d3 (HS:584-607), then the QR return mapping (HS:686-720).
 // With an MLP (use_mlp), the cloth return mapping of plastic elements is predicted
 // by the learned map (cloth rows of the same network) and checked against the
-// exact projection as in k_g2p_learned; the warp runs the network when any of its
+// exact projection as in k_mlp_finish; the warp runs the network when any of its
 // elements is plastic.  With a harvest buffer, plastic elements record
 // [r13, r23, r33 - 1, 0, 2, projected - trial (3)].
 __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArrays nxt, GArrays G, MeshArrays M,
                                                    float dt, uint32_t* __restrict__ keys_next, DevStats* st,
-                                                   Harvest H, MlpParams mlp, int use_mlp, float tol) {
+                                                   Harvest H, MlpParams mlp, int use_mlp, float tol_rel,
+                                                   float tol_abs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = e < M.nf;
@@ -1380,8 +1311,8 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
         mlp_load_smem(mlp, W, threadIdx.x, blockDim.x);
         __syncthreads();
     }
-    float Q[9], r[3] = {0, 0, 1}, rp[3] = {0, 0, 1};
-    bool plastic = false;
+    float Q[9], r[3] = {0, 0, 1}, rp[3] = {0, 0, 1}, cap = 0.0f;
+    bool plastic = false, tension = false;
     int j = 0, pc = 0;
     if (live) {
         const int id = M.ebase + e;
@@ -1428,11 +1359,19 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
         rp[0] = r[0]; rp[1] = r[1]; rp[2] = r[2];
         cloth_project(rp, M.shear, M.stiffness, M.friction);
         plastic = rp[0] != r[0] || rp[1] != r[1] || rp[2] != r[2];
-        if (H.buf && plastic && (e % H.stride) == 0) {
+        if (plastic && r[2] > 1.0f) {  // tension: the constant r = e3, taken exactly
+            plastic = false;
+            tension = true;
+        }
+        cap = cloth_cap_ratio(r, M.shear, M.stiffness, M.friction);
+        // records of states within 1e-5 of r = e3 would carry the FP32 rounding of
+        // r33 as more than 1e-2 of their size: skipped
+        if (H.buf && plastic && (e % H.stride) == 0 &&
+            fmaxf(fmaxf(fabsf(r[0]), fabsf(r[1])), fabsf(r[2] - 1.0f)) >= 1e-5f) {
             const unsigned long long slot = atomicAdd(H.count, 1ull);
             if ((long long)slot < H.capacity) {
                 float* o = H.buf + 8ull * slot;
-                o[0] = r[0]; o[1] = r[1]; o[2] = r[2] - 1.0f; o[3] = 0.0f; o[4] = (float)kMlpCloth;
+                o[0] = r[0]; o[1] = r[1]; o[2] = r[2] - 1.0f; o[3] = cap; o[4] = (float)kMlpCloth;
                 o[5] = rp[0] - r[0]; o[6] = rp[1] - r[1]; o[7] = rp[2] - r[2];
             }
         }
@@ -1466,9 +1405,10 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
         __nv_bfloat16* MH0 = MX + kMlpWarpX;
         __nv_bfloat16* MH1 = MH0 + kMlpWarpH;
         float* MY = reinterpret_cast<float*>(MH1 + kMlpWarpH);
+        bool ok = false;
         if (__any_sync(0xffffffffu, plastic)) {  // warp-uniform
             const float in[3] = {r[0], r[1], r[2] - 1.0f};
-            const float sc = mlp_features(in, 0.0f, plastic ? kMlpCloth : 0, MX + lane * kStrideIn);
+            const float sc = mlp_features(in, cap, plastic ? kMlpCloth : 0, MX + lane * kStrideIn);
             mlp_forward_warp(W, MX, MH0, MH1, MY, lane);
             if (plastic) {
                 // residual relative to the projected shear and normal strain
@@ -1480,13 +1420,20 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
                     err = fmaxf(err, fabsf(pred[a] - rp[a]));
                 }
                 const float ref = fmaxf(fmaxf(fabsf(rp[0]), fabsf(rp[1])), fabsf(rp[2] - 1.0f));
-                if (err <= tol * fmaxf(ref, 1e-5f)) {
+                ok = err <= fmaxf(tol_rel * ref, tol_abs);
+                if (ok) {
                     rp[0] = pred[0]; rp[1] = pred[1]; rp[2] = pred[2];
-                    atomicAdd(&st->learned_ok, 1ull);
-                } else {
-                    atomicAdd(&st->learned_rejected, 1ull);
                 }
             }
+        }
+        // warp-aggregated counters (every lane of the warp is here)
+        const unsigned b_ok = __ballot_sync(0xffffffffu, plastic && ok);
+        const unsigned b_rej = __ballot_sync(0xffffffffu, plastic && !ok);
+        const unsigned b_ex = __ballot_sync(0xffffffffu, tension);
+        if (lane == 0) {
+            if (b_ok) atomicAdd(&st->learned_ok, (unsigned long long)__popc(b_ok));
+            if (b_rej) atomicAdd(&st->learned_rejected, (unsigned long long)__popc(b_rej));
+            if (b_ex) atomicAdd(&st->learned_exact, (unsigned long long)__popc(b_ex));
         }
     }
     if (live) {
@@ -1790,27 +1737,30 @@ void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s) {
 }
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
                 const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s,
-                const Harvest& H, const MlpParams* mlp, float learned_tol, const uint32_t* keys_sorted) {
+                const Harvest& H, const MlpParams* mlp, float tol_rel, float tol_abs, const uint32_t* keys_sorted,
+                const MlpQueue& Qu) {
     if (n > 0) {
         if (mlp) {
-            const int smem = kLrnSmemBytes;
-            cudaFuncSetAttribute(k_g2p_learned, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            k_g2p<true><<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H, keys_sorted,
+                                                          Qu);
+            const int smem = kMlpSmemBytes + (kFinThreads / 32) * kMlpWarpBytes;
+            cudaFuncSetAttribute(k_mlp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             int dev = 0, sms = 0, per_sm = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_g2p_learned, kLrnThreads, smem);
-            const int blocks = std::min(blocks_for(n, kLrnThreads), std::max(1, sms * std::max(per_sm, 1)));
-            k_g2p_learned<<<blocks, kLrnThreads, smem, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, *mlp,
-                                                            learned_tol, keys_sorted);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_finish, kFinThreads, smem);
+            const int blocks = std::min(blocks_for(Qu.cap, kFinThreads), std::max(1, sms * std::max(per_sm, 1)));
+            k_mlp_finish<<<blocks, kFinThreads, smem, s>>>(P, cur, nxt, Qu, st, *mlp, tol_rel, tol_abs);
         } else {
-            k_g2p<<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H, keys_sorted);
+            k_g2p<false><<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H,
+                                                           keys_sorted, Qu);
         }
     }
     if (M.nf > 0) {
         const int smem = mlp ? kMlpSmemBytes + 4 * kMlpWarpBytes : 0;
         if (mlp) cudaFuncSetAttribute(k_cloth_g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         k_cloth_g2p<<<blocks_for(M.nf, 128), 128, smem, s>>>(P, cur, nxt, G, M, dt, keys_next, st, H,
-                                                             mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, learned_tol);
+                                                             mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, tol_rel, tol_abs);
     }
 }
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,

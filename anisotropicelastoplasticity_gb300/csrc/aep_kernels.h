@@ -19,7 +19,8 @@ void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_f
 void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s);
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
                 const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s,
-                const Harvest& H, const MlpParams* mlp, float learned_tol, const uint32_t* keys_sorted);
+                const Harvest& H, const MlpParams* mlp, float tol_rel, float tol_abs, const uint32_t* keys_sorted,
+                const MlpQueue& queue);
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s);
 void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s,

@@ -5,8 +5,9 @@
 // sorted descending (3; normalised for sand, scaled by kLnScale for snow, see
 // mlp_features), the sand plastic amount q (1), and the material one-hot (snow,
 // sand, cloth) (3); padded to 16 columns.  Cloth elements use the same network
-// on (r13, r23, r33 - 1) of their QR factor.  Output: the correction (ln s_projected -
-// ln s_trial) in the same order and the same scaling (3 of 8).
+// on (r13, r23, r33 - 1) of their QR factor, normalised, with the ratio of the
+// friction cap to the trial shear force in column 3.  Output: the correction
+// (ln s_projected - ln s_trial) in the same order and the same scaling (3 of 8).
 // The return mappings it stands in for (HybridSolver.cpp:626-674) are invariant
 // under permutations of the singular values, so sorting canonicalises the input.
 //
@@ -171,27 +172,31 @@ __device__ __forceinline__ void mlp_forward_warp(const MlpSmem& W, __nv_bfloat16
 }
 
 constexpr int kMlpCloth = 2;        // material code of cloth element records
-constexpr float kClothScale = 50.0f;  // cloth features and outputs are R entries times this
+constexpr float kQScale = 100.0f;   // sand plastic amount feature scale
 
-// Feature row of one particle and the scale of its output.  Sand: the Drucker-Prager
-// projection onto a cone is positively homogeneous in ln s, so the sorted trial
-// log singular values are normalised by their norm r and the network predicts the
-// correction divided by r.  Snow: the clamp bounds are absolute, so ln s and the
-// correction are scaled by kLnScale.  Returns the factor that maps a correction to
-// the network's output (sand: 1/r, snow: kLnScale).
-// Cloth (mat == kMlpCloth): the input is (r13, r23, r33 - 1) of the QR factor of the
-// element directions, the output the change of (r13, r23, r33) by the cloth return
-// mapping (HybridSolver.cpp:701-717), both scaled by kClothScale; one-hot column 6.
+// Feature row of one state and the scale of its output; returns the factor that
+// maps a correction to the network's output.
+// Sand (mat 1): the Drucker-Prager projection onto a cone is positively homogeneous
+// in ln s, so the sorted trial log singular values are normalised by their norm r
+// and the network predicts the correction divided by r; column 3 is the plastic
+// amount q times kQScale (it sets the cone's opening through the hardening).
+// Snow (mat 0): the clamp bounds are absolute, so ln s and the correction are
+// scaled by kLnScale.
+// Cloth (mat kMlpCloth): the input is u = (r13, r23, r33 - 1) / rho, rho = |(r13,
+// r23, r33 - 1)|, of the QR factor of the element directions; column 3 (`q`) is the
+// ratio of the friction cap to the trial shear force (HybridSolver.cpp:707-716),
+// clamped to [0, 1]; the output is the change of (r13, r23, r33) divided by rho.
+// Constant projections (the sand apex, cloth in tension) never reach the network.
 __device__ __forceinline__ float mlp_features(const float ln_sorted[3], float q, int mat, __nv_bfloat16* row) {
-    float sc = mat == kMlpCloth ? kClothScale : kLnScale;
-    if (mat == 1) {
+    float sc = kLnScale;
+    if (mat != 0) {
         const float r = sqrtf(ln_sorted[0] * ln_sorted[0] + ln_sorted[1] * ln_sorted[1] + ln_sorted[2] * ln_sorted[2]);
-        sc = 1.0f / fmaxf(r, 1e-20f);
+        sc = 1.0f / fmaxf(r, 1e-30f);
     }
     row[0] = __float2bfloat16(ln_sorted[0] * sc);
     row[1] = __float2bfloat16(ln_sorted[1] * sc);
     row[2] = __float2bfloat16(ln_sorted[2] * sc);
-    row[3] = __float2bfloat16(mat == 1 ? q : 0.0f);
+    row[3] = __float2bfloat16(mat == 1 ? q * kQScale : mat == kMlpCloth ? q : 0.0f);
     row[4] = __float2bfloat16(mat == 0 ? 1.0f : 0.0f);
     row[5] = __float2bfloat16(mat == 1 ? 1.0f : 0.0f);
     row[6] = __float2bfloat16(mat == kMlpCloth ? 1.0f : 0.0f);

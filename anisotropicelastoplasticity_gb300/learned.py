@@ -5,7 +5,8 @@ kernels from (trial, projected) pairs that the exact return mapping produces
 computation runs in libaep.so.
 
 Record layout (8 float32): [ln s0, ln s1, ln s2 (trial, sorted descending), q,
-material, d0, d1, d2], d = ln s_projected - ln s_trial.
+material, d0, d1, d2], d = ln s_projected - ln s_trial; cloth element records
+(material 2): [r13, r23, r33 - 1, cap ratio, 2, change of (r13, r23, r33)].
 """
 from __future__ import annotations
 

@@ -86,12 +86,14 @@ def sand_column(n: int = 524288, res: int = 128, seed: int = 1) -> Scene:
 def snow_sand_collision(n: int = 2097152, res: int = 256, seed: int = 3) -> Scene:
     """Mixed snow and sand at scale: half snow (snow-block material, density 400), half
     sand (sand-column material, density 2200) in two cubes of 8 particles per cell,
-    placed at random (seed 3) and colliding at relative speed 2; grid 256^3."""
+    colliding at relative speed 2; grid 256^3.  The cubes are placed face to face
+    along x (the impact starts at the first step), each shifted at random (seed 3)
+    by up to +-0.02 in y and z."""
     rng = np.random.default_rng(seed)
     nh = n // 2
     side = (nh / 8.0) ** (1.0 / 3.0) / res
-    c_snow = np.array([0.30, 0.50, 0.30]) + 0.04 * (rng.random(3) - 0.5)
-    c_sand = np.array([0.70, 0.50, 0.30]) + 0.04 * (rng.random(3) - 0.5)
+    c_snow = np.array([0.5 - side / 2, 0.50, 0.30]) + 0.04 * (rng.random(3) - 0.5) * np.array([0, 1, 1])
+    c_sand = np.array([0.5 + side / 2, 0.50, 0.30]) + 0.04 * (rng.random(3) - 0.5) * np.array([0, 1, 1])
     xs = _block(rng, nh, c_snow - side / 2, c_snow + side / 2)
     xd = _block(rng, n - nh, c_sand - side / 2, c_sand + side / 2)
     x = np.concatenate([xs, xd])

@@ -506,10 +506,15 @@ class HybridSolver:
         self._check(self._lib.aep_get_harvest_count(self._h, C.byref(cnt)))
         return cnt.value
 
-    def set_return_map(self, mlp=None, tolerance: float = 1e-3):
-        """Use a trained ReturnMapMLP (None: the exact mapping of the reference)."""
+    def set_return_map(self, mlp=None, tolerance: float = 1e-3, abs_tolerance: float | None = None):
+        """Use a trained ReturnMapMLP (None: the exact mapping of the reference).  A
+        prediction is kept when it is within max(tolerance x |exact|, abs_tolerance)
+        of the exact projection (abs_tolerance None: 2^-23, the FP32 resolution of
+        ln s near 1); otherwise the exact value is used and counted as a fallback."""
         self._mlp_ref = mlp
         self._check(self._lib.aep_set_return_map(self._h, mlp.handle if mlp is not None else None, tolerance))
+        if abs_tolerance is not None:
+            self._check(self._lib.aep_set_return_map_bounds(self._h, tolerance, abs_tolerance))
 
     def set_stream(self, cuda_stream_ptr: int | None):
         """Order the solver's work on an external cudaStream_t (e.g. torch.cuda.Stream.cuda_stream)."""
@@ -531,5 +536,6 @@ class HybridSolver:
         return dict(steps=s.steps, num_particles=s.num_particles, active_blocks=s.active_blocks,
                     out_of_domain=s.out_of_domain, fp64_fallbacks=s.fp64_fallbacks, overflow=s.overflow,
                     active_nodes=s.active_nodes, learned_accepted=s.learned_accepted,
-                    learned_fallbacks=s.learned_fallbacks, sort_movers=s.sort_movers,
+                    learned_fallbacks=s.learned_fallbacks, learned_exact=s.learned_exact,
+                    sort_movers=s.sort_movers,
                     total_mass=s.total_mass, total_momentum=list(s.total_momentum))

@@ -138,7 +138,9 @@ typedef struct aep_stats {
     int64_t learned_fallbacks;  /* learned outputs replaced by the exact mapping         */
     int64_t sort_movers;        /* particles that changed cell key in the last ordering,
                                    -1 when it was a full radix sort                      */
-    double reserved[4];
+    int64_t learned_exact;      /* plastic states with a constant projection (sand apex,
+                                   cloth in tension), taken exactly by the learned path  */
+    double reserved[3];
 } aep_stats;
 
 /* ---- version / defaults ------------------------------------------------------- */
@@ -391,11 +393,18 @@ aep_status aep_set_harvest(aep_solver* s, float* d_records, int64_t capacity, in
 /* Number of records written so far (capped at the capacity). */
 aep_status aep_get_harvest_count(aep_solver* s, int64_t* count);
 /* Use the learned return map in later steps (NULL: the exact mapping).  Every
- * prediction is checked in the kernel against the exact mapping; if the projected
- * log singular values differ by more than `tolerance` times their largest
- * magnitude (absolute floor 1e-5), the exact value is used
- * (aep_stats.learned_fallbacks).  The handle must outlive its use.             */
+ * prediction is checked in the kernel against the exact projection (the point of
+ * the yield surface that the flow rule reaches); if the projected log singular
+ * values (cloth: r13, r23, r33) differ from it by more than
+ * max(tolerance x their largest magnitude, 2^-23), the exact value is used
+ * (aep_stats.learned_fallbacks).  Constant projections (sand apex, cloth in
+ * tension) are taken exactly (aep_stats.learned_exact).  The handle must outlive
+ * its use.                                                                     */
 aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance);
+/* The two bounds of that check: relative (rel_tol) and absolute (abs_tol, in
+ * ln-strain units; 2^-23 after aep_set_return_map, the FP32 resolution of ln s
+ * near s = 1).  A residual bound of 1e-4 is rel_tol = 0, abs_tol = 1e-4.       */
+aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_tol);
 
 /* ---- particle-to-grid without allocation --------------------------------------------- */
 

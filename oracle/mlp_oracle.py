@@ -10,8 +10,9 @@ pin against central finite differences.
 Packed parameters (9928 floats): W1^T [64][16], W2^T [64][64], W3^T [64][64],
 W4^T [8][64], b1 [64], b2 [64], b3 [64], b4 [8].  Records: [ln s0, ln s1, ln s2,
 q, material, d0, d1, d2] (material 0 snow, 1 sand); cloth records (material 2)
-carry [r13, r23, r33 - 1, 0, 2, change of (r13, r23, r33)].  Features and targets
-are scaled per record (sand by 1/|ln s|, snow and cloth by 50), as the kernels do
+carry [r13, r23, r33 - 1, cap ratio, 2, change of (r13, r23, r33)].  Features and
+targets are scaled per record (sand and cloth by 1/|first three|, snow by 50;
+column 3 is q x 100 for sand, the cap ratio for cloth), as the kernels do
 (aep_mlp.cuh mlp_features).
 """
 from __future__ import annotations
@@ -19,6 +20,7 @@ from __future__ import annotations
 import numpy as np
 
 LN_SCALE = 50.0
+Q_SCALE = 100.0
 LAYOUT = [("w1t", (64, 16)), ("w2t", (64, 64)), ("w3t", (64, 64)), ("w4t", (8, 64)),
           ("b1", (64,)), ("b2", (64,)), ("b3", (64,)), ("b4", (8,))]
 
@@ -45,14 +47,14 @@ def bf16(x):
 
 
 def scales(rec):
-    """Per-record scaling of features and outputs: sand 1/|ln s| (the cone projection
-    is positively homogeneous), snow 50."""
+    """Per-record scaling of features and outputs: sand and cloth 1/|first three|
+    (the cone projection is positively homogeneous), snow 50."""
     rec = np.asarray(rec, np.float64)
     ln = rec[:, 0:3].astype(np.float32)
     r = np.sqrt((ln * ln).sum(1, dtype=np.float32)).astype(np.float32)
-    sand = rec[:, 4].astype(int) == 1
+    scaled = rec[:, 4].astype(int) != 0
     sc = np.full(len(rec), np.float32(LN_SCALE), np.float32)
-    sc[sand] = np.float32(1.0) / np.maximum(r[sand], np.float32(1e-20))
+    sc[scaled] = np.float32(1.0) / np.maximum(r[scaled], np.float32(1e-30))
     return sc
 
 
@@ -63,7 +65,8 @@ def features(rec, rnd=True):
     sc = scales(rec)
     X[:, 0:3] = rec[:, 0:3].astype(np.float32) * sc[:, None]
     mat = rec[:, 4].astype(int)
-    X[:, 3] = np.where(mat == 1, rec[:, 3].astype(np.float32), 0.0)
+    q = rec[:, 3].astype(np.float32)
+    X[:, 3] = np.where(mat == 1, q * np.float32(Q_SCALE), np.where(mat == 2, q, 0.0))
     X[:, 4] = (mat == 0)
     X[:, 5] = (mat == 1)
     X[:, 6] = (mat == 2)

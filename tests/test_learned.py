@@ -104,11 +104,23 @@ def test_gpu_forward_matches_oracle():
     assert np.abs(out.cpu().numpy() - ref).max() < 2e-4 * max(np.abs(ref).max(), 1e-3)
 
 
+def _strained(sc, seed):
+    """The scene with +-1% random elastic strain: every state carries stress from the
+    first step, and the plastic ones sit well above the FP32 resolution of ln s."""
+    ps = sc.particles
+    rng = np.random.default_rng(seed)
+    ps.elastic_deformation_gradients = np.eye(3) + 0.01 * rng.standard_normal((len(ps), 3, 3))
+    return sc
+
+
 def _harvest_small(torch):
     from anisotropicelastoplasticity_gb300.learned import harvest_records
 
-    recs = [harvest_records(scenes.snow_block(n=4096, res=32, seed=1), steps=40, capacity=200000, stride=1),
-            harvest_records(scenes.sand_column(n=12000, res=32, seed=2), steps=40, capacity=400000, stride=1)]
+    # the snow block meets the ground after ~1,750 steps of 1e-4 s: harvest its impact
+    recs = [harvest_records(scenes.snow_block(n=4096, res=32, seed=1), steps=200, capacity=100000, stride=1,
+                            warm_steps=1650),
+            harvest_records(_strained(scenes.sand_column(n=12000, res=32, seed=2), 7), steps=40, capacity=200000,
+                            stride=1)]
     return torch.cat(recs)
 
 
@@ -123,6 +135,11 @@ def test_training_reduces_loss_on_harvested_pairs():
     host = rec.cpu().numpy()
     assert np.all(np.isfinite(host))
     assert np.all(np.abs(host[:, 5:8]).max(axis=1) > 0)  # only projected (plastic) states are kept
+    mat = host[:, 4].astype(int)
+    assert (mat == 0).sum() > 1000 and (mat == 1).sum() > 1000
+    # no sand apex (projection to ln s = 0, a constant the network never predicts)
+    sand = host[mat == 1]
+    assert np.all(np.abs(sand[:, 0:3] + sand[:, 5:8]).max(axis=1) > 0)
     m = ReturnMapMLP(seed=3)
     _, loss0 = m.gradient(rec.data_ptr(), n)
     loss1 = m.train(rec.data_ptr(), n, steps=1500, batch=4096, lr=2e-3, lr_final=2e-5)
@@ -154,17 +171,22 @@ def test_learned_step_matches_oracle_and_training_gains():
     trained = ReturnMapMLP(seed=3)
     trained.train(rec.data_ptr(), len(rec), steps=2000, batch=4096, lr=2e-3, lr_final=2e-5)
     untrained = ReturnMapMLP(seed=3)
-    sc = scenes.sand_column(n=12000, res=32, seed=5)
+    strained = _strained(scenes.sand_column(n=12000, res=32, seed=5), 8)
     steps = 10
-    s_tr, acc_tr, fb_tr = _learned_run(trained, sc, steps)
-    s_un, acc_un, fb_un = _learned_run(untrained, sc, steps)
     # what training gains: the share of plastic states whose prediction passes the
-    # in-kernel residual check (relative 1e-3) instead of falling back
+    # in-kernel check against the exact projection (here within 1e-2 of its
+    # magnitude) instead of falling back
+    _, acc_tr, fb_tr = _learned_run(trained, strained, steps, tol=1e-2)
+    _, acc_un, fb_un = _learned_run(untrained, strained, steps, tol=1e-2)
     rate_tr = acc_tr / max(acc_tr + fb_tr, 1)
     rate_un = acc_un / max(acc_un + fb_un, 1)
-    assert acc_tr + fb_tr > 0 and acc_un + fb_un == acc_tr + fb_tr
+    assert acc_tr + fb_tr > 1000 and acc_un + fb_un > 1000
     assert rate_tr > rate_un + 0.3, (rate_tr, rate_un)
-    # the learned path stays within its tolerance of the FP64 oracle step
+    # the learned path (default check, 1e-3) stays within its tolerance of the FP64
+    # oracle step on the column at rest
+    sc = scenes.sand_column(n=12000, res=32, seed=5)
+    s_tr, acc, fb = _learned_run(trained, sc, steps)
+    assert acc + fb > 0
     o = Oracle(sc.grid, sc.params)
     o.set_particle_system(sc.particles)
     o.set_level_set(sc.levelset)
