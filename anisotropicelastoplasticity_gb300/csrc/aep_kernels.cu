@@ -91,17 +91,27 @@ __device__ __forceinline__ unsigned run_heads(unsigned hmask, int l, uint32_t ke
     return __ballot_sync(hmask, head) >> (threadIdx.x & 16);
 }
 
+// The block's 512 particles (8 half-warps x 64) mostly share one 4x4x4 cell
+// block; the runs whose stencil lies in the 2x2x2 node blocks from that block
+// (the grid tile of G2P) are summed into a fixed-point copy of the tile in shared
+// memory, which is added to the grid once per node at the end; other runs add
+// to the grid directly.  Integer sums: the result does not depend on the order.
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                      const int32_t* __restrict__ perm, int n, GArrays G,
                                                      int32_t* __restrict__ slot_of, int32_t* __restrict__ curidx_of) {
     __shared__ float4 sm4[(kP2GThreads / 16) * kP2GRegion];
+    __shared__ unsigned long long tacc[4 * kTileNodes];  // [channel][tile node]
     const int hw = threadIdx.x >> 4, l = threadIdx.x & 15;
     float4* const region = sm4 + hw * kP2GRegion;
     const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
     const int ox = l & 3, oy = l >> 2;
-    const long chunk0 = ((long)blockIdx.x * (kP2GThreads / 16) + hw) * kP2GChunk;
-    if (chunk0 >= n) return;  // uniform per half-warp
-    const int cnt_total = (int)min((long)kP2GChunk, (long)n - chunk0);
+    const long blk0 = (long)blockIdx.x * (kP2GThreads / 16) * kP2GChunk;
+    const long chunk0 = blk0 + (long)hw * kP2GChunk;
+    const int cnt_total = (int)max(0L, min((long)kP2GChunk, (long)n - chunk0));  // uniform per half-warp
+    int org[3];
+    tile_origin(P, keys[blk0], org);
+    for (int i = threadIdx.x; i < 4 * kTileNodes; i += kP2GThreads) tacc[i] = 0ull;
+    __syncthreads();
 
     float am[4] = {0, 0, 0, 0}, ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     uint32_t run_key = kInvalidKey;
@@ -126,6 +136,23 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
         if (l == 5) mf[1] += run_T - S;
         run_T = 0;
         int x = rb[0] + ox, y = rb[1] + oy;
+        if ((rb[0] >> 2) == org[0] && (rb[1] >> 2) == org[1] && (rb[2] >> 2) == org[2]) {  // half-warp-uniform
+            const int tx = x - 4 * org[0], ty = y - 4 * org[1];
+            const int txy = (tx >> 2) * 64 + (tx & 3) + (ty >> 2) * 128 + ((ty & 3) << 2);
+#pragma unroll
+            for (int oz = 0; oz < 4; ++oz) {
+                if (mf[oz] != 0) {
+                    const int tz = rb[2] + oz - 4 * org[2];
+                    unsigned long long* a = tacc + txy + (tz >> 2) * 256 + ((tz & 3) << 4);
+                    atomicAdd(a, (unsigned long long)mf[oz]);
+                    atomicAdd(a + kTileNodes, to_fixed(ax[oz], P.mom_scale));
+                    atomicAdd(a + 2 * kTileNodes, to_fixed(ay[oz], P.mom_scale));
+                    atomicAdd(a + 3 * kTileNodes, to_fixed(az[oz], P.mom_scale));
+                }
+                am[oz] = ax[oz] = ay[oz] = az[oz] = 0.0f;
+            }
+            return;
+        }
 #pragma unroll
         for (int oz = 0; oz < 4; ++oz) {
             if (mf[oz] != 0) {
@@ -228,6 +255,19 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
         __syncwarp(hmask);
     }
     flush();
+    __syncthreads();
+    // the tile into the grid, one atomic per nonzero node and channel
+    for (int i = threadIdx.x; i < kTileNodes; i += kP2GThreads) {
+        const int t = i >> 6;
+        const uint32_t gblk = (uint32_t)(((org[2] + (t >> 2)) * P.nb[1] + org[1] + ((t >> 1) & 1)) * P.nb[0] + org[0] +
+                                         (t & 1));
+        unsigned long long* a = G.acc + 4ull * ((gblk << 6) | (uint32_t)(i & 63));
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const unsigned long long v = tacc[c * kTileNodes + i];
+            if (v != 0ull) atomicAdd(a + c, v);
+        }
+    }
 }
 
 // ===================================================================================
@@ -1209,7 +1249,7 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
                                                             float tol_abs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int rows = (int)min(st->mlp_rows, (unsigned)Qu.cap);
-    if (rows == 0) return;  // block-uniform
+    if ((long)blockIdx.x * kFinThreads >= rows) return;  // no tile for this block (block-uniform)
     const MlpSmem W = mlp_smem_carve(smem_raw);
     mlp_load_smem(mlp, W, threadIdx.x, blockDim.x);
     __syncthreads();

@@ -1,8 +1,10 @@
 // aep_mlp.cu -- training and batched inference of the learned return map
 // (see aep_mlp.cuh).  Everything runs on the device with hand-written kernels:
 //   k_mlp_train_tile : forward + backward of 64 training rows per block on the tensor
-//                      cores (mma.sync bf16, f32 accumulation); weight and bias
-//                      gradients are added to one f32 gradient vector
+//                      cores (mma.sync bf16, f32 accumulation); each block writes its
+//                      weight and bias gradients to its own row of a partial array
+//   k_mlp_reduce     : sums the partial rows in block order (training is
+//                      deterministic: the same records give the same parameters)
 //   k_mlp_adam       : Adam on the f32 master parameters, refreshes the bf16 copies
 //   k_mlp_infer      : batched forward pass (32 rows per warp), as used inside G2P
 // Training records (harvested from the exact return mapping where it changed the
@@ -10,6 +12,7 @@
 //   [ln s0, ln s1, ln s2 (trial, sorted descending), q, material, d0, d1, d2]
 // with d = ln s_projected - ln s_trial in the same order.  The loss is the mean
 // squared error of the network output against d in the scaling of mlp_features.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -37,6 +40,7 @@ constexpr int kNumWeights = kOffB1;     // 9728 bf16 copies
 static_assert(kNumParams == AEP_MLP_NUM_PARAMS, "parameter count");
 
 constexpr int kTrainRows = 64;
+constexpr int kPartBlocks = 256;  // blocks of one gradient pass (16,384 rows)
 constexpr int kTrainThreads = 128;
 
 using bf16 = __nv_bfloat16;
@@ -75,7 +79,7 @@ struct TrainSmem {
     float T[kTrainRows * 4];
     bf16 dY[kTrainRows * 8];
     bf16 dZ[2][kTrainRows * 64];  // ping-pong
-    float loss;
+    float wloss[kTrainThreads / 32];
 };
 
 __device__ __forceinline__ float dsilu(float z) {
@@ -83,15 +87,18 @@ __device__ __forceinline__ float dsilu(float z) {
     return s * (1.0f + z * (1.0f - s));
 }
 
-// forward and backward of one block of rows; gradients added to grad (f32, packed)
+// Forward and backward of one block of rows.  The block's gradient (f32, packed)
+// goes to its own row of `part` and its loss to part_loss[block]; k_mlp_reduce
+// sums the rows in block order, so training repeats bit for bit.
 __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* __restrict__ params,
                                                                   const float* __restrict__ rec, int n, int row0,
-                                                                  int rows_total, float* __restrict__ grad,
-                                                                  float* __restrict__ loss_out) {
+                                                                  int row_end, int rows_total, float* __restrict__ part,
+                                                                  float* __restrict__ part_loss) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int base = row0 + blockIdx.x * kTrainRows;
+    float* const grad = part + (long)blockIdx.x * kNumParams;
     for (int i = tid; i < kOffB1; i += kTrainThreads) {
         const bf16 w = __float2bfloat16(params[i]);
         if (i < kOffW2) S.W1[i - kOffW1] = w;
@@ -100,11 +107,10 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         else S.W4[i - kOffW4] = w;
     }
     for (int i = tid; i < 200; i += kTrainThreads) S.b[i] = params[kOffB1 + i];
-    if (tid == 0) S.loss = 0.0f;
     for (int r = tid; r < kTrainRows; r += kTrainThreads) {
         const long gi = (long)(base + r) % n;  // wrap around the record set
         const float* q = rec + 8 * gi;
-        const bool live = base + r < row0 + rows_total;
+        const bool live = base + r < row_end;
         float ln[3] = {q[0], q[1], q[2]};
         const float sc = mlp_features(ln, q[3], (int)q[4], S.X + r * 16);
         for (int k = 0; k < 3; ++k) S.T[r * 4 + k] = live ? q[5 + k] * sc : 0.0f;
@@ -153,7 +159,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-        if (lane == 0) atomicAdd(&S.loss, lsum);
+        if (lane == 0) S.wloss[warp] = lsum;
     }
     __syncthreads();
     // ---- backward
@@ -165,13 +171,13 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         const int g = lane >> 2, t = lane & 3;
         for (int e = 0; e < 4; ++e) {
             const int j = g + (e >> 1) * 8, k = n0 + 2 * t + (e & 1);
-            if (j < 8) atomicAdd(&grad[kOffW4 + j * 64 + k], c[e]);
+            if (j < 8) grad[kOffW4 + j * 64 + k] = c[e];
         }
     }
     if (tid < 8) {
         float s = 0.0f;
         for (int r = 0; r < kTrainRows; ++r) s += __bfloat162float(S.dY[r * 8 + tid]);
-        atomicAdd(&grad[kOffB4 + tid], s);
+        grad[kOffB4 + tid] = s;
     }
     // dZ3 = (dY W4^T) * silu'(Z3):  dH3[r][k] = sum_j dY[r][j] W4t[j][k]
     for (int tt = warp; tt < 32; tt += 4) {
@@ -202,13 +208,13 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
             const int g = lane >> 2, t = lane & 3;
             for (int e = 0; e < 4; ++e) {
                 const int nn = m0 + g + (e >> 1) * 8, k = n0 + 2 * t + (e & 1);
-                atomicAdd(&grad[offW[l] + nn * kin + k], c[e]);
+                grad[offW[l] + nn * kin + k] = c[e];
             }
         }
         if (tid < 64) {
             float s = 0.0f;
             for (int r = 0; r < kTrainRows; ++r) s += __bfloat162float(dZ[r * 64 + tid]);
-            atomicAdd(&grad[offB[l] + tid], s);
+            grad[offB[l] + tid] = s;
         }
         if (l > 0) {
             bf16* dZn = S.dZ[1 - cur];
@@ -227,7 +233,27 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         __syncthreads();
         cur = 1 - cur;
     }
-    if (tid == 0) atomicAdd(loss_out, S.loss / (3.0f * rows_total));
+    if (tid == 0) {
+        float l = 0.0f;
+        for (int w = 0; w < kTrainThreads / 32; ++w) l += S.wloss[w];
+        part_loss[blockIdx.x] = l / (3.0f * rows_total);
+    }
+}
+
+// grad[i] (+)= sum over the blocks of part[b][i] in block order; loss likewise
+__global__ void k_mlp_reduce(const float* __restrict__ part, const float* __restrict__ part_loss, int blocks,
+                             float* __restrict__ grad, float* __restrict__ loss, int accumulate) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kNumParams) {
+        float s = accumulate ? grad[i] : 0.0f;
+        for (int b = 0; b < blocks; ++b) s += part[(long)b * kNumParams + i];
+        grad[i] = s;
+    }
+    if (i == 0) {
+        float l = accumulate ? *loss : 0.0f;
+        for (int b = 0; b < blocks; ++b) l += part_loss[b];
+        *loss = l;
+    }
 }
 
 // Adam (Kingma & Ba 2015) on the f32 master parameters; zeroes the gradient and
@@ -289,6 +315,8 @@ struct aep_mlp {
     float* v = nullptr;
     bf16* wb = nullptr;   // bf16 weights (W^T blocks)
     float* loss = nullptr;
+    float* part = nullptr;       // per-block gradients of one pass [kPartBlocks][kNumParams]
+    float* part_loss = nullptr;  // per-block losses
     int64_t t = 0;        // Adam step
     std::string err;
 };
@@ -330,6 +358,8 @@ aep_status aep_mlp_create(uint64_t seed, aep_mlp** out) {
     MCK(cudaMalloc(&mlp->v, sizeof(float) * kNumParams));
     MCK(cudaMalloc(&mlp->wb, sizeof(bf16) * kNumWeights));
     MCK(cudaMalloc(&mlp->loss, sizeof(float)));
+    MCK(cudaMalloc(&mlp->part, sizeof(float) * kNumParams * kPartBlocks));
+    MCK(cudaMalloc(&mlp->part_loss, sizeof(float) * kPartBlocks));
     // He-normal weights (SiLU), zero biases, seeded
     std::vector<float> h(kNumParams, 0.0f);
     std::mt19937_64 rng(seed);
@@ -364,6 +394,8 @@ aep_status aep_mlp_destroy(aep_mlp* mlp) {
     cudaFree(mlp->v);
     cudaFree(mlp->wb);
     cudaFree(mlp->loss);
+    cudaFree(mlp->part);
+    cudaFree(mlp->part_loss);
     delete mlp;
     return AEP_OK;
 }
@@ -383,23 +415,31 @@ aep_status aep_mlp_set_params(aep_mlp* mlp, const float* host, int64_t count) {
     return AEP_OK;
 }
 
+// gradient and loss of `rows` records from row0 (cyclic) into mlp->g / mlp->loss:
+// passes of at most kPartBlocks blocks, each reduced in block order
 static aep_status grad_pass(aep_mlp* mlp, const float* rec, int64_t n, int64_t row0, int rows, cudaStream_t s) {
-    const int blocks = (rows + kTrainRows - 1) / kTrainRows;
     static bool attr = false;
     if (!attr) {
         MCK(cudaFuncSetAttribute(k_mlp_train_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem)));
         attr = true;
     }
-    k_mlp_train_tile<<<blocks, kTrainThreads, sizeof(TrainSmem), s>>>(mlp->p, rec, (int)n, (int)row0, rows, mlp->g,
-                                                                      mlp->loss);
-    MCK(cudaGetLastError());
+    const int blocks = (rows + kTrainRows - 1) / kTrainRows;
+    for (int b0 = 0; b0 < blocks; b0 += kPartBlocks) {
+        const int nb = std::min(kPartBlocks, blocks - b0);
+        k_mlp_train_tile<<<nb, kTrainThreads, sizeof(TrainSmem), s>>>(mlp->p, rec, (int)n,
+                                                                      (int)(row0 + (int64_t)b0 * kTrainRows),
+                                                                      (int)(row0 + rows), rows, mlp->part,
+                                                                      mlp->part_loss);
+        MCK(cudaGetLastError());
+        k_mlp_reduce<<<(kNumParams + 255) / 256, 256, 0, s>>>(mlp->part, mlp->part_loss, nb, mlp->g, mlp->loss,
+                                                              b0 > 0 ? 1 : 0);
+        MCK(cudaGetLastError());
+    }
     return AEP_OK;
 }
 
 aep_status aep_mlp_gradient(aep_mlp* mlp, const float* d_records, int64_t n, float* host_grad, double* loss) {
     if (!mlp || !d_records || n <= 0 || n > (1 << 24) || !host_grad) return AEP_INVALID_ARG;
-    MCK(cudaMemset(mlp->g, 0, sizeof(float) * kNumParams));
-    MCK(cudaMemset(mlp->loss, 0, sizeof(float)));
     aep_status st = grad_pass(mlp, d_records, n, 0, (int)n, nullptr);
     if (st) return st;
     MCK(cudaDeviceSynchronize());
@@ -424,7 +464,6 @@ aep_status aep_mlp_train(aep_mlp* mlp, const float* d_records, int64_t n, int64_
         const double frac = steps > 1 ? (double)it / (double)(steps - 1) : 1.0;
         const double lri = lr_final + 0.5 * (lr - lr_final) * (1.0 + std::cos(3.14159265358979323846 * frac));
         const bool report = it == steps - 1;
-        if (report) MCK(cudaMemsetAsync(mlp->loss, 0, sizeof(float), s));
         aep_status st = grad_pass(mlp, d_records, n, row0 % n, batch, s);
         if (st) return st;
         ++mlp->t;

@@ -143,8 +143,14 @@ def test_training_reduces_loss_on_harvested_pairs():
     m = ReturnMapMLP(seed=3)
     _, loss0 = m.gradient(rec.data_ptr(), n)
     loss1 = m.train(rec.data_ptr(), n, steps=1500, batch=4096, lr=2e-3, lr_final=2e-5)
-    _, loss_end = m.gradient(rec.data_ptr(), n)
+    g_end, loss_end = m.gradient(rec.data_ptr(), n)
     assert loss_end < 0.05 * loss0, (loss0, loss1, loss_end)
+    # the per-block gradients are summed in block order: training repeats bit for bit
+    m2 = ReturnMapMLP(seed=3)
+    assert m2.train(rec.data_ptr(), n, steps=1500, batch=4096, lr=2e-3, lr_final=2e-5) == loss1
+    assert np.array_equal(m2.get_params(), m.get_params())
+    g2, l2 = m2.gradient(rec.data_ptr(), n)
+    assert np.array_equal(g2, g_end) and l2 == loss_end
 
 
 def _learned_run(mlp, scene, steps, tol=1e-3):
@@ -237,6 +243,7 @@ def test_learned_cloth_return_map():
         fb += st["learned_fallbacks"]
     assert acc + fb > 0
     # an accepted prediction may differ from the exact projection by up to the
-    # tolerance (1e-3) relative to the projected strain, per step; the directions
-    # get the matching bound, the rest keeps the exact-path tolerances
-    _compare_mesh(g2.get_mesh(), orc.get_mesh(), 2e-6, 1e-3, 1e-3, 5e-3)
+    # tolerance (1e-3) relative to the projected (r13, r23, r33 - 1), whose size is
+    # at most ~1, in each of the 10 steps: the directions get 10 x 1e-3, the rest
+    # keeps the exact-path tolerances
+    _compare_mesh(g2.get_mesh(), orc.get_mesh(), 2e-6, 1e-3, 1e-2, 5e-3)
