@@ -74,7 +74,9 @@ class aep_params(C.Structure):
         ("mesh_damp", C.c_double),
         ("cloth_volume_weighting", C.c_int32),
         ("full_sort", C.c_int32),
-        ("reserved", C.c_int64 * 6),
+        ("reorder_interval", C.c_int32),
+        ("reserved_i", C.c_int32),
+        ("reserved", C.c_int64 * 5),
     ]
 
 
@@ -93,7 +95,8 @@ class aep_stats(C.Structure):
         ("learned_fallbacks", C.c_int64),
         ("sort_movers", C.c_int64),
         ("learned_exact", C.c_int64),
-        ("reserved", C.c_double * 3),
+        ("orderings", C.c_int64),
+        ("reserved", C.c_double * 2),
     ]
 
 

@@ -79,15 +79,15 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
     }
 }
 
-// Run structure of a batch of 16 sorted particles held one per lane of a
-// half-warp: bit t of the result is set if particle t starts a new run of equal
-// keys (the first particle is compared with the run carried in from the
-// previous batch).  __match_any_sync groups the lanes by key; since keys are
-// sorted, a lane heads its group iff it is the lowest lane of the group.
+// Run structure of a batch of 16 particles held one per lane of a half-warp: bit
+// t of the result is set if particle t starts a new run of equal keys, i.e. its
+// key differs from the previous particle's (the first particle is compared with
+// the run carried in from the previous batch).  Sorted keys give one run per key;
+// a particle out of order (the steps that keep the last ordering) starts a run
+// of its own, so the scatter stays correct for any order.
 __device__ __forceinline__ unsigned run_heads(unsigned hmask, int l, uint32_t key, uint32_t carried) {
-    const unsigned peers = __match_any_sync(hmask, key) >> (threadIdx.x & 16);
-    const bool lowest = (peers & ((1u << l) - 1u)) == 0u;
-    const bool head = lowest && !(l == 0 && key == carried);
+    const uint32_t before = __shfl_up_sync(hmask, key, 1, 16);
+    const bool head = key != (l == 0 ? carried : before);
     return __ballot_sync(hmask, head) >> (threadIdx.x & 16);
 }
 

@@ -537,5 +537,5 @@ class HybridSolver:
                     out_of_domain=s.out_of_domain, fp64_fallbacks=s.fp64_fallbacks, overflow=s.overflow,
                     active_nodes=s.active_nodes, learned_accepted=s.learned_accepted,
                     learned_fallbacks=s.learned_fallbacks, learned_exact=s.learned_exact,
-                    sort_movers=s.sort_movers,
+                    sort_movers=s.sort_movers, orderings=s.orderings,
                     total_mass=s.total_mass, total_momentum=list(s.total_momentum))

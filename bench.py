@@ -212,6 +212,7 @@ def run_ours(args):
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    orderings0 = solver.stats()["orderings"]
     solver.set_profiling(True)
     barrier()
     with ClockSampler(local) as clk:
@@ -229,6 +230,7 @@ def run_ours(args):
     phase_ms, timed = solver.phase_times()
     solver.set_profiling(False)
     st = solver.stats()
+    orderings = st["orderings"] - orderings0
     value, sec = job_throughput(n_p, args.steps, ms * 1e-3, world)
     ms = sec * 1e3
 
@@ -265,15 +267,17 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic (seeded sand column)",
         "config": {"workload": "sand_column", "particles": n_p, "grid": [args.res] * 3, "dt": sc.dt,
                    "material": "drucker_prager_sand", "return_map": "plain", "parallelism": f"replicas{world}",
+                   "reorder_interval": int(sc.params.reorder_interval), "orderings_timed": orderings,
                    "l2": "flushed between timed steps (512 MB write)", "active_nodes": nodes,
                    "active_blocks": int(st["active_blocks"])},
         "roofline": roofline,
-        # per step: the ordering graph's k_flag_movers + k_place_stayers (+ k_place_movers
-        # when more than 512 particles change cell; CUB radix-sort kernels instead when
-        # more than 8,192 do), k_p2g, k_normalize, k_force, k_force_fp64, k_grid, k_g2p
-        "gpu_launches": 8 * args.steps + (args.steps if st["sort_movers"] > 512 else 0),
-        "launches_note": "8 library kernels per step on this workload (2 of them inside the ordering graph); "
-                         f"last step's ordering moved {st['sort_movers']} particles (-1: full CUB radix sort)",
+        # per step k_p2g, k_normalize, k_force, k_force_fp64, k_grid, k_g2p; per ordering
+        # (every reorder_interval-th step) the ordering graph's k_flag_movers +
+        # k_place_stayers (+ k_place_movers when more than 512 particles changed cell;
+        # CUB radix-sort kernels instead when more than 8,192 did)
+        "gpu_launches": 6 * args.steps + 2 * orderings,
+        "launches_note": f"6 library kernels per step + 2 per ordering ({orderings} orderings in the timed "
+                         f"steps, every {int(sc.params.reorder_interval)}th step)",
         "fp64_fallbacks_last_step": int(st["fp64_fallbacks"]),
         "wall_s": wall,
     }

@@ -120,7 +120,13 @@ typedef struct aep_params {
                                 from the last sorted keys when at most a quarter of the
                                 particles changed cell (same result up to the order of
                                 equal keys)                                            */
-    int64_t reserved[6];
+    int32_t reorder_interval; /* order the particles every this many steps (default 4;
+                                1 or 0: every step); the steps between keep the last order, and
+                                the few particles that changed cell since are scattered
+                                and gathered out of order (same physics; the FP32 sums
+                                of a run take its particles in another order)           */
+    int32_t reserved_i;
+    int64_t reserved[5];
 } aep_params;
 
 /* Counters of the last step (all zero until a step ran). */
@@ -140,7 +146,8 @@ typedef struct aep_stats {
                                    -1 when it was a full radix sort                      */
     int64_t learned_exact;      /* plastic states with a constant projection (sand apex,
                                    cloth in tension), taken exactly by the learned path  */
-    double reserved[3];
+    int64_t orderings;          /* particle orderings run by this handle (reorder_interval) */
+    double reserved[2];
 } aep_stats;
 
 /* ---- version / defaults ------------------------------------------------------- */

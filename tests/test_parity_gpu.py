@@ -219,6 +219,7 @@ def test_incremental_ordering_matches_full_sort():
     for full in (0, 1):
         prm = capi.aep_params.from_buffer_copy(sc.params)
         prm.full_sort = full
+        prm.reorder_interval = 1
         s = HybridSolver(sc.particles, sc.grid, prm)
         s.set_level_set(sc.levelset)
         s.init_volumes()
@@ -233,6 +234,62 @@ def test_incremental_ordering_matches_full_sort():
     assert inc[2] == full[2]  # exact fixed-point mass
     assert np.abs(inc[0]["positions"] - full[0]["positions"]).max() < 1e-6
     assert max_rel(inc[0]["velocities"], full[0]["velocities"]) < 1e-4
+
+
+def test_reorder_interval_keeps_order_between_orderings():
+    """reorder_interval = 4: three of every four steps keep the particles in their
+    slots, and the particles that changed cell meanwhile are scattered and
+    gathered out of order.  Against ordering every step: the same particles, exact
+    fixed-point mass, results equal up to the FP32 rounding of the per-run sums;
+    against the FP64 oracle at the usual step tolerances; and a checkpoint taken
+    between two orderings resumes bit for bit."""
+    from oracle.oracle import Oracle
+
+    sc = perturbed(scenes.sand_column(n=40000, res=32, seed=14), seed=15, vscale=2.0)
+    runs = {}
+    for interval in (1, 4):
+        prm = capi.aep_params.from_buffer_copy(sc.params)
+        prm.reorder_interval = interval
+        s = HybridSolver(sc.particles, sc.grid, prm)
+        s.set_level_set(sc.levelset)
+        s.init_volumes()
+        movers = []
+        for _ in range(10):
+            s.step(sc.dt)
+            movers.append(s.stats()["sort_movers"])
+        runs[interval] = (s, movers, s.stats()["total_mass"])
+    every, kept = runs[1], runs[4]
+    # steps 1 (a full sort: the particles are still in the upload order), 5 and 9
+    # order, the others keep the order
+    assert kept[1][0] == -1 and kept[1][4] > 0 and kept[1][8] > 0
+    assert all(kept[1][k] == 0 for k in (1, 2, 3, 5, 6, 7, 9))
+    assert every[2] == kept[2]
+    a, b = every[0].get_particles(), kept[0].get_particles()
+    assert np.abs(a["positions"] - b["positions"]).max() < 1e-6
+    assert max_rel(a["velocities"], b["velocities"]) < 1e-4
+    o = Oracle(sc.grid, sc.params)
+    o.set_particle_system(sc.particles)
+    o.set_level_set(sc.levelset)
+    o.init(volumes=True)
+    for _ in range(10):
+        o.step(sc.dt)
+    op = o.get_particles()
+    assert np.abs(b["positions"] - op["positions"]).max() < 2e-6
+    assert max_rel(b["velocities"], op["velocities"]) < 2e-3
+    # resume between orderings (one step after the ordering of step 9)
+    s = kept[0]
+    blob = s.checkpoint()
+    for _ in range(4):
+        s.step(sc.dt)
+    ref = s.get_particles()
+    s.load_checkpoint(blob)
+    for _ in range(4):
+        s.step(sc.dt)
+    again = s.get_particles()
+    for k in ("positions", "velocities", "elastic_deformation_gradients"):
+        assert np.array_equal(ref[k], again[k])
+    for s, _, _ in runs.values():
+        s.close()
 
 
 @pytest.mark.parametrize("where", ["pinned", "device"])
