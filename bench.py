@@ -324,12 +324,15 @@ def stress(F, plastic, mat, prm, vol=1.0):
 
 
 def rel_stats(a, b):
-    """Per-particle |P_gpu - P_fp64| / max(|P_fp64|, 1e-2 * rms |P_fp64|) (Frobenius)."""
+    """Per-particle |P_gpu - P_fp64| / max(|P_fp64|, 1e-2 * rms |P_fp64|) (Frobenius), and
+    the same error relative to the rms stress of the sample (p99_rms, max_rms)."""
     na = np.linalg.norm((a - b).reshape(len(a), -1), axis=1)
     nb = np.linalg.norm(b.reshape(len(b), -1), axis=1)
-    floor = 1e-2 * np.sqrt(np.mean(nb ** 2))
+    rms = np.sqrt(np.mean(nb ** 2))
+    floor = 1e-2 * rms
     r = na / np.maximum(nb, floor)
     return {"median": float(np.median(r)), "p99": float(np.percentile(r, 99)), "max": float(r.max()),
+            "p99_rms": float(np.percentile(na, 99) / rms), "max_rms": float(na.max() / rms),
             "particles": int(len(r)), "floor": float(floor)}
 
 
