@@ -52,16 +52,15 @@ __global__ void k_keys(KParams P, PArrays cur, int n, uint32_t* keys, DevStats* 
 // D^-1 = 3/h^2 (:177), x_i - x_p = (o - 1 - f) h  =>  w (b + Mh o) with
 // Mh[:,a] = m D^-1 h_a B[:,a] and b = m v - Mh (1 + f).
 constexpr int kP2GThreads = 128;
-constexpr int kP2GChunk = 64;  // particles per half-warp
+constexpr int kP2GChunk = 128;  // particles per warp (4 batches of 32)
 // Prep record of one particle, 9 float4 (36 words, 16-byte aligned):
 //   q0 = (b, m)  q1 = Mh[0..3]  q2 = Mh[4..7]  q3 = (Mh[8], T lo, T hi, -)
 //   q4 = wx  q5 = wy  q6 = wz  q7 = (base, key)
 // A lane writes its own record with 128-bit stores; a stride of 36 words puts
-// the 8 lanes of each store wavefront on distinct banks.  Each half-warp's 16
-// records are skewed by one float4 so the two halves of a warp reading the
-// same slot do not collide either.
+// the 8 lanes of each store wavefront on distinct banks; the whole warp then
+// reads one record at a time (broadcast).
 constexpr int kP2GRec = 9;
-constexpr int kP2GRegion = 16 * kP2GRec + 1;  // float4 per half-warp region
+constexpr int kP2GRegion = 32 * kP2GRec;  // float4 per warp region
 __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, uint32_t key) {
     uint32_t blk = key >> 6;
     int bx = (int)(blk % (uint32_t)P.nb[0]);
@@ -91,85 +90,86 @@ __device__ __forceinline__ unsigned run_heads(unsigned hmask, int l, uint32_t ke
     return __ballot_sync(hmask, head) >> (threadIdx.x & 16);
 }
 
-// The block's 512 particles (8 half-warps x 64) mostly share one 4x4x4 cell
-// block; the runs whose stencil lies in the 2x2x2 node blocks from that block
-// (the grid tile of G2P) are summed into a fixed-point copy of the tile in shared
-// memory, which is added to the grid once per node at the end; other runs add
-// to the grid directly.  Integer sums: the result does not depend on the order.
+// One warp streams through 128 ordered particles, one particle per iteration:
+// lane (l & 15) owns the stencil column (ox, oy) = (l & 3, (l >> 2) & 3) and the
+// half h = l >> 4 the two z-layers oz = 2h, 2h + 1, so each lane accumulates 2 nodes
+// x (mass, momentum) in FP32 registers over a run of particles with the same base
+// node.  At the end of a run (warp-uniform) the node sums are rounded to fixed
+// point and added as integers: runs whose stencil lies in the block's grid tile
+// (the 2x2x2 node blocks of its first particle, where almost all of its 512
+// particles sit) into a fixed-point copy of the tile in shared memory, which is
+// added to the grid once per node at the end; other runs into the grid directly.
+// Integer sums: the result does not depend on the order.
+// Exact mass: rounding the node masses one by one loses the difference between
+// a run's exact fixed-point particle mass T = sum_p T_p and the sum S of its
+// rounded node masses; the run adds T - S to its stencil node (1,1,1), which
+// always exists, so the grid mass is sum_p T_p exactly and is conserved bit for
+// bit from step to step.  T - S is far below 2^31 (FP32 weight-sum error and
+// roundings), so it is computed from the low 32 bits of T and of the node masses
+// with one 32-bit warp reduction.
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                      const int32_t* __restrict__ perm, int n, GArrays G,
                                                      int32_t* __restrict__ slot_of, int32_t* __restrict__ curidx_of) {
-    __shared__ float4 sm4[(kP2GThreads / 16) * kP2GRegion];
+    __shared__ float4 sm4[(kP2GThreads / 32) * kP2GRegion];
     __shared__ unsigned long long tacc[4 * kTileNodes];  // [channel][tile node]
-    const int hw = threadIdx.x >> 4, l = threadIdx.x & 15;
-    float4* const region = sm4 + hw * kP2GRegion;
-    const unsigned hmask = 0xFFFFu << (threadIdx.x & 16);
-    const int ox = l & 3, oy = l >> 2;
-    const long blk0 = (long)blockIdx.x * (kP2GThreads / 16) * kP2GChunk;
-    const long chunk0 = blk0 + (long)hw * kP2GChunk;
-    const int cnt_total = (int)max(0L, min((long)kP2GChunk, (long)n - chunk0));  // uniform per half-warp
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* const region = sm4 + warp * kP2GRegion;
+    const int half = lane >> 4, ox = lane & 3, oy = (lane >> 2) & 3;
+    const long blk0 = (long)blockIdx.x * (kP2GThreads / 32) * kP2GChunk;
+    const long chunk0 = blk0 + (long)warp * kP2GChunk;
+    const int cnt_total = (int)max(0L, min((long)kP2GChunk, (long)n - chunk0));  // warp-uniform
     int org[3];
     tile_origin(P, keys[blk0], org);
     for (int i = threadIdx.x; i < 4 * kTileNodes; i += kP2GThreads) tacc[i] = 0ull;
     __syncthreads();
 
-    float am[4] = {0, 0, 0, 0}, ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
+    float am[2] = {0, 0}, ax[2] = {0, 0}, ay[2] = {0, 0}, az[2] = {0, 0};
     uint32_t run_key = kInvalidKey;
     int rb[3] = {0, 0, 0};
-
-    // Exact mass: the run's node masses are rounded to fixed point one by one;
-    // their sum S differs from the run's exact fixed-point mass T = sum_p T_p by
-    // the FP32 weight-sum error and the roundings.  The residual T - S is added
-    // to stencil node (1,1,1), which always exists, so the grid mass equals
-    // sum_p T_p exactly and is conserved bit-for-bit from step to step.
     long long run_T = 0;
-    auto flush = [&]() {
+    auto flush = [&]() {  // warp-uniform
         if (run_key == kInvalidKey) return;
-        long long mf[4], S = 0;
+        long long mf[2];
 #pragma unroll
-        for (int oz = 0; oz < 4; ++oz) {
-            mf[oz] = __float2ll_rn(am[oz] * P.mass_scale);
-            S += mf[oz];
-        }
-#pragma unroll
-        for (int o = 8; o > 0; o >>= 1) S += __shfl_xor_sync(hmask, S, o, 16);
-        if (l == 5) mf[1] += run_T - S;
-        run_T = 0;
-        int x = rb[0] + ox, y = rb[1] + oy;
-        if ((rb[0] >> 2) == org[0] && (rb[1] >> 2) == org[1] && (rb[2] >> 2) == org[2]) {  // half-warp-uniform
+        for (int k = 0; k < 2; ++k) mf[k] = __float2ll_rn(am[k] * P.mass_scale);
+        const unsigned s_lo = __reduce_add_sync(0xffffffffu, (unsigned)mf[0] + (unsigned)mf[1]);
+        if (lane == 5) mf[1] += (long long)(int)((unsigned)run_T - s_lo);  // (ox, oy, oz) = (1, 1, 1)
+        const int x = rb[0] + ox, y = rb[1] + oy;
+        if ((rb[0] >> 2) == org[0] && (rb[1] >> 2) == org[1] && (rb[2] >> 2) == org[2]) {
             const int tx = x - 4 * org[0], ty = y - 4 * org[1];
             const int txy = (tx >> 2) * 64 + (tx & 3) + (ty >> 2) * 128 + ((ty & 3) << 2);
 #pragma unroll
-            for (int oz = 0; oz < 4; ++oz) {
-                if (mf[oz] != 0) {
-                    const int tz = rb[2] + oz - 4 * org[2];
+            for (int k = 0; k < 2; ++k) {
+                if (mf[k] != 0) {
+                    const int tz = rb[2] + 2 * half + k - 4 * org[2];
                     unsigned long long* a = tacc + txy + (tz >> 2) * 256 + ((tz & 3) << 4);
-                    atomicAdd(a, (unsigned long long)mf[oz]);
-                    atomicAdd(a + kTileNodes, to_fixed(ax[oz], P.mom_scale));
-                    atomicAdd(a + 2 * kTileNodes, to_fixed(ay[oz], P.mom_scale));
-                    atomicAdd(a + 3 * kTileNodes, to_fixed(az[oz], P.mom_scale));
+                    atomicAdd(a, (unsigned long long)mf[k]);
+                    atomicAdd(a + kTileNodes, to_fixed(ax[k], P.mom_scale));
+                    atomicAdd(a + 2 * kTileNodes, to_fixed(ay[k], P.mom_scale));
+                    atomicAdd(a + 3 * kTileNodes, to_fixed(az[k], P.mom_scale));
                 }
-                am[oz] = ax[oz] = ay[oz] = az[oz] = 0.0f;
             }
-            return;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (mf[k] != 0) {
+                    unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + 2 * half + k);
+                    atomicAdd(a + 0, (unsigned long long)mf[k]);
+                    atomicAdd(a + 1, to_fixed(ax[k], P.mom_scale));
+                    atomicAdd(a + 2, to_fixed(ay[k], P.mom_scale));
+                    atomicAdd(a + 3, to_fixed(az[k], P.mom_scale));
+                }
+            }
         }
 #pragma unroll
-        for (int oz = 0; oz < 4; ++oz) {
-            if (mf[oz] != 0) {
-                unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + oz);
-                atomicAdd(a + 0, (unsigned long long)mf[oz]);
-                atomicAdd(a + 1, to_fixed(ax[oz], P.mom_scale));
-                atomicAdd(a + 2, to_fixed(ay[oz], P.mom_scale));
-                atomicAdd(a + 3, to_fixed(az[oz], P.mom_scale));
-            }
-            am[oz] = ax[oz] = ay[oz] = az[oz] = 0.0f;
-        }
+        for (int k = 0; k < 2; ++k) am[k] = ax[k] = ay[k] = az[k] = 0.0f;
+        run_T = 0;
     };
 
-    for (int b0 = 0; b0 < cnt_total; b0 += 16) {
-        const long j = chunk0 + b0 + l;
+    for (int b0 = 0; b0 < cnt_total; b0 += 32) {
+        const long j = chunk0 + b0 + lane;
         uint32_t my_key = kInvalidKey;
-        if (b0 + l < cnt_total) {
+        if (b0 + lane < cnt_total) {
             const uint32_t key = keys[j];
             if (j == 0 || (keys[j - 1] >> 6) != (key >> 6)) mark_blocks(P, G, key);
             const int pj = perm[j];
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
                 }
                 b[a] = t;
             }
-            float4* r = region + l * kP2GRec;
+            float4* r = region + lane * kP2GRec;
             r[0] = make_float4(b[0], b[1], b[2], m);
             r[1] = make_float4(Mh[0], Mh[1], Mh[2], Mh[3]);
             r[2] = make_float4(Mh[4], Mh[5], Mh[6], Mh[7]);
@@ -216,9 +216,11 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
                                __uint_as_float(key));
             my_key = key;
         }
-        __syncwarp(hmask);
-        const int cnt = min(16, cnt_total - b0);
-        const unsigned heads = run_heads(hmask, l, my_key, run_key);
+        // run heads: a particle whose key differs from the previous one's (any order)
+        const uint32_t before = __shfl_up_sync(0xffffffffu, my_key, 1);
+        const unsigned heads = __ballot_sync(0xffffffffu, my_key != (lane == 0 ? run_key : before));
+        __syncwarp();
+        const int cnt = min(32, cnt_total - b0);
         for (int t = 0; t < cnt; ++t) {
             const float4* r = region + t * kP2GRec;
             if ((heads >> t) & 1u) {
@@ -227,32 +229,32 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
                 run_key = __float_as_uint(q7.w);
                 rb[0] = __float_as_int(q7.x); rb[1] = __float_as_int(q7.y); rb[2] = __float_as_int(q7.z);
             }
-            const float4 q0 = r[0], q1 = r[1], q2 = r[2], q3 = r[3], q6 = r[6];
+            const float4 q0 = r[0], q1 = r[1], q2 = r[2], q3 = r[3];
             const float wxo = reinterpret_cast<const float*>(r + 4)[ox];
             const float wyo = reinterpret_cast<const float*>(r + 5)[oy];
+            const float2 wz2 = reinterpret_cast<const float2*>(r + 6)[half];
             run_T += (long long)(((unsigned long long)(unsigned)__float_as_int(q3.z) << 32) |
                                  (unsigned long long)(unsigned)__float_as_int(q3.y));
             const float wxy = wxo * wyo;
-            const float fx = (float)ox, fy = (float)oy;
+            const float fx = (float)ox, fy = (float)oy, fz = (float)(2 * half);
             // Mh row-major: row a = (Mh[3a], Mh[3a+1], Mh[3a+2])
-            float tx = q0.x + q1.x * fx + q1.y * fy;
-            float ty = q0.y + q1.w * fx + q2.x * fy;
-            float tz = q0.z + q2.z * fx + q2.w * fy;
-            const float mz0 = q1.z, mz1 = q2.y, mz2 = q3.x;
-            const float wz4[4] = {q6.x, q6.y, q6.z, q6.w};
+            float tx = q0.x + q1.x * fx + q1.y * fy + q1.z * fz;
+            float ty = q0.y + q1.w * fx + q2.x * fy + q2.y * fz;
+            float tz = q0.z + q2.z * fx + q2.w * fy + q3.x * fz;
+            const float wz[2] = {wz2.x, wz2.y};
 #pragma unroll
-            for (int oz = 0; oz < 4; ++oz) {
-                const float w = wxy * wz4[oz];
-                am[oz] = fmaf(w, q0.w, am[oz]);
-                ax[oz] = fmaf(w, tx, ax[oz]);
-                ay[oz] = fmaf(w, ty, ay[oz]);
-                az[oz] = fmaf(w, tz, az[oz]);
-                tx += mz0;
-                ty += mz1;
-                tz += mz2;
+            for (int k = 0; k < 2; ++k) {
+                const float w = wxy * wz[k];
+                am[k] = fmaf(w, q0.w, am[k]);
+                ax[k] = fmaf(w, tx, ax[k]);
+                ay[k] = fmaf(w, ty, ay[k]);
+                az[k] = fmaf(w, tz, az[k]);
+                tx += q1.z;
+                ty += q2.y;
+                tz += q3.x;
             }
         }
-        __syncwarp(hmask);
+        __syncwarp();
     }
     flush();
     __syncthreads();
@@ -1752,7 +1754,7 @@ void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, cons
                 const GArrays& G, int32_t* slot_of, int32_t* curidx_of, cudaStream_t s) {
     long hw = (n + kP2GChunk - 1) / kP2GChunk;
     if (n > 0)
-        k_p2g<<<blocks_for(hw, kP2GThreads / 16), kP2GThreads, 0, s>>>(P, cur, keys, perm, n, G, slot_of, curidx_of);
+        k_p2g<<<blocks_for(hw, kP2GThreads / 32), kP2GThreads, 0, s>>>(P, cur, keys, perm, n, G, slot_of, curidx_of);
 }
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s) {
     k_normalize<<<grid_blocks, 256, 0, s>>>(P, G, st);
