@@ -474,7 +474,6 @@ aep_status run_p2g(aep_solver* s) {
         s->step_keys = s->keys_sorted;
         s->step_perm = s->perm;
     }
-    CK(cudaMemsetAsync(s->G.nactive, 0, sizeof(int32_t), s->stream));
     mark(s, AEP_PHASE_P2G);
     launch_p2g(s->kp, P, s->step_keys, s->step_perm, (int)s->n, s->G, s->slot_of, s->curidx_of, s->stream);
     CKLAUNCH();
@@ -554,13 +553,12 @@ aep_status aep_solver_create(const aep_grid_desc* grid, const aep_params* params
     CK(cudaMalloc(&s->G.vbf, sizeof(float4) * s->nnodes));
     CK(cudaMalloc(&s->G.flag, sizeof(uint32_t) * (size_t)s->nblocks));
     CK(cudaMalloc(&s->G.active, sizeof(int32_t) * (size_t)s->nblocks));
-    CK(cudaMalloc(&s->G.nactive, sizeof(int32_t)));
     CK(cudaMalloc(&s->dstats, sizeof(DevStats)));
+    s->G.nactive = &s->dstats->nactive;  // device address inside the counters
     CK(cudaMemsetAsync(s->G.acc, 0, sizeof(unsigned long long) * 4 * s->nnodes, s->stream));
     CK(cudaMemsetAsync(s->G.vel, 0, sizeof(float4) * s->nnodes, s->stream));
     CK(cudaMemsetAsync(s->G.vbf, 0, sizeof(float4) * s->nnodes, s->stream));
     CK(cudaMemsetAsync(s->G.flag, 0, sizeof(uint32_t) * (size_t)s->nblocks, s->stream));
-    CK(cudaMemsetAsync(s->G.nactive, 0, sizeof(int32_t), s->stream));
     CK(cudaMemsetAsync(s->dstats, 0, sizeof(DevStats), s->stream));
     CK(cudaStreamSynchronize(s->stream));
     *out = s;
@@ -577,7 +575,6 @@ aep_status aep_solver_destroy(aep_solver* s) {
     cudaFree(s->G.vbf);
     cudaFree(s->G.flag);
     cudaFree(s->G.active);
-    cudaFree(s->G.nactive);
     cudaFree(s->dstats);
     cudaFree(s->dforce);
     cudaFree(s->harvest_count);

@@ -133,6 +133,10 @@ struct DevStats {
     long long movers;              // particles that changed key (incremental ordering), -1: full sort
     unsigned int force_fp64;       // entries of the force pass's FP64 list (k_force_fp64)
     unsigned int mlp_rows;         // rows queued for the learned return map (k_mlp_finish)
+    // length of the active node-block list (GArrays::nactive points here: zeroed with
+    // the counters at each step), on its own cache line: every grid thread reads it
+    // while the counters above take the blocks' atomics
+    alignas(128) int32_t nactive;
 };
 
 // Rows of the learned return map that the G2P pass queues for k_mlp_finish
