@@ -274,10 +274,13 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
 
 // ===================================================================================
 // v_i = p_i / m_i on touched nodes (HybridSolver.cpp:233-240); clears the accumulators
-// for the force impulse; exact int64 totals of mass and momentum.
-__global__ void k_normalize(KParams P, GArrays G, DevStats* st) {
+// for the force impulse; exact int64 totals of mass and momentum (summed per block,
+// one atomic per block and total).  Launched with 256 threads.
+__global__ void __launch_bounds__(256) k_normalize(KParams P, GArrays G, DevStats* st) {
+    __shared__ long long red[5][8];
     const int nact = *G.nactive;
     const long total = (long)nact * 64;
+    if ((long)blockIdx.x * blockDim.x >= total) return;  // no node for this block (block-uniform)
     long long sm_ = 0, sx = 0, sy = 0, sz = 0;
     unsigned long long cnt = 0;
     bool ovf = false;
@@ -311,12 +314,20 @@ __global__ void k_normalize(KParams P, GArrays G, DevStats* st) {
         sz += __shfl_xor_sync(0xffffffffu, sz, o);
         cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        if (cnt) atomicAdd(&st->nodes, cnt);
-        if (sm_) atomicAdd(&st->mass, (unsigned long long)sm_);
-        if (sx) atomicAdd(&st->mom[0], (unsigned long long)sx);
-        if (sy) atomicAdd(&st->mom[1], (unsigned long long)sy);
-        if (sz) atomicAdd(&st->mom[2], (unsigned long long)sz);
+        red[0][w] = (long long)cnt;
+        red[1][w] = sm_;
+        red[2][w] = sx;
+        red[3][w] = sy;
+        red[4][w] = sz;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        long long t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[threadIdx.x][k];
+        unsigned long long* dst[5] = {&st->nodes, &st->mass, &st->mom[0], &st->mom[1], &st->mom[2]};
+        if (t) atomicAdd(dst[threadIdx.x], (unsigned long long)t);
     }
     if (ovf) atomicOr(&st->overflow, 1ull);
 }
@@ -683,6 +694,7 @@ __global__ void k_cloth_force(KParams P, PArrays cur, MeshArrays M, float dt_for
 __global__ void k_grid(KParams P, GArrays G, float dt_force, int write_force, double* force_out) {
     const int nact = *G.nactive;
     const long total = (long)nact * 64;
+    if ((long)blockIdx.x * blockDim.x >= total) return;  // no node for this block
     dt_force = step_dt(P, dt_force, 0);
     float vmax = 0.0f;  // max |v|^2 after the update, before collision (RegularGrid.cpp:188-200, HS:878)
     // the loop trip count differs between threads: the warp reduction runs after it
