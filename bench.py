@@ -588,7 +588,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-steps", type=int, default=10)
     ap.add_argument("--no-config4", action="store_true")
-    ap.add_argument("--train-steps", type=int, default=40000)
+    ap.add_argument("--train-steps", type=int, default=200000)
     ap.add_argument("--harvest", type=int, default=4000000)
     ap.add_argument("--err-particles", type=int, default=65536)
     ap.add_argument("--err-steps", type=int, default=5)
