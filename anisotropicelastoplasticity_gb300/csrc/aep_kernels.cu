@@ -78,18 +78,6 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
     }
 }
 
-// Run structure of a batch of 16 particles held one per lane of a half-warp: bit
-// t of the result is set if particle t starts a new run of equal keys, i.e. its
-// key differs from the previous particle's (the first particle is compared with
-// the run carried in from the previous batch).  Sorted keys give one run per key;
-// a particle out of order (the steps that keep the last ordering) starts a run
-// of its own, so the scatter stays correct for any order.
-__device__ __forceinline__ unsigned run_heads(unsigned hmask, int l, uint32_t key, uint32_t carried) {
-    const uint32_t before = __shfl_up_sync(hmask, key, 1, 16);
-    const bool head = key != (l == 0 ? carried : before);
-    return __ballot_sync(hmask, head) >> (threadIdx.x & 16);
-}
-
 // One warp streams through 128 ordered particles, one particle per iteration:
 // lane (l & 15) owns the stencil column (ox, oy) = (l & 3, (l >> 2) & 3) and the
 // half h = l >> 4 the two z-layers oz = 2h, 2h + 1, so each lane accumulates 2 nodes
@@ -596,65 +584,74 @@ __global__ void __launch_bounds__(kFrcThreads, 5) k_force(KParams P, PArrays cur
         r[10] = make_float4(av[0], av[1], av[2], mat == kClothVertex ? 1.0f : 0.0f);
     }
     __syncwarp();
-    // stream: half h takes particles [16h, 16h+16)
+    // stream the warp's particles run by run (a run: consecutive particles with the
+    // same base node); half h takes the run's particles t + h, t + h + 2, ... and
+    // both halves accumulate all 4 z-layers of the lane's stencil column (ox, oy);
+    // at the end of the run (warp-uniform) the halves are added and half h adds
+    // z-layers 2h, 2h + 1 to the grid
     const int h = lane >> 4, l = lane & 15, ox = l & 3, oy = l >> 2;
-    const unsigned hmask = 0xFFFFu << (lane & 16);
-    const int cnt = (int)max(0l, min(16l, (long)n - (chunk0 + 16 * h)));
+    const int cnt = (int)max(0l, min(32l, (long)n - chunk0));
     float fx[4] = {0, 0, 0, 0}, fy[4] = {0, 0, 0, 0}, fz[4] = {0, 0, 0, 0};
-    uint32_t run_key = kInvalidKey;
-    int rb[3] = {0, 0, 0};
-    auto flush = [&]() {
-        if (run_key == kInvalidKey) return;
-        int x = rb[0] + ox, y = rb[1] + oy;
-#pragma unroll
-        for (int oz = 0; oz < 4; ++oz) {
-            if (fx[oz] != 0.0f || fy[oz] != 0.0f || fz[oz] != 0.0f) {
-                unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + oz);
-                atomicAdd(a + 1, to_fixed(fx[oz], P.mom_scale));
-                atomicAdd(a + 2, to_fixed(fy[oz], P.mom_scale));
-                atomicAdd(a + 3, to_fixed(fz[oz], P.mom_scale));
-            }
-            fx[oz] = fy[oz] = fz[oz] = 0.0f;
-        }
-    };
-    const unsigned heads = run_heads(hmask, l, my_key, kInvalidKey);
-    for (int i = 0; i < cnt; ++i) {
-        const float4* r = buf + frc_slot(16 * h + i);
-        if ((heads >> i) & 1u) {
-            flush();
-            const float4 q9 = r[9];
-            run_key = __float_as_uint(q9.w);
-            rb[0] = __float_as_int(q9.x); rb[1] = __float_as_int(q9.y); rb[2] = __float_as_int(q9.z);
-        }
-        const float4 q0 = r[0], q1 = r[1], q2 = r[2], q5 = r[5], q8 = r[8];
-        const float wxo = reinterpret_cast<const float*>(r + 3)[ox];
-        const float wyo = reinterpret_cast<const float*>(r + 4)[oy];
-        const float dxo = reinterpret_cast<const float*>(r + 6)[ox];
-        const float dyo = reinterpret_cast<const float*>(r + 7)[oy];
-        // grad w = (dwx wy wz, wx dwy wz, wx wy dwz); S g = wz (p1 S[:,0] + p2 S[:,1]) + dwz p3 S[:,2]
-        // S row-major: S[3a+b] -> q0=(S0,S1,S2,S3) q1=(S4,S5,S6,S7) q2.x=S8
-        const float p1 = dxo * wyo, p2 = wxo * dyo, p3 = wxo * wyo;
-        const float ax_ = p1 * q0.x + p2 * q0.y, ay_ = p1 * q0.w + p2 * q1.x, az_ = p1 * q1.z + p2 * q1.w;
-        const float cx = p3 * q0.z, cy = p3 * q1.y, cz = p3 * q2.x;
-        const float wz4[4] = {q5.x, q5.y, q5.z, q5.w}, dz4[4] = {q8.x, q8.y, q8.z, q8.w};
-#pragma unroll
-        for (int oz = 0; oz < 4; ++oz) {
-            fx[oz] = fmaf(wz4[oz], ax_, fmaf(dz4[oz], cx, fx[oz]));
-            fy[oz] = fmaf(wz4[oz], ay_, fmaf(dz4[oz], cy, fy[oz]));
-            fz[oz] = fmaf(wz4[oz], az_, fmaf(dz4[oz], cz, fz[oz]));
-        }
-        const float4 q10 = r[10];
-        if (q10.w != 0.0f) {  // cloth vertex: + w f_v (uniform across the half-warp)
-            const float wx_ = p3 * q10.x, wy_ = p3 * q10.y, wz_ = p3 * q10.z;
+    // run heads: a particle whose key differs from the previous one's (any order)
+    const uint32_t key_before = __shfl_up_sync(0xffffffffu, my_key, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || my_key != key_before);
+    for (int t = 0; t < cnt;) {
+        const unsigned after = heads & ~((2u << t) - 1u);  // heads after t (none for t = 31)
+        const int e = min(cnt, after ? __ffs(after) - 1 : 32);
+        const float4 q9 = (buf + frc_slot(t))[9];
+        const int rb[3] = {__float_as_int(q9.x), __float_as_int(q9.y), __float_as_int(q9.z)};
+        for (int i = t + h; i < e; i += 2) {
+            const float4* r = buf + frc_slot(i);
+            const float4 q0 = r[0], q1 = r[1], q2 = r[2], q5 = r[5], q8 = r[8];
+            const float wxo = reinterpret_cast<const float*>(r + 3)[ox];
+            const float wyo = reinterpret_cast<const float*>(r + 4)[oy];
+            const float dxo = reinterpret_cast<const float*>(r + 6)[ox];
+            const float dyo = reinterpret_cast<const float*>(r + 7)[oy];
+            // grad w = (dwx wy wz, wx dwy wz, wx wy dwz); S g = wz (p1 S[:,0] + p2 S[:,1]) + dwz p3 S[:,2]
+            // S row-major: S[3a+b] -> q0=(S0,S1,S2,S3) q1=(S4,S5,S6,S7) q2.x=S8
+            const float p1 = dxo * wyo, p2 = wxo * dyo, p3 = wxo * wyo;
+            const float ax_ = p1 * q0.x + p2 * q0.y, ay_ = p1 * q0.w + p2 * q1.x, az_ = p1 * q1.z + p2 * q1.w;
+            const float cx = p3 * q0.z, cy = p3 * q1.y, cz = p3 * q2.x;
+            const float wz4[4] = {q5.x, q5.y, q5.z, q5.w}, dz4[4] = {q8.x, q8.y, q8.z, q8.w};
 #pragma unroll
             for (int oz = 0; oz < 4; ++oz) {
-                fx[oz] = fmaf(wz4[oz], wx_, fx[oz]);
-                fy[oz] = fmaf(wz4[oz], wy_, fy[oz]);
-                fz[oz] = fmaf(wz4[oz], wz_, fz[oz]);
+                fx[oz] = fmaf(wz4[oz], ax_, fmaf(dz4[oz], cx, fx[oz]));
+                fy[oz] = fmaf(wz4[oz], ay_, fmaf(dz4[oz], cy, fy[oz]));
+                fz[oz] = fmaf(wz4[oz], az_, fmaf(dz4[oz], cz, fz[oz]));
+            }
+            const float4 q10 = r[10];
+            if (q10.w != 0.0f) {  // cloth vertex: + w f_v
+                const float wx_ = p3 * q10.x, wy_ = p3 * q10.y, wz_ = p3 * q10.z;
+#pragma unroll
+                for (int oz = 0; oz < 4; ++oz) {
+                    fx[oz] = fmaf(wz4[oz], wx_, fx[oz]);
+                    fy[oz] = fmaf(wz4[oz], wy_, fy[oz]);
+                    fz[oz] = fmaf(wz4[oz], wz_, fz[oz]);
+                }
             }
         }
+        // the run's sums: the two halves added, then z-layers 2h, 2h + 1 from half h
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            fx[oz] += __shfl_xor_sync(0xffffffffu, fx[oz], 16);
+            fy[oz] += __shfl_xor_sync(0xffffffffu, fy[oz], 16);
+            fz[oz] += __shfl_xor_sync(0xffffffffu, fz[oz], 16);
+        }
+        const int x = rb[0] + ox, y = rb[1] + oy;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const float gx = h ? fx[2 + k] : fx[k], gy = h ? fy[2 + k] : fy[k], gz = h ? fz[2 + k] : fz[k];
+            if (gx != 0.0f || gy != 0.0f || gz != 0.0f) {
+                unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + 2 * h + k);
+                atomicAdd(a + 1, to_fixed(gx, P.mom_scale));
+                atomicAdd(a + 2, to_fixed(gy, P.mom_scale));
+                atomicAdd(a + 3, to_fixed(gz, P.mom_scale));
+            }
+        }
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) fx[oz] = fy[oz] = fz[oz] = 0.0f;
+        t = e;
     }
-    flush();
 }
 
 // ===================================================================================
