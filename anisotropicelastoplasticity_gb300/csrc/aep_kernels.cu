@@ -78,11 +78,12 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
     }
 }
 
-// One warp streams through 128 ordered particles, one particle per iteration:
-// lane (l & 15) owns the stencil column (ox, oy) = (l & 3, (l >> 2) & 3) and the
-// half h = l >> 4 the two z-layers oz = 2h, 2h + 1, so each lane accumulates 2 nodes
-// x (mass, momentum) in FP32 registers over a run of particles with the same base
-// node.  At the end of a run (warp-uniform) the node sums are rounded to fixed
+// One warp streams through 128 ordered particles run by run (a run: consecutive
+// particles with the same base node): lane (l & 15) owns the stencil column
+// (ox, oy) = (l & 3, (l >> 2) & 3), and the half h = l >> 4 takes the run's particles
+// t + h, t + h + 2, ..., accumulating the column's 4 nodes x (mass, momentum) in
+// FP32 registers.  At the end of a run (warp-uniform) the halves' sums are added,
+// half h takes the z-layers 2h, 2h + 1, and the node sums are rounded to fixed
 // point and added as integers: runs whose stencil lies in the block's grid tile
 // (the 2x2x2 node blocks of its first particle, where almost all of its 512
 // particles sit) into a fixed-point copy of the tile in shared memory, which is
@@ -111,15 +112,32 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
     for (int i = threadIdx.x; i < 4 * kTileNodes; i += kP2GThreads) tacc[i] = 0ull;
     __syncthreads();
 
-    float am[2] = {0, 0}, ax[2] = {0, 0}, ay[2] = {0, 0}, az[2] = {0, 0};
+    float am[4] = {0, 0, 0, 0}, ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
     uint32_t run_key = kInvalidKey;
     int rb[3] = {0, 0, 0};
     long long run_T = 0;
     auto flush = [&]() {  // warp-uniform
         if (run_key == kInvalidKey) return;
+        // the two halves' sums added; half h then adds z-layers 2h, 2h + 1
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            am[oz] += __shfl_xor_sync(0xffffffffu, am[oz], 16);
+            ax[oz] += __shfl_xor_sync(0xffffffffu, ax[oz], 16);
+            ay[oz] += __shfl_xor_sync(0xffffffffu, ay[oz], 16);
+            az[oz] += __shfl_xor_sync(0xffffffffu, az[oz], 16);
+        }
+        run_T += __shfl_xor_sync(0xffffffffu, run_T, 16);
+        float gm[2], gx[2], gy[2], gz[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            gm[k] = half ? am[2 + k] : am[k];
+            gx[k] = half ? ax[2 + k] : ax[k];
+            gy[k] = half ? ay[2 + k] : ay[k];
+            gz[k] = half ? az[2 + k] : az[k];
+        }
         long long mf[2];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) mf[k] = __float2ll_rn(am[k] * P.mass_scale);
+        for (int k = 0; k < 2; ++k) mf[k] = __float2ll_rn(gm[k] * P.mass_scale);
         const unsigned s_lo = __reduce_add_sync(0xffffffffu, (unsigned)mf[0] + (unsigned)mf[1]);
         if (lane == 5) mf[1] += (long long)(int)((unsigned)run_T - s_lo);  // (ox, oy, oz) = (1, 1, 1)
         const int x = rb[0] + ox, y = rb[1] + oy;
@@ -132,9 +150,9 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
                     const int tz = rb[2] + 2 * half + k - 4 * org[2];
                     unsigned long long* a = tacc + txy + (tz >> 2) * 256 + ((tz & 3) << 4);
                     atomicAdd(a, (unsigned long long)mf[k]);
-                    atomicAdd(a + kTileNodes, to_fixed(ax[k], P.mom_scale));
-                    atomicAdd(a + 2 * kTileNodes, to_fixed(ay[k], P.mom_scale));
-                    atomicAdd(a + 3 * kTileNodes, to_fixed(az[k], P.mom_scale));
+                    atomicAdd(a + kTileNodes, to_fixed(gx[k], P.mom_scale));
+                    atomicAdd(a + 2 * kTileNodes, to_fixed(gy[k], P.mom_scale));
+                    atomicAdd(a + 3 * kTileNodes, to_fixed(gz[k], P.mom_scale));
                 }
             }
         } else {
@@ -143,14 +161,14 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
                 if (mf[k] != 0) {
                     unsigned long long* a = G.acc + 4ull * node_index(P, x, y, rb[2] + 2 * half + k);
                     atomicAdd(a + 0, (unsigned long long)mf[k]);
-                    atomicAdd(a + 1, to_fixed(ax[k], P.mom_scale));
-                    atomicAdd(a + 2, to_fixed(ay[k], P.mom_scale));
-                    atomicAdd(a + 3, to_fixed(az[k], P.mom_scale));
+                    atomicAdd(a + 1, to_fixed(gx[k], P.mom_scale));
+                    atomicAdd(a + 2, to_fixed(gy[k], P.mom_scale));
+                    atomicAdd(a + 3, to_fixed(gz[k], P.mom_scale));
                 }
             }
         }
 #pragma unroll
-        for (int k = 0; k < 2; ++k) am[k] = ax[k] = ay[k] = az[k] = 0.0f;
+        for (int oz = 0; oz < 4; ++oz) am[oz] = ax[oz] = ay[oz] = az[oz] = 0.0f;
         run_T = 0;
     };
 
@@ -209,38 +227,43 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
         const unsigned heads = __ballot_sync(0xffffffffu, my_key != (lane == 0 ? run_key : before));
         __syncwarp();
         const int cnt = min(32, cnt_total - b0);
-        for (int t = 0; t < cnt; ++t) {
-            const float4* r = region + t * kP2GRec;
+        // run by run: half h takes the run's particles t + h, t + h + 2, ...
+        for (int t = 0; t < cnt;) {
             if ((heads >> t) & 1u) {
                 flush();
-                const float4 q7 = r[7];
+                const float4 q7 = region[t * kP2GRec + 7];
                 run_key = __float_as_uint(q7.w);
                 rb[0] = __float_as_int(q7.x); rb[1] = __float_as_int(q7.y); rb[2] = __float_as_int(q7.z);
             }
-            const float4 q0 = r[0], q1 = r[1], q2 = r[2], q3 = r[3];
-            const float wxo = reinterpret_cast<const float*>(r + 4)[ox];
-            const float wyo = reinterpret_cast<const float*>(r + 5)[oy];
-            const float2 wz2 = reinterpret_cast<const float2*>(r + 6)[half];
-            run_T += (long long)(((unsigned long long)(unsigned)__float_as_int(q3.z) << 32) |
-                                 (unsigned long long)(unsigned)__float_as_int(q3.y));
-            const float wxy = wxo * wyo;
-            const float fx = (float)ox, fy = (float)oy, fz = (float)(2 * half);
-            // Mh row-major: row a = (Mh[3a], Mh[3a+1], Mh[3a+2])
-            float tx = q0.x + q1.x * fx + q1.y * fy + q1.z * fz;
-            float ty = q0.y + q1.w * fx + q2.x * fy + q2.y * fz;
-            float tz = q0.z + q2.z * fx + q2.w * fy + q3.x * fz;
-            const float wz[2] = {wz2.x, wz2.y};
+            const unsigned after = heads & ~((2u << t) - 1u);  // heads after t (none for t = 31)
+            const int e = min(cnt, after ? __ffs(after) - 1 : 32);
+            for (int i = t + half; i < e; i += 2) {
+                const float4* r = region + i * kP2GRec;
+                const float4 q0 = r[0], q1 = r[1], q2 = r[2], q3 = r[3], q6 = r[6];
+                const float wxo = reinterpret_cast<const float*>(r + 4)[ox];
+                const float wyo = reinterpret_cast<const float*>(r + 5)[oy];
+                run_T += (long long)(((unsigned long long)(unsigned)__float_as_int(q3.z) << 32) |
+                                     (unsigned long long)(unsigned)__float_as_int(q3.y));
+                const float wxy = wxo * wyo;
+                const float fx = (float)ox, fy = (float)oy;
+                // Mh row-major: row a = (Mh[3a], Mh[3a+1], Mh[3a+2])
+                float tx = q0.x + q1.x * fx + q1.y * fy;
+                float ty = q0.y + q1.w * fx + q2.x * fy;
+                float tz = q0.z + q2.z * fx + q2.w * fy;
+                const float wz[4] = {q6.x, q6.y, q6.z, q6.w};
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const float w = wxy * wz[k];
-                am[k] = fmaf(w, q0.w, am[k]);
-                ax[k] = fmaf(w, tx, ax[k]);
-                ay[k] = fmaf(w, ty, ay[k]);
-                az[k] = fmaf(w, tz, az[k]);
-                tx += q1.z;
-                ty += q2.y;
-                tz += q3.x;
+                for (int oz = 0; oz < 4; ++oz) {
+                    const float w = wxy * wz[oz];
+                    am[oz] = fmaf(w, q0.w, am[oz]);
+                    ax[oz] = fmaf(w, tx, ax[oz]);
+                    ay[oz] = fmaf(w, ty, ay[oz]);
+                    az[oz] = fmaf(w, tz, az[oz]);
+                    tx += q1.z;
+                    ty += q2.y;
+                    tz += q3.x;
+                }
             }
+            t = e;
         }
         __syncwarp();
     }
