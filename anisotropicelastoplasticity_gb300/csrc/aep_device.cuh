@@ -252,6 +252,15 @@ __device__ __forceinline__ void tile_origin(const KParams& P, uint32_t key, int 
     org[2] = (int)(r / (uint32_t)P.nb[1]);
 }
 
+// asynchronous 4-byte copy global -> shared (cp.async; no registers held while in
+// flight), its commit and the wait for all of this thread's copies
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // cooperative copy of the tile (all threads of the block); src2 / dst2 may be null
 __device__ __forceinline__ void load_tile(const KParams& P, const int org[3], const float4* __restrict__ src,
                                           const float4* __restrict__ src2, float4* dst, float4* dst2) {
