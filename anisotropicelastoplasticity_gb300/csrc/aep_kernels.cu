@@ -172,20 +172,44 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
         run_T = 0;
     };
 
+    // the next batch's particle state (x, m, v, B: 16 words per particle) is copied to
+    // shared memory with cp.async while the current batch's runs are scattered;
+    // each lane reads back only its own column
+    __shared__ float stage[kP2GThreads / 32][16][32];
+    float(*const stg)[32] = stage[warp];
+    auto prefetch = [&](int pj) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            cp_async4(&stg[a][lane], &cur.x[a][pj]);
+            cp_async4(&stg[4 + a][lane], &cur.v[a][pj]);
+        }
+        cp_async4(&stg[3][lane], &cur.m[pj]);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) cp_async4(&stg[7 + k][lane], &cur.B[k][pj]);
+        cp_async_commit();
+    };
+    int pj_cur = lane < cnt_total ? perm[chunk0 + lane] : 0;
+    prefetch(pj_cur);
     for (int b0 = 0; b0 < cnt_total; b0 += 32) {
         const long j = chunk0 + b0 + lane;
+        const int pj_next = b0 + 32 + lane < cnt_total ? perm[j + 32] : 0;
         uint32_t my_key = kInvalidKey;
+        cp_async_wait_all();
+        float xs_[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) xs_[k] = stg[k][lane];
+        if (b0 + 32 < cnt_total) prefetch(pj_next);
         if (b0 + lane < cnt_total) {
             const uint32_t key = keys[j];
             if (j == 0 || (keys[j - 1] >> 6) != (key >> 6)) mark_blocks(P, G, key);
-            const int pj = perm[j];
+            const int pj = pj_cur;
             if (slot_of) {  // a mesh is present: where each id sits in this step's order
                 const int id = cur.id[pj];
                 slot_of[id] = (int32_t)j;
                 curidx_of[id] = pj;
             }
-            float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
-            float m = cur.m[pj];
+            float xp[3] = {xs_[0], xs_[1], xs_[2]};
+            float m = xs_[3];
             int cell[3];
             float f[3], w[3][4], dw[3][4];
             locate(P, xp[0], xp[1], xp[2], cell, f);
@@ -200,10 +224,10 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
             float Mh[9], b[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                float t = m * cur.v[a][pj];
+                float t = m * xs_[4 + a];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float mh = m * P.apic[c] * cur.B[3 * a + c][pj];
+                    const float mh = m * P.apic[c] * xs_[7 + 3 * a + c];
                     Mh[3 * a + c] = mh;
                     t -= mh * (1.0f + f[c]);
                 }
@@ -266,7 +290,9 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
             t = e;
         }
         __syncwarp();
+        pj_cur = pj_next;
     }
+    cp_async_wait_all();  // a warp without particles still issued its first prefetch
     flush();
     __syncthreads();
     // the tile into the grid, one atomic per nonzero node and channel
