@@ -1057,18 +1057,22 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
     load_tile(P, org, G.vel, G.vbf, tile_v, tile_b);
     // the particle's own loads and weights overlap the tile copy; F_E and the
     // per-particle scalars, read after the gather, are copied to shared memory
-    // asynchronously meanwhile (each thread reads back only its own entries)
+    // asynchronously meanwhile (each thread reads back only its own entries).  The
+    // learned form (kDefer), with its queue code, loads them directly: it is at its
+    // register limit already.
     const bool live = j < n;
     const int pj = live ? perm[j] : 0;
     __shared__ float sF[9][128], sq[128], sm[128], svol[128];
     __shared__ int32_t sid[128];
+    if (!kDefer) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) cp_async4(&sF[k][threadIdx.x], &cur.F[k][pj]);
-    cp_async4(&sq[threadIdx.x], &cur.plastic[pj]);
-    cp_async4(&sm[threadIdx.x], &cur.m[pj]);
-    cp_async4(&svol[threadIdx.x], &cur.vol[pj]);
-    cp_async4(&sid[threadIdx.x], &cur.id[pj]);
-    cp_async_commit();
+        for (int k = 0; k < 9; ++k) cp_async4(&sF[k][threadIdx.x], &cur.F[k][pj]);
+        cp_async4(&sq[threadIdx.x], &cur.plastic[pj]);
+        cp_async4(&sm[threadIdx.x], &cur.m[pj]);
+        cp_async4(&svol[threadIdx.x], &cur.vol[pj]);
+        cp_async4(&sid[threadIdx.x], &cur.id[pj]);
+        cp_async_commit();
+    }
     const int mat = live ? (int)cur.mat[pj] : (int)kClothElement;
     float xp[3] = {cur.x[0][pj], cur.x[1][pj], cur.x[2][pj]};
     int cell[3];
@@ -1139,15 +1143,15 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         return;
     }
     // F update (HS:560-576)
-    cp_async_wait_all();
+    if (!kDefer) cp_async_wait_all();
     float F[9], GF[9], Ftr[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) F[k] = sF[k][threadIdx.x];
+    for (int k = 0; k < 9; ++k) F[k] = kDefer ? cur.F[k][pj] : sF[k][threadIdx.x];
     mat_mul(Gb, F, GF);
 #pragma unroll
     for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
     // return mapping (HS:612-677)
-    float q = sq[threadIdx.x];
+    float q = kDefer ? cur.plastic[pj] : sq[threadIdx.x];
     float U[9], s[3], V[9];
     float Fe[9], sn[3];
     float sprod = 1.0f;  // prod(s_trial / s_new) for J_P
@@ -1264,9 +1268,9 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         nxt.plastic[j] = q;
     }
     nxt.mat[j] = (uint8_t)mat;
-    nxt.m[j] = sm[threadIdx.x];
-    nxt.vol[j] = svol[threadIdx.x];
-    nxt.id[j] = sid[threadIdx.x];
+    nxt.m[j] = kDefer ? cur.m[pj] : sm[threadIdx.x];
+    nxt.vol[j] = kDefer ? cur.vol[pj] : svol[threadIdx.x];
+    nxt.id[j] = kDefer ? cur.id[pj] : sid[threadIdx.x];
     int ncell[3];
     float nf[3];
     bool clamped = locate(P, xn[0], xn[1], xn[2], ncell, nf);
