@@ -49,7 +49,7 @@ namespace {
 
 constexpr int kFlagThreads = 1024;  // slots per block of the flag and stayer kernels
 constexpr int kRankThreads = 256;
-constexpr int kSmallMovers = 512;   // movers placed by the last flag block
+constexpr int kSmallMovers = 32;    // movers placed by the last flag block (one warp each)
 
 // first index i of the ascending a[0, n) with a[i] > k, found by one warp with
 // 32-way probes (about four dependent loads for a million entries)
