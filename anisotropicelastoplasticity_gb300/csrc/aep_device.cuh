@@ -356,6 +356,11 @@ __device__ __forceinline__ float log_t(float x) { return logf(x); }
 __device__ __forceinline__ double log_t(double x) { return log(x); }
 __device__ __forceinline__ float sin_t(float x) { return sinf(x); }
 __device__ __forceinline__ double sin_t(double x) { return sin(x); }
+// division for the Jacobi rotation angle: the angle only has to be close (the
+// rotation stays exactly orthogonal through c = rsqrt(1 + t^2), s = c t, and W = A V
+// holds whatever angle is applied), so FP32 uses the 2-ulp fast division
+__device__ __forceinline__ float rot_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double rot_div(double a, double b) { return a / b; }
 __device__ __forceinline__ float abs_t(float x) { return fabsf(x); }
 __device__ __forceinline__ double abs_t(double x) { return fabs(x); }
 
@@ -381,10 +386,10 @@ __device__ __forceinline__ bool svd3(const T A[9], T U[9], T s[3], T V[9], int m
             T gamma = W[p] * W[q] + W[3 + p] * W[3 + q] + W[6 + p] * W[6 + q];
             if (abs_t(gamma) > tol * sqrt_t(alpha * beta)) {
                 rotated = true;
-                T zeta = (beta - alpha) / (T(2) * gamma);
+                T zeta = rot_div(beta - alpha, T(2) * gamma);
                 T az = abs_t(zeta);
-                T t = az > T(1e15) ? T(0.5) / zeta
-                                   : (zeta >= T(0) ? T(1) : T(-1)) / (az + sqrt_t(T(1) + zeta * zeta));
+                T t = az > T(1e15) ? rot_div(T(0.5), zeta)
+                                   : rot_div(zeta >= T(0) ? T(1) : T(-1), az + sqrt_t(T(1) + zeta * zeta));
                 T c = rsqrt_t(T(1) + t * t), sn = c * t;
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
