@@ -142,9 +142,19 @@ def cpu_baseline(args, steps: int):
     for _ in range(steps):
         orc.step(sc.dt)
     dt = time.perf_counter() - t0
+    # one thread, as the reference runs: one step of the same scene
+    one = Oracle(sc.grid, sc.params, threads=1)
+    one.set_particle_system(sc.particles)
+    one.set_level_set(sc.levelset)
+    one.init(volumes=True)
+    t1 = time.perf_counter()
+    one.step(sc.dt)
+    dt1 = time.perf_counter() - t1
     return {"value": len(sc.particles) * steps / dt, "unit": UNIT, "cores": orc.threads, "kind": "port",
             "sample": f"{steps} full steps of the {len(sc.particles)}-particle sand column (128^3 grid), FP64, "
-                      f"{orc.threads} OpenMP threads, after 1 warm-up step"}
+                      f"{orc.threads} OpenMP threads, after 1 warm-up step",
+            "single_thread": {"value": len(sc.particles) / dt1, "unit": UNIT, "cores": 1,
+                              "sample": "1 full step of the same scene on one thread"}}
 
 
 def run_reference(args):
