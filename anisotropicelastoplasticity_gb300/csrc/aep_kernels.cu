@@ -52,7 +52,7 @@ __global__ void k_keys(KParams P, PArrays cur, int n, uint32_t* keys, DevStats* 
 // D^-1 = 3/h^2 (:177), x_i - x_p = (o - 1 - f) h  =>  w (b + Mh o) with
 // Mh[:,a] = m D^-1 h_a B[:,a] and b = m v - Mh (1 + f).
 constexpr int kP2GThreads = 128;
-constexpr int kP2GChunk = 128;  // particles per warp (4 batches of 32)
+constexpr int kP2GMaxChunk = 128;  // particles per warp at most (the launch picks the chunk)
 // Prep record of one particle, 9 float4 (36 words, 16-byte aligned):
 //   q0 = (b, m)  q1 = Mh[0..3]  q2 = Mh[4..7]  q3 = (Mh[8], T lo, T hi, -)
 //   q4 = wx  q5 = wy  q6 = wz  q7 = (base, key)
@@ -78,15 +78,16 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
     }
 }
 
-// One warp streams through 128 ordered particles run by run (a run: consecutive
+// One warp streams through a chunk of ordered particles (32 to 128, chosen at the
+// launch so that the blocks fill the GPU in whole waves) run by run (a run: consecutive
 // particles with the same base node): lane (l & 15) owns the stencil column
 // (ox, oy) = (l & 3, (l >> 2) & 3), and the half h = l >> 4 takes the run's particles
 // t + h, t + h + 2, ..., accumulating the column's 4 nodes x (mass, momentum) in
 // FP32 registers.  At the end of a run (warp-uniform) the halves' sums are added,
 // half h takes the z-layers 2h, 2h + 1, and the node sums are rounded to fixed
 // point and added as integers: runs whose stencil lies in the block's grid tile
-// (the 2x2x2 node blocks of its first particle, where almost all of its 512
-// particles sit) into a fixed-point copy of the tile in shared memory, which is
+// (the 2x2x2 node blocks of its middle particle, where most of its particles
+// sit) into a fixed-point copy of the tile in shared memory, which is
 // added to the grid once per node at the end; other runs into the grid directly.
 // Integer sums: the result does not depend on the order.
 // Exact mass: rounding the node masses one by one loses the difference between
@@ -97,18 +98,20 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
 // roundings), so it is computed from the low 32 bits of T and of the node masses
 // with one 32-bit warp reduction.
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
-                                                     const int32_t* __restrict__ perm, int n, GArrays G,
+                                                     const int32_t* __restrict__ perm, int n, int chunk, GArrays G,
                                                      int32_t* __restrict__ slot_of, int32_t* __restrict__ curidx_of) {
     __shared__ float4 sm4[(kP2GThreads / 32) * kP2GRegion];
     __shared__ unsigned long long tacc[4 * kTileNodes];  // [channel][tile node]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const region = sm4 + warp * kP2GRegion;
     const int half = lane >> 4, ox = lane & 3, oy = (lane >> 2) & 3;
-    const long blk0 = (long)blockIdx.x * (kP2GThreads / 32) * kP2GChunk;
-    const long chunk0 = blk0 + (long)warp * kP2GChunk;
-    const int cnt_total = (int)max(0L, min((long)kP2GChunk, (long)n - chunk0));  // warp-uniform
+    const long blk0 = (long)blockIdx.x * (kP2GThreads / 32) * chunk;
+    const long chunk0 = blk0 + (long)warp * chunk;
+    const int cnt_total = (int)max(0L, min((long)chunk, (long)n - chunk0));  // warp-uniform
+    // the tile: the node blocks of the block's middle particle (the particles are
+    // ordered by node block: across two node blocks, the middle one's holds half)
     int org[3];
-    tile_origin(P, keys[blk0], org);
+    tile_origin(P, keys[blk0 + (min((long)n, blk0 + (long)(kP2GThreads / 32) * chunk) - 1 - blk0) / 2], org);
     for (int i = threadIdx.x; i < 4 * kTileNodes; i += kP2GThreads) tacc[i] = 0ull;
     __syncthreads();
 
@@ -1830,9 +1833,22 @@ void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, De
 }
 void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
                 const GArrays& G, int32_t* slot_of, int32_t* curidx_of, cudaStream_t s) {
-    long hw = (n + kP2GChunk - 1) / kP2GChunk;
+    // particles per warp: a multiple of 32 (whole batches) that fills the resident
+    // blocks of the device in a whole number of waves, at most kP2GMaxChunk
+    static const long slots = [] {  // resident warps of k_p2g on the device
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_p2g, kP2GThreads, 0);
+        return (long)std::max(1, sms * per) * (kP2GThreads / 32);
+    }();
+    const long waves = std::max(1L, ((long)n + slots * kP2GMaxChunk - 1) / (slots * kP2GMaxChunk));
+    const long per_warp = ((long)n + waves * slots - 1) / (waves * slots);
+    const int chunk = (int)std::min((long)kP2GMaxChunk, std::max(32L, (per_warp + 31) / 32 * 32));
+    const long hw = ((long)n + chunk - 1) / chunk;
     if (n > 0)
-        k_p2g<<<blocks_for(hw, kP2GThreads / 32), kP2GThreads, 0, s>>>(P, cur, keys, perm, n, G, slot_of, curidx_of);
+        k_p2g<<<blocks_for(hw, kP2GThreads / 32), kP2GThreads, 0, s>>>(P, cur, keys, perm, n, chunk, G, slot_of,
+                                                                        curidx_of);
 }
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s) {
     k_normalize<<<grid_blocks, 256, 0, s>>>(P, G, st);
