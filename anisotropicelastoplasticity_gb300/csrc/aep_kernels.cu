@@ -562,7 +562,7 @@ __global__ void k_force_fp64(KParams P, PArrays cur, GArrays G, float dt_force, 
 }
 
 // impulse scatter: f_i -= sum_p stress_p grad w_ip (HS:356-366), stored as dt * f_i
-__global__ void __launch_bounds__(kFrcThreads, 5) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(kFrcThreads, 6) k_force(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                        const int32_t* __restrict__ perm, int n, GArrays G,
                                                        float dt_force, DevStats* st, MeshArrays M,
                                                        int32_t* fp64_list, int fp64_cap) {
