@@ -33,6 +33,23 @@ def test_p2g_grid_matches_oracle(kind):
     assert mass_weighted_rel(g["velocities"], o["velocities"], o["masses"]) < 2e-5
 
 
+@pytest.mark.parametrize("n", [1, 33, 127, 129, 4097, 100003])
+def test_p2g_grid_matches_oracle_at_chunk_boundaries(n):
+    """P2G picks its particles per warp (32 to 128) from the particle count, and
+    each block's grid tile from its middle particle: particle counts around a
+    warp, a block and an uneven last chunk give the oracle's grid."""
+    sc = perturbed(scenes.sand_column(n=n, res=32, seed=n), seed=n + 1)
+    gpu, orc = make_pair(sc)
+    gpu.step_stage(sc.dt, capi.AEP_STAGE_P2G)
+    g = gpu.get_grid()
+    orc.init(volumes=False)
+    o = orc.get_grid()
+    assert max_rel(g["masses"], o["masses"]) < 2e-6
+    assert abs(g["masses"].sum() - o["masses"].sum()) / o["masses"].sum() < 1e-6
+    assert mass_weighted_rel(g["velocities"], o["velocities"], o["masses"]) < 2e-5
+    gpu.close()
+
+
 @pytest.mark.parametrize("kind", KINDS)
 def test_force_scatter_matches_oracle(kind):
     sc = perturbed(small_scene(kind), seed=12)
