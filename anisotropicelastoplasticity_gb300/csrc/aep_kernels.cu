@@ -78,8 +78,8 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
     }
 }
 
-// One warp streams through a chunk of ordered particles (32 to 128, chosen at the
-// launch so that the blocks fill the GPU in whole waves) run by run (a run: consecutive
+// One warp streams through a chunk of ordered particles (32 to 128: the particles
+// spread evenly over the fewest waves of resident warps) run by run (a run: consecutive
 // particles with the same base node): lane (l & 15) owns the stencil column
 // (ox, oy) = (l & 3, (l >> 2) & 3), and the half h = l >> 4 takes the run's particles
 // t + h, t + h + 2, ..., accumulating the column's 4 nodes x (mass, momentum) in
@@ -1833,8 +1833,9 @@ void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, De
 }
 void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
                 const GArrays& G, int32_t* slot_of, int32_t* curidx_of, cudaStream_t s) {
-    // particles per warp: a multiple of 32 (whole batches) that fills the resident
-    // blocks of the device in a whole number of waves, at most kP2GMaxChunk
+    // particles per warp: the particles spread evenly over the fewest waves of the
+    // device's resident warps with at most kP2GMaxChunk each, rounded up to a
+    // multiple of 32 (whole batches)
     static const long slots = [] {  // resident warps of k_p2g on the device
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
