@@ -50,6 +50,7 @@ namespace {
 constexpr int kFlagThreads = 1024;  // slots per block of the flag and stayer kernels
 constexpr int kRankThreads = 256;
 constexpr int kSmallMovers = 32;    // movers placed by the last flag block (one warp each)
+constexpr int kMoverBlocks = 256;   // k_place_movers: 2,048 warps, a mover each (more: in turn)
 
 // first index i of the ascending a[0, n) with a[i] > k, found by one warp with
 // 32-way probes (about four dependent loads for a million entries)
@@ -99,7 +100,7 @@ __device__ __forceinline__ void place_mover(int i, int m, const uint32_t* __rest
 }
 
 // counters: [0] movers, [1] finished flag blocks
-__global__ void __launch_bounds__(kFlagThreads) k_flag_movers(const uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(kFlagThreads, 2) k_flag_movers(const uint32_t* __restrict__ keys,
                                                               const uint32_t* __restrict__ prev, int n, int cap,
                                                               uint32_t* __restrict__ mask, int32_t* __restrict__ blk,
                                                               uint32_t* __restrict__ mk, int32_t* __restrict__ mj,
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(kFlagThreads) k_flag_movers(const uint32_t* __
     }
 }
 
-// placement of up to kBruteMovers movers, one warp each
+// placement of up to kBruteMovers movers, one warp each (grid-stride over the movers)
 __global__ void __launch_bounds__(kRankThreads) k_place_movers(const uint32_t* __restrict__ prev, int n, int cap,
                                                                const uint32_t* __restrict__ mk,
                                                                const int32_t* __restrict__ mj,
@@ -180,9 +181,9 @@ __global__ void __launch_bounds__(kRankThreads) k_place_movers(const uint32_t* _
                                                                int32_t* __restrict__ mpos) {
     const int m = counters[0];
     if (m > cap || m > kBruteMovers) return;  // the full-sort branch (never launched with these)
-    const int i = (int)(((long)blockIdx.x * kRankThreads + threadIdx.x) >> 5);
-    if (i >= m) return;
-    place_mover(i, m, prev, n, mk, mj, mkeys, mslot, mpos, threadIdx.x & 31);
+    const int warps = (int)(((long)gridDim.x * kRankThreads) >> 5);
+    for (int i = (int)(((long)blockIdx.x * kRankThreads + threadIdx.x) >> 5); i < m; i += warps)  // warp-uniform
+        place_mover(i, m, prev, n, mk, mj, mkeys, mslot, mpos, threadIdx.x & 31);
 }
 
 // stayer j: (stayers before j) + (movers with key < key_j); threads t < m also
@@ -285,8 +286,8 @@ cudaError_t order_graph_build(void** out, cudaStream_t cs, const OrderBuffers& b
     for (int c = 0; c < 2; ++c) {
         OG_CK(cudaStreamBeginCaptureToGraph(cs, body[c], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
         if (c == 1)
-            k_place_movers<<<(unsigned)((32l * kBruteMovers + kRankThreads - 1) / kRankThreads), kRankThreads, 0,
-                             cs>>>(b.keys_sorted, n, b.cap, b.mk, b.mj, counters, b.mkeys, b.mslot, b.mpos);
+            k_place_movers<<<kMoverBlocks, kRankThreads, 0, cs>>>(b.keys_sorted, n, b.cap, b.mk, b.mj, counters,
+                                                                  b.mkeys, b.mslot, b.mpos);
         k_place_stayers<<<nb, kFlagThreads, 0, cs>>>(b.keys, n, b.cap, mask, blk, b.mkeys, b.mslot, b.mpos, counters,
                                                      b.keys_sorted, b.perm);
         OG_CK(cudaGetLastError());
