@@ -1,0 +1,74 @@
+"""Run one of the seeded scenes for a number of steps and print one JSON line with
+the step time and the per-kernel CUDA-event times:
+
+    python -m anisotropicelastoplasticity_gb300.run_scene cloth_drape --steps 20
+
+Scenes: snow_block (32,768 particles, 64^3), sand_column (524,288, 128^3),
+cloth_drape (65,536 vertices + 130,050 elements, 128^3), snow_sand_collision
+(2,097,152, 256^3), sand_cloth (8,388,608 items, 512^3).  The steps are timed
+twice: once with a start and an end event each, then again with the library's
+events between its kernels (which add a few microseconds per step) for the
+per-kernel times."""
+import argparse
+import json
+import sys
+
+from . import HybridSolver, scenes
+
+SCENES = {
+    "snow_block": scenes.snow_block,
+    "sand_column": scenes.sand_column,
+    "cloth_drape": scenes.cloth_drape,
+    "snow_sand_collision": scenes.snow_sand_collision,
+    "sand_cloth": scenes.sand_cloth,
+}
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("scene", choices=sorted(SCENES))
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    args = ap.parse_args(argv)
+    import torch
+
+    sc = SCENES[args.scene]()
+    s = HybridSolver(sc.particles, sc.grid, sc.params)
+    if sc.mesh is not None:
+        s.set_lagrangian_mesh(sc.mesh)
+    s.set_level_set(sc.levelset)
+    stream = torch.cuda.Stream()
+    s.set_stream(stream.cuda_stream)
+    s.init_volumes()
+    for _ in range(args.warmup):
+        s.step(sc.dt)
+    s.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for a, b in ev:
+            a.record(stream)
+            s.step(sc.dt)
+            b.record(stream)
+    s.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / max(args.steps, 1)
+    s.set_profiling(True)
+    for _ in range(args.steps):
+        s.step(sc.dt)
+    s.synchronize()
+    phases, k = s.phase_times()
+    s.set_profiling(False)
+    st = s.stats()
+    s.close()
+    items = sc.num_items()
+    print(json.dumps({
+        "scene": args.scene, "items": items, "grid": [int(r) for r in sc.grid.resolution], "dt": sc.dt,
+        "steps": args.steps, "ms_per_step": ms, "item_steps_per_s": items / (ms * 1e-3),
+        "phases_ms_per_step": {p: v / max(k, 1) for p, v in phases.items()},
+        "active_nodes": st["active_nodes"], "fp64_fallbacks_last_step": st["fp64_fallbacks"],
+        "total_mass": st["total_mass"],
+    }))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
