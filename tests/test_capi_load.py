@@ -66,3 +66,20 @@ def test_struct_layout_matches_header(tmp_path):
             C.sizeof(capi.aep_stats), capi.aep_params.friction_bug.offset, capi.aep_params.mass_bits.offset,
             capi.aep_stats.total_mass.offset]
     assert got == want
+
+
+def test_scene_runner_parses_its_arguments(capsys):
+    """The scene runner (python -m anisotropicelastoplasticity_gb300.run_scene) lists
+    the five seeded scenes and rejects others before touching a GPU."""
+    import pytest
+
+    from anisotropicelastoplasticity_gb300 import run_scene
+
+    assert sorted(run_scene.SCENES) == ["cloth_drape", "sand_cloth", "sand_column", "snow_block",
+                                        "snow_sand_collision"]
+    with pytest.raises(SystemExit) as e:
+        run_scene.main(["--help"])
+    assert e.value.code == 0
+    with pytest.raises(SystemExit) as e:
+        run_scene.main(["no_such_scene"])
+    assert e.value.code == 2
