@@ -252,6 +252,19 @@ __device__ __forceinline__ void tile_origin(const KParams& P, uint32_t key, int 
     org[2] = (int)(r / (uint32_t)P.nb[1]);
 }
 
+// Programmatic dependent launch within a step: a kernel launched with the
+// programmatic-serialisation attribute may be scheduled while the kernel before it
+// in the stream finishes.  pdl_entry() first lets the next kernel be launched once
+// every block of this one has started (pdl_trigger), then waits until the previous
+// kernel has completed and its memory is visible (griddepcontrol.wait), before
+// this kernel reads or writes anything.  Both are no-ops for a kernel launched
+// without the attribute.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_entry() {
+    pdl_trigger();
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // asynchronous 4-byte copy global -> shared (cp.async; no registers held while in
 // flight), its commit and the wait for all of this thread's copies
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {

@@ -23,6 +23,7 @@
 // particle); __match_any_sync + __ballot_sync find the run structure of each
 // batch of 16 particles.
 #include <algorithm>
+#include <utility>
 
 #include <cooperative_groups.h>
 
@@ -100,6 +101,7 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, const uint32_t* __restrict__ keys,
                                                      const int32_t* __restrict__ perm, int n, int chunk, GArrays G,
                                                      int32_t* __restrict__ slot_of, int32_t* __restrict__ curidx_of) {
+    pdl_trigger();  // the normalisation may launch once every block has started
     __shared__ float4 sm4[(kP2GThreads / 32) * kP2GRegion];
     __shared__ unsigned long long tacc[4 * kTileNodes];  // [channel][tile node]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -317,6 +319,7 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
 // for the force impulse; exact int64 totals of mass and momentum (summed per block,
 // one atomic per block and total).  Launched with 256 threads.
 __global__ void __launch_bounds__(256) k_normalize(KParams P, GArrays G, DevStats* st) {
+    pdl_entry();
     __shared__ long long red[5][8];
     const int nact = *G.nactive;
     const long total = (long)nact * 64;
@@ -501,6 +504,7 @@ __device__ void particle_stress_impulse(const KParams& P, const float4* vel, con
 // not matter).  Grid-stride over the list; usually empty.
 __global__ void k_force_fp64(KParams P, PArrays cur, GArrays G, float dt_force, DevStats* st,
                              const int32_t* __restrict__ fp64_list, int fp64_cap) {
+    pdl_entry();
     dt_force = step_dt(P, dt_force, 0);
     const int count = min((int)st->force_fp64, fp64_cap);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
@@ -566,6 +570,7 @@ __global__ void __launch_bounds__(kFrcThreads, 6) k_force(KParams P, PArrays cur
                                                        const int32_t* __restrict__ perm, int n, GArrays G,
                                                        float dt_force, DevStats* st, MeshArrays M,
                                                        int32_t* fp64_list, int fp64_cap) {
+    pdl_entry();
     __shared__ float4 sm4[(kFrcThreads / 32) * kFrcWarpBuf];
     __shared__ float4 tile_v[kTileNodes];
     dt_force = step_dt(P, dt_force, 0);
@@ -711,6 +716,7 @@ __global__ void __launch_bounds__(kFrcThreads, 6) k_force(KParams P, PArrays cur
 // accumulated per vertex in fixed point, and the element normal/shear stress
 // (HybridSolver.cpp:389-442) stored for the element's scatter in k_force.
 __global__ void k_cloth_force(KParams P, PArrays cur, MeshArrays M, float dt_force) {
+    pdl_entry();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= M.nf) return;
     dt_force = step_dt(P, dt_force, 0);
@@ -741,6 +747,7 @@ __global__ void k_cloth_force(KParams P, PArrays cur, MeshArrays M, float dt_for
 // grid velocity update + gravity (HS:725-737, 457) and level-set collision with
 // friction (HS:460-511), fused; clears the accumulators and block flags.
 __global__ void k_grid(KParams P, GArrays G, float dt_force, int write_force, double* force_out) {
+    pdl_entry();
     const int nact = *G.nactive;
     const long total = (long)nact * 64;
     if ((long)blockIdx.x * blockDim.x >= total) return;  // no node for this block
@@ -1053,6 +1060,7 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
                                              int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
                                              DevStats* st, Harvest H, const uint32_t* __restrict__ keys_sorted,
                                              MlpQueue Qu) {
+    pdl_entry();
     __shared__ float4 tile_v[kTileNodes], tile_b[kTileNodes];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     int org[3];
@@ -1330,6 +1338,7 @@ constexpr int kFinThreads = 128;
 __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays cur, PArrays nxt, MlpQueue Qu,
                                                             DevStats* st, MlpParams mlp, float tol_rel,
                                                             float tol_abs) {
+    pdl_entry();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int rows = (int)min(st->mlp_rows, (unsigned)Qu.cap);
     if ((long)blockIdx.x * kFinThreads >= rows) return;  // no tile for this block (block-uniform)
@@ -1424,6 +1433,7 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
                                                    float dt, uint32_t* __restrict__ keys_next, DevStats* st,
                                                    Harvest H, MlpParams mlp, int use_mlp, float tol_rel,
                                                    float tol_abs) {
+    pdl_entry();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = e < M.nf;
@@ -1828,6 +1838,25 @@ __global__ void k_grid_dense(KParams P, GArrays G, double* mass, double* vel, do
 // host launchers
 static inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
 
+// A launch that may overlap the tail of the previous kernel in the stream (the
+// kernel waits for it in pdl_entry before touching memory): hides the launch
+// latency between the kernels of a step.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, DevStats* st, cudaStream_t s) {
     if (n > 0) k_keys<<<blocks_for(n, 256), 256, 0, s>>>(P, cur, n, keys, st);
 }
@@ -1852,22 +1881,22 @@ void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, cons
                                                                         curidx_of);
 }
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s) {
-    k_normalize<<<grid_blocks, 256, 0, s>>>(P, G, st);
+    launch_pdl(k_normalize, grid_blocks, 256, 0, s, P, G, st);
 }
 void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
                   const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s,
                   int32_t* fp64_list) {
     long warps = (n + 31) / 32;
-    if (M.nf > 0) k_cloth_force<<<blocks_for(M.nf, 128), 128, 0, s>>>(P, cur, M, dt_force);
+    if (M.nf > 0) launch_pdl(k_cloth_force, blocks_for(M.nf, 128), 128, 0, s, P, cur, M, dt_force);
     if (n > 0) {
-        k_force<<<blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s>>>(P, cur, keys, perm, n, G, dt_force, st, M,
-                                                                            fp64_list, n);
-        k_force_fp64<<<8, 128, 0, s>>>(P, cur, G, dt_force, st, fp64_list, n);
+        launch_pdl(k_force, blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s, P, cur, keys, perm, n, G, dt_force,
+                   st, M, fp64_list, n);
+        launch_pdl(k_force_fp64, 8, 128, 0, s, P, cur, G, dt_force, st, (const int32_t*)fp64_list, n);
     }
 }
 void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
                  int grid_blocks, cudaStream_t s) {
-    k_grid<<<grid_blocks, 256, 0, s>>>(P, G, dt_force, write_force, force_out);
+    launch_pdl(k_grid, grid_blocks, 256, 0, s, P, G, dt_force, write_force, force_out);
 }
 void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s) {
     k_grid_clear<<<grid_blocks, 256, 0, s>>>(G);
@@ -1878,8 +1907,8 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
                 const MlpQueue& Qu) {
     if (n > 0) {
         if (mlp) {
-            k_g2p<true><<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H, keys_sorted,
-                                                          Qu);
+            launch_pdl(k_g2p<true>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
+                       keys_sorted, Qu);
             const int smem = kMlpSmemBytes + (kFinThreads / 32) * kMlpWarpBytes;
             cudaFuncSetAttribute(k_mlp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             int dev = 0, sms = 0, per_sm = 0;
@@ -1887,17 +1916,17 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_finish, kFinThreads, smem);
             const int blocks = std::min(blocks_for(Qu.cap, kFinThreads), std::max(1, sms * std::max(per_sm, 1)));
-            k_mlp_finish<<<blocks, kFinThreads, smem, s>>>(P, cur, nxt, Qu, st, *mlp, tol_rel, tol_abs);
+            launch_pdl(k_mlp_finish, blocks, kFinThreads, smem, s, P, cur, nxt, Qu, st, *mlp, tol_rel, tol_abs);
         } else {
-            k_g2p<false><<<blocks_for(n, 128), 128, 0, s>>>(P, cur, nxt, perm, n, G, dt, keys_next, st, H,
-                                                           keys_sorted, Qu);
+            launch_pdl(k_g2p<false>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
+                       keys_sorted, Qu);
         }
     }
     if (M.nf > 0) {
         const int smem = mlp ? kMlpSmemBytes + 4 * kMlpWarpBytes : 0;
         if (mlp) cudaFuncSetAttribute(k_cloth_g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_cloth_g2p<<<blocks_for(M.nf, 128), 128, smem, s>>>(P, cur, nxt, G, M, dt, keys_next, st, H,
-                                                             mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, tol_rel, tol_abs);
+        launch_pdl(k_cloth_g2p, blocks_for(M.nf, 128), 128, smem, s, P, cur, nxt, G, M, dt, keys_next, st, H,
+                   mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, tol_rel, tol_abs);
     }
 }
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
