@@ -204,7 +204,38 @@ class AepError(RuntimeError):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
 
 
+# The reference's literal values, the same table as aep_default_params in
+# csrc/aep_capi.cu (tests/test_capi_load.py checks that the two agree).  Filled here
+# in Python so that building a scene does not load libaep.so: the CPU arms of the
+# benchmark construct the same scenes without mapping the GPU library.
+_DEFAULTS = {
+    "snow": {"E": 1.4e5, "nu": 0.2, "theta_c": 2.5e-2, "theta_s": 7.5e-3, "xi": 10.0},  # ParticleSystem.cpp:173-176, HS:267
+    "sand": {"E": 3.537e5, "nu": 0.3, "h0": 35.0, "h1": 9.0, "h2": 0.2, "h3": 10.0},  # ParticleSystem.cpp:233-234, HS:641-644
+    "gravity": (0.0, 0.0, -9.8),  # HybridSolver.cpp:457
+    "friction": 0.2,  # HybridSolver.cpp:465
+    "friction_bug": 1,  # HybridSolver.cpp:500-501
+    "track_plastic_F": 0,
+    "particle_damp": 0.0,  # HybridSolver.cpp:916
+    "mesh_damp": 1.0,  # HybridSolver.cpp:926,932
+    "mass_bits": 34,
+    "momentum_bits": 40,
+    "cloth_volume_weighting": 0,
+    "full_sort": 0,
+    "reorder_interval": 4,
+}
+
+
 def default_params() -> aep_params:
+    """aep_params with the reference's literal values (no library call)."""
     p = aep_params()
-    load().aep_default_params(C.byref(p))
+    for k, v in _DEFAULTS.items():
+        if isinstance(v, dict):
+            sub = getattr(p, k)
+            for kk, vv in v.items():
+                setattr(sub, kk, vv)
+        elif k == "gravity":
+            for a in range(3):
+                p.gravity[a] = v[a]
+        else:
+            setattr(p, k, v)
     return p

@@ -1112,6 +1112,64 @@ size_t ckpt_bytes(int64_t n, int64_t nf, int nfixed, int nfa) {
            (size_t)nf * (3 * sizeof(int32_t) + 6 * sizeof(float)) + (size_t)nfixed * sizeof(int32_t);
 }
 
+// Host-side check of a checkpoint blob whose header and size are consistent, with
+// the rules the uploads apply (aep_solver_create's parameter bounds, aep_set_particles'
+// material tags, aep_set_mesh's face indices, aep_set_levelset's shape types) plus
+// the invariants the kernels index with: ids a permutation of [0, n) with the tag
+// their range implies, the saved ordering keys ascending inside the padded grid, and
+// fixed vertices inside the mesh.  Nothing reaches the device before it passes.
+const char* ckpt_invalid(const CkptHeader& h, const char* body, int nblocks) {
+    const aep_params& p = h.prm;
+    if (p.mass_bits <= 0 || p.mass_bits > 50 || p.momentum_bits <= 0 || p.momentum_bits > 50)
+        return "fixed-point bits out of range";
+    if (p.reorder_interval < 0 || (p.friction_bug | 1) != 1 || (p.track_plastic_F | 1) != 1 ||
+        (p.full_sort | 1) != 1 || (p.cloth_volume_weighting | 1) != 1)
+        return "bad parameter flags";
+    if (h.steps < 0 || h.since_order < 0 || (h.prev_sorted | 1) != 1) return "bad step counters";
+    for (int k = 0; k < h.nshapes; ++k)
+        if (h.shapes[k].type < kSdfPlane || h.shapes[k].type > kSdfWall2Ground) return "unknown level-set shape";
+    const size_t n = (size_t)h.n;
+    const uint8_t* mat = reinterpret_cast<const uint8_t*>(body + sizeof(float) * n * (size_t)h.float_arrays);
+    const char* ids_raw = reinterpret_cast<const char*>(mat + n);
+    const char* keys_raw = ids_raw + sizeof(int32_t) * n;
+    std::vector<uint8_t> seen(n, 0);
+    for (size_t j = 0; j < n; ++j) {
+        int32_t id;
+        std::memcpy(&id, ids_raw + sizeof(int32_t) * j, sizeof(id));
+        if (id < 0 || (int64_t)id >= h.n || seen[(size_t)id]) return "particle ids are not a permutation";
+        seen[(size_t)id] = 1;
+        const int want = id < h.np ? -1 : (id < h.np + h.nv ? kClothVertex : kClothElement);
+        if (want < 0 ? mat[j] > kSand : mat[j] != want) return "material tag does not match the item";
+    }
+    if (h.prev_sorted) {
+        const uint64_t key_end = (uint64_t)nblocks * 64;
+        uint32_t last = 0;
+        for (size_t j = 0; j < n; ++j) {
+            uint32_t k;
+            std::memcpy(&k, keys_raw + sizeof(uint32_t) * j, sizeof(k));
+            if ((uint64_t)k >= key_end || (j > 0 && k < last)) return "ordering keys not ascending inside the grid";
+            last = k;
+        }
+    }
+    const char* q = keys_raw + sizeof(uint32_t) * n;
+    if (h.nf > 0) {
+        for (int64_t i = 0; i < 3 * h.nf; ++i) {
+            int32_t v;
+            std::memcpy(&v, q + sizeof(int32_t) * i, sizeof(v));
+            if (v < 0 || v >= h.nv) return "face index out of range";
+        }
+        for (int k = 0; k < 5; ++k)
+            if (!std::isfinite(h.cloth[k])) return "bad cloth parameters";
+        q += sizeof(int32_t) * 3 * h.nf + sizeof(float) * 6 * h.nf;
+    }
+    for (int i = 0; i < h.nfixed; ++i) {
+        int32_t v;
+        std::memcpy(&v, q + sizeof(int32_t) * i, sizeof(v));
+        if (v < 0 || v >= h.nv) return "fixed vertex out of range";
+    }
+    return nullptr;
+}
+
 }  // namespace
 
 aep_status aep_checkpoint_size(aep_solver* s, int64_t* bytes) {
@@ -1188,6 +1246,8 @@ aep_status aep_checkpoint_load(aep_solver* s, const void* buf, int64_t bytes) {
     for (int a = 0; a < 3; ++a)
         if (h.grid.res[a] != s->grid.res[a] || h.grid.min[a] != s->grid.min[a] || h.grid.max[a] != s->grid.max[a])
             return fail(s, AEP_INVALID_ARG, "aep_checkpoint_load: the grid differs from the handle's");
+    if (const char* why = ckpt_invalid(h, static_cast<const char*>(buf) + sizeof(h), s->nblocks))
+        return fail(s, AEP_INVALID_ARG, std::string("aep_checkpoint_load: ") + why);
     CK(cudaStreamSynchronize(s->stream));
     free_mesh(s);
     free_particles(s);

@@ -10,18 +10,19 @@
 //   k_g2p        G2P velocity, APIC, advection, F update, return mapping
 //                (HS:739-825, 940-951, 553-577, 612-681)
 //
-// Scatter design (P2G and force): particles are sorted so that all particles
-// with the same stencil base node are contiguous.  A half-warp (16 lanes)
-// streams through a chunk of sorted particles; lane l owns the four stencil
-// nodes (l&3, l>>2, 0..3) and accumulates their contributions in FP32
-// registers in a fixed particle order.  When the base node changes, the lane
-// converts its sums to int64 fixed point and adds them to the grid with
-// 64-bit atomics.  Integer addition is associative, so the grid sums are
-// order-independent and the step repeats bit-for-bit.  Same-node
-// contributions of all particles that share a base node are merged in
-// registers before any atomic (one atomic per node per run instead of one per
-// particle); __match_any_sync + __ballot_sync find the run structure of each
-// batch of 16 particles.
+// Scatter design (P2G and force): particles are ordered so that all particles
+// with the same stencil base node are contiguous.  A warp streams through a
+// chunk of ordered particles; lane l owns the stencil column (l&3, (l>>2)&3)
+// and accumulates its nodes' contributions in FP32 registers in a fixed
+// particle order.  When the base node changes, the lanes convert their sums to
+// int64 fixed point and add them to the grid with 64-bit atomics.  Integer
+// addition is associative, so the grid sums are order-independent and the step
+// repeats bit-for-bit.  Same-node contributions of all particles that share a
+// base node are merged in registers before any atomic (one atomic per node per
+// run instead of one per particle).  The run structure of each batch of 32
+// particles comes from comparing each lane's key with the previous lane's
+// (__shfl_up_sync) and a __ballot_sync of the run heads: on ordered keys that
+// is the grouping __match_any_sync would give, at the cost of one shuffle.
 #include <algorithm>
 #include <utility>
 
@@ -1912,13 +1913,18 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
         if (mlp) {
             launch_pdl(k_g2p<true>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
                        keys_sorted, Qu);
-            const int smem = kMlpSmemBytes + (kFinThreads / 32) * kMlpWarpBytes;
-            cudaFuncSetAttribute(k_mlp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            int dev = 0, sms = 0, per_sm = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_finish, kFinThreads, smem);
-            const int blocks = std::min(blocks_for(Qu.cap, kFinThreads), std::max(1, sms * std::max(per_sm, 1)));
+            constexpr int smem = kMlpSmemBytes + (kFinThreads / 32) * kMlpWarpBytes;
+            // resident finisher blocks of the device, looked up once (the attribute is
+            // set with it, before the first launch)
+            static const int resident = [] {
+                cudaFuncSetAttribute(k_mlp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+                int dev = 0, sms = 0, per_sm = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_finish, kFinThreads, smem);
+                return std::max(1, sms * std::max(per_sm, 1));
+            }();
+            const int blocks = std::min(blocks_for(Qu.cap, kFinThreads), resident);
             launch_pdl(k_mlp_finish, blocks, kFinThreads, smem, s, P, cur, nxt, Qu, st, *mlp, tol_rel, tol_abs);
         } else {
             launch_pdl(k_g2p<false>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
@@ -1926,8 +1932,15 @@ void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const 
         }
     }
     if (M.nf > 0) {
-        const int smem = mlp ? kMlpSmemBytes + 4 * kMlpWarpBytes : 0;
-        if (mlp) cudaFuncSetAttribute(k_cloth_g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        constexpr int kClothMlpSmem = kMlpSmemBytes + 4 * kMlpWarpBytes;
+        const int smem = mlp ? kClothMlpSmem : 0;
+        if (mlp) {
+            static const bool attr_set = [] {  // once per process, before the first learned launch
+                cudaFuncSetAttribute(k_cloth_g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, kClothMlpSmem);
+                return true;
+            }();
+            (void)attr_set;
+        }
         launch_pdl(k_cloth_g2p, blocks_for(M.nf, 128), 128, smem, s, P, cur, nxt, G, M, dt, keys_next, st, H,
                    mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, tol_rel, tol_abs);
     }

@@ -4,9 +4,8 @@
 // Who needs it: code that runs inside a host application which owns every byte
 // of device memory through its own pool (a renderer or another framework with a
 // caching allocator, where a stray cudaMalloc breaks its budget or fragments its
-// heap), code that runs while the application is capturing a CUDA graph (an
-// allocation there is not allowed), and real-time loops that cannot pay for the
-// device-wide synchronisation a cudaMalloc/cudaFree implies.  Such callers pass
+// heap), and real-time loops that cannot pay for the device-wide synchronisation
+// a cudaMalloc/cudaFree implies.  Such callers pass
 // their particle arrays and their output grid as device pointers; the only other
 // memory this path touches is a fixed scratch array compiled into the library.
 //
@@ -33,7 +32,8 @@ std::mutex g_setup_mutex;
 unsigned long long* g_scratch_on_device[kMaxDevices] = {};
 
 // Device address of the scratch on the current device; looked up on the first
-// call made on each device (with that device current).
+// call made on each device (with that device current) and kept for the life of
+// the process (not valid after a cudaDeviceReset of that device).
 cudaError_t scratch_for_current_device(unsigned long long** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

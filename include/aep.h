@@ -417,8 +417,9 @@ aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_t
 
 /* No counterpart in the reference.  For callers that must not allocate GPU memory:
  * code running inside a host application that owns all device memory through its
- * own pool, code running while a CUDA graph is being captured, or real-time loops
- * that cannot afford the synchronisation of cudaMalloc/cudaFree.  It performs the
+ * own pool (a stray cudaMalloc breaks its budget or fragments its heap), or
+ * real-time loops that cannot afford the device-wide synchronisation of
+ * cudaMalloc/cudaFree.  It performs the
  * step's particle-to-grid transfer (mass and APIC momentum, then v = p / m) from
  * the caller's device arrays into the caller's device output arrays, and allocates
  * nothing: its only working memory is a fixed array compiled into the library
@@ -435,10 +436,12 @@ aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_t
  * Limits: the padded grid, ((res+2)/4 + 2)^3 * 64 nodes, must not exceed
  * AEP_NOALLOC_MAX_NODES (a 64^3 grid fits); larger grids return AEP_CAPACITY.
  * The first call on a device looks up the device address of the fixed array
- * (cudaGetSymbolAddress); make that first call before any stream capture begins.
- * Every call shares the one array and clears the part it uses at its start, so
- * calls that can overlap on the GPU (different streams, or different host
- * threads) race and must be serialised by the caller.                          */
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; make that
+ * first call before any stream capture begins.  The kept address is not valid
+ * after cudaDeviceReset on that device: a process that resets a device must not
+ * call this entry point on it again.  Every call shares the one array and clears
+ * the part it uses at its start, so calls that can overlap on the GPU (different
+ * streams, or different host threads) race and must be serialised by the caller. */
 #define AEP_NOALLOC_MAX_NODES 373248
 aep_status aep_p2g_noalloc(const aep_grid_desc* grid, int64_t n,
                            const float* x, const float* v, const float* B, const float* m,

@@ -40,6 +40,24 @@ def test_no_device_calls_without_gpu_are_safe():
     p = capi.default_params()
     assert p.gravity[2] == -9.8 and p.friction == 0.2 and p.friction_bug == 1
     assert p.sand.h0 == 35.0 and p.snow.xi == 10.0
+    # the Python table (used where libaep.so must not be loaded) equals the library's
+    q = capi.aep_params()
+    lib.aep_default_params(C.byref(q))
+    assert bytes(p) == bytes(q)
+
+
+def test_scenes_do_not_load_the_gpu_library():
+    """The CPU arms of the benchmark build scenes without mapping libaep.so."""
+    import subprocess
+    import sys
+
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from anisotropicelastoplasticity_gb300 import scenes, capi\n"
+            "scenes.sand_column(n=1000, res=32); scenes.sand_cloth(nside=16, n_sand=1000, res=32)\n"
+            "assert capi._lib is None\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libaep.so' not in maps\n" % str(ROOT))
+    subprocess.run([sys.executable, "-c", code], check=True)
 
 
 def test_null_arguments_rejected():

@@ -1,6 +1,9 @@
 """Full-state checkpoint (bit-exact resume) and the interpolation-weight query
 (one row of HybridSolver::evaluateInterpolationWeights_, HybridSolver.cpp:18-97)
 against the oracle's weights."""
+import ctypes
+import struct
+
 import numpy as np
 import pytest
 
@@ -81,6 +84,61 @@ def test_checkpoint_rejects_other_grid_and_garbage():
         a.load_checkpoint(b"not a checkpoint" * 40)
     with pytest.raises(capi.AepError):
         a.load_checkpoint(blob[:-4])
+
+
+def test_checkpoint_load_rejects_corrupted_contents():
+    """A blob whose header and size are consistent but whose contents break what the
+    kernels index with (a face index, a fixed vertex, a material tag, an id, the
+    fixed-point bits of the parameters) is refused before anything reaches the GPU,
+    and the handle keeps working afterwards."""
+    from .test_cloth_gpu import _edge_fixed, small_cloth
+
+    grid, ps, mesh, ls, prm = small_cloth(True, seed=4)
+    a = HybridSolver(None, grid, prm)
+    a.set_particle_system(ps)
+    a.set_lagrangian_mesh(mesh)
+    a.set_level_set(ls)
+    a.bind_constraints(_edge_fixed(mesh))
+    a.init_volumes()
+    a.step(2e-5)
+    blob = a.checkpoint()
+    n = len(ps) + len(mesh.vertex_positions) + len(mesh.faces)
+    nv, nf = len(mesh.vertex_positions), len(mesh.faces)
+    nfixed = int((_edge_fixed(mesh) != 0).sum())
+    nfa = 27  # x, v, B, F, m, vol, plastic (no F_P)
+    body = n * (4 * nfa + 1 + 4 + 4) + nf * (12 + 24) + 4 * nfixed
+    hdr = len(blob) - body
+    assert hdr > 0
+    mat_off = hdr + 4 * nfa * n
+    ids_off = mat_off + n
+    faces_off = ids_off + 8 * n
+    fixed_off = faces_off + nf * (12 + 24)
+    prm_off = 8 + 8 + 40 + ctypes.sizeof(capi.aep_grid_desc)  # magic, version + float arrays, 5 int64, grid
+    mass_bits_off = prm_off + capi.aep_params.mass_bits.offset
+    assert struct.unpack_from("<i", blob, mass_bits_off)[0] == prm.mass_bits
+
+    def corrupt(off, fmt, value):
+        b = bytearray(blob)
+        struct.pack_into(fmt, b, off, value)
+        return bytes(b)
+
+    bad = {"face index": corrupt(faces_off + 4 * 7, "<i", nv + 3),
+           "negative face index": corrupt(faces_off, "<i", -1),
+           "fixed vertex": corrupt(fixed_off, "<i", nv),
+           "material tag": corrupt(mat_off + 5, "<B", 7),
+           "id": corrupt(ids_off + 4 * 2, "<i", n + 100),
+           "mass bits": corrupt(mass_bits_off, "<i", 99)}
+    b = HybridSolver(None, grid, prm)
+    for what, blob_bad in bad.items():
+        with pytest.raises(capi.AepError) as e:
+            b.load_checkpoint(blob_bad)
+        assert e.value.status == capi.AEP_INVALID_ARG, what
+    b.mesh = mesh
+    b.load_checkpoint(blob)  # the intact blob still loads and steps
+    b.step(2e-5)
+    a.step(2e-5)
+    for k, v in a.get_mesh().items():
+        assert np.array_equal(b.get_mesh()[k], v), k
 
 
 def test_weights_match_oracle_rows():
