@@ -75,7 +75,7 @@ class aep_params(C.Structure):
         ("cloth_volume_weighting", C.c_int32),
         ("full_sort", C.c_int32),
         ("reorder_interval", C.c_int32),
-        ("reserved_i", C.c_int32),
+        ("fp64_apex", C.c_int32),
         ("reserved", C.c_int64 * 5),
     ]
 
@@ -96,7 +96,8 @@ class aep_stats(C.Structure):
         ("sort_movers", C.c_int64),
         ("learned_exact", C.c_int64),
         ("orderings", C.c_int64),
-        ("reserved", C.c_double * 2),
+        ("fp64_apex", C.c_int64),
+        ("reserved", C.c_double * 1),
     ]
 
 
@@ -130,6 +131,7 @@ SIGNATURES = {
     "aep_set_mesh": (C.c_int, [_solver_p, C.c_int64, C.c_int64, _dp, C.POINTER(C.c_int32), _dp, _dp, _dp, _dp, _dp,
                                _dp, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
     "aep_get_mesh": (C.c_int, [_solver_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "aep_set_mesh_state": (C.c_int, [_solver_p, C.c_int64, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "aep_init_volumes": (C.c_int, [_solver_p]),
     "aep_step": (C.c_int, [_solver_p, C.c_double]),
     "aep_synchronize": (C.c_int, [_solver_p]),
@@ -153,6 +155,9 @@ SIGNATURES = {
     "aep_p2g_noalloc": (C.c_int, [C.POINTER(aep_grid_desc), C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
     "aep_last_error": (C.c_char_p, [_solver_p]),
+    "aep_sort_pairs_temp_bytes": (C.c_int64, [C.c_int64, C.c_int32]),
+    "aep_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p,
+                                 C.c_int64, C.c_void_p]),
     "aep_mlp_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
     "aep_mlp_destroy": (C.c_int, [C.c_void_p]),
     "aep_mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64]),
@@ -170,7 +175,7 @@ SIGNATURES = {
 
 AEP_MLP_NUM_PARAMS = 9928
 
-PHASES = ["sort", "p2g", "normalize", "force", "grid", "g2p"]
+PHASES = ["sort", "p2g", "normalize", "cloth_force", "force", "grid", "g2p", "mlp", "cloth_g2p"]
 
 _lib = None
 
@@ -222,6 +227,7 @@ _DEFAULTS = {
     "cloth_volume_weighting": 0,
     "full_sort": 0,
     "reorder_interval": 4,
+    "fp64_apex": 0,
 }
 
 

@@ -91,6 +91,7 @@ struct aep_solver {
     bool have_particles = false, keys_valid = false, dirty_grid = false;
     int last_stage = 0;
     double m_max = 1.0;
+    double mesh_m_max = 0.0;  // heaviest mesh vertex or element (aep_set_mesh)
     int64_t steps = 0;
     int grid_blocks = 1024;
     cudaStream_t own_stream = nullptr;
@@ -182,6 +183,7 @@ void fill_kparams(aep_solver* s) {
     k.particle_damp = (float)p.particle_damp;
     k.mesh_damp = (float)p.mesh_damp;
     k.track_fp = p.track_plastic_F;
+    k.fp64_apex = p.fp64_apex;
 }
 
 MeshArrays mesh_arrays(aep_solver* s) {
@@ -218,6 +220,7 @@ void free_mesh(aep_solver* s) {
     s->vforce = nullptr;
     s->slot_of = s->curidx_of = nullptr;
     s->nv = s->nf = 0;
+    s->mesh_m_max = 0.0;
     cudaFree(s->fixed);
     s->fixed = nullptr;
     s->nfixed = 0;
@@ -480,7 +483,7 @@ aep_status run_p2g(aep_solver* s) {
     mark(s, AEP_PHASE_NORMALIZE);
     launch_normalize(s->kp, s->G, s->dstats, s->grid_blocks, s->stream);
     CKLAUNCH();
-    mark(s, AEP_PHASE_FORCE);
+    mark(s, AEP_PHASE_CLOTH_FORCE);
     return AEP_OK;
 }
 
@@ -599,10 +602,10 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     if (!s) return AEP_INVALID_ARG;
     if (n <= 0 || n > (int64_t)INT32_MAX / 2 || !x || !Fe || !m)
         return fail(s, AEP_INVALID_ARG, "aep_set_particles: need n > 0 and non-null x, Fe, m");
-    // Re-uploading the same particle set keeps the device's current (sorted) order:
-    // item q goes to the slot its id occupies now, so the next ordering sees nearly
-    // sorted keys and the permuted particle reads stay coalesced.
-    const bool keep_order = s->have_particles && s->n == n && s->np == n && s->nf == 0;
+    // Re-uploading the same particle set keeps the device's current (sorted) order
+    // and an attached mesh: item q goes to the slot its id occupies now, so the next
+    // ordering sees nearly sorted keys and the permuted particle reads stay coalesced.
+    const bool keep_order = s->have_particles && s->np == n && s->n == s->np + s->nv + s->nf;
     if (!keep_order) {
         CK(cudaStreamSynchronize(s->stream));
         free_mesh(s);  // a mesh must be (re)attached after the particles
@@ -615,11 +618,13 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     }
     const int32_t* map = nullptr;
     if (keep_order) {
-        launch_inverse_ids((int)n, s->P[s->cur].id, s->perm, s->stream);
+        launch_inverse_ids((int)s->n, s->P[s->cur].id, s->perm, s->stream);  // over every item: ids 0..n-1 first
         CKLAUNCH();
         map = s->perm;
+    } else {
+        s->n = n;
     }
-    s->n = s->np = n;
+    s->np = n;
     PArrays& P = s->P[s->cur];
     // Arrays in page-locked host or device memory are read by the conversion
     // kernel directly; pageable ones are staged first (doubles): x 0, v 3n, B 6n,
@@ -652,11 +657,12 @@ aep_status aep_set_particles(aep_solver* s, int64_t n, const double* x, const do
     std::memcpy(&mm, &chk[0], sizeof(mm));
     if (chk[1] || !(mm > 0.0)) {
         s->have_particles = false;  // the device arrays are partly overwritten
+        free_mesh(s);
         s->n = s->np = 0;
         return fail(s, AEP_INVALID_ARG, chk[1] ? "aep_set_particles: bad mass or unknown material tag"
                                                : "aep_set_particles: all masses are zero");
     }
-    s->m_max = mm;
+    s->m_max = std::max(mm, s->mesh_m_max);
     fill_kparams(s);
     s->have_particles = true;
     s->keys_valid = false;
@@ -684,15 +690,16 @@ aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv,
             int32_t v = faces[c * nf + e];
             if (v < 0 || v >= nv) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: face index out of range");
         }
-    double mm = s->have_particles ? s->m_max : 0.0;
+    double mm = s->have_particles ? s->m_max : 0.0, mesh_mm = 0.0;
     for (int64_t i = 0; i < nv; ++i) {
         if (!(mv[i] >= 0.0) || !std::isfinite(mv[i])) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: bad mass");
-        mm = std::max(mm, mv[i]);
+        mesh_mm = std::max(mesh_mm, mv[i]);
     }
     for (int64_t e = 0; e < nf; ++e) {
         if (!(me[e] >= 0.0) || !std::isfinite(me[e])) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: bad mass");
-        mm = std::max(mm, me[e]);
+        mesh_mm = std::max(mesh_mm, me[e]);
     }
+    mm = std::max(mm, mesh_mm);
     if (!(mm > 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_mesh: all masses are zero");
     // rest data per element: inverseR of the rest in-plane R (geometry.cpp:67-73, from the
     // Gram-Schmidt QR of the rest directions, LagrangianMesh.cpp:421-429) and the third
@@ -731,6 +738,7 @@ aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv,
     s->prev_sorted = false;
     s->cur = 0;
     s->m_max = mm;
+    s->mesh_m_max = mesh_mm;
     s->cloth[0] = mu;
     s->cloth[1] = lambda;
     s->cloth[2] = shear_stiffness;
@@ -820,6 +828,36 @@ aep_status aep_get_mesh(aep_solver* s, double* xv, double* vv, double* Bv, doubl
     return AEP_OK;
 }
 
+// Writes to LagrangianMesh's public members between steps (LagrangianMesh.h:37-61), the
+// counterpart of aep_get_mesh: any pointer may be NULL (kept).  Items go to the slots
+// they occupy now, so the device order survives.
+aep_status aep_set_mesh_state(aep_solver* s, int64_t nv, int64_t nf, const double* xv, const double* vv,
+                              const double* Bv, const double* xe, const double* ve, const double* Be,
+                              const double* d) {
+    if (!s) return AEP_INVALID_ARG;
+    if (s->nf == 0) return fail(s, AEP_NOT_READY, "aep_set_mesh_state: no mesh");
+    if (nv != s->nv || nf != s->nf) return fail(s, AEP_INVALID_ARG, "aep_set_mesh_state: sizes differ from the mesh's");
+    PArrays& P = s->P[s->cur];
+    const int64_t vb = s->np, eb = s->np + s->nv;
+    const size_t V = (size_t)s->nv, F = (size_t)s->nf;
+    launch_inverse_ids((int)s->n, P.id, s->perm, s->stream);  // perm[id] = slot
+    CKLAUNCH();
+    const int32_t* mv = s->perm + vb;
+    const int32_t* me = s->perm + eb;
+    aep_status st;
+    // staging offsets (doubles) as in aep_get_mesh, so that pageable sources do not overlap
+    if (xv && (st = upload(s, xv, 3, 0, P.x, nv, 0, mv, 0))) return st;
+    if (vv && (st = upload(s, vv, 3, 0, P.v, nv, 0, mv, 3 * V))) return st;
+    if (Bv && (st = upload(s, Bv, 9, 1, P.B, nv, 0, mv, 6 * V))) return st;
+    if (xe && (st = upload(s, xe, 3, 0, P.x, nf, 0, me, 15 * V))) return st;
+    if (ve && (st = upload(s, ve, 3, 0, P.v, nf, 0, me, 15 * V + 3 * F))) return st;
+    if (Be && (st = upload(s, Be, 9, 1, P.B, nf, 0, me, 15 * V + 6 * F))) return st;
+    if (d && (st = upload(s, d, 9, 4, P.F, nf, 0, me, 15 * V + 15 * F))) return st;
+    if (xv || xe) s->keys_valid = false;  // positions changed: fresh keys at the next step
+    CK(cudaStreamSynchronize(s->stream));
+    return AEP_OK;
+}
+
 aep_status aep_set_levelset(aep_solver* s, const aep_sdf* shapes, int32_t n) {
     if (!s) return AEP_INVALID_ARG;
     if (n < 0 || n > kMaxShapes || (n > 0 && !shapes))
@@ -891,6 +929,9 @@ aep_status step_impl(aep_solver* s, double dt_force, double dt, int32_t stage, b
     const float dtf = (float)dt_force;
     const PArrays& P = s->P[s->cur];
     const MeshArrays M = mesh_arrays(s);
+    launch_cloth_force(s->kp, P, M, dtf, s->stream);
+    CKLAUNCH();
+    if (timed) mark(s, AEP_PHASE_FORCE);
     launch_force(s->kp, P, s->step_keys, s->step_perm, (int)s->n, s->G, dtf, s->dstats, M, s->stream, s->inv);
     CKLAUNCH();
     if (timed) mark(s, AEP_PHASE_GRID);
@@ -933,8 +974,18 @@ aep_status step_impl(aep_solver* s, double dt_force, double dt, int32_t stage, b
             s->queue.cap = (int)cap;
         }
     }
-    launch_g2p(s->kp, P, s->P[nx], s->step_perm, (int)s->n, s->G, (float)dt, s->keys, s->dstats, M, s->stream, H,
-               s->mlp ? &mp : nullptr, (float)s->learned_tol, (float)s->learned_abs, s->step_keys, s->queue);
+    launch_g2p(s->kp, P, s->P[nx], s->step_perm, (int)s->n, s->G, (float)dt, s->keys, s->dstats, s->stream, H,
+               s->mlp != nullptr, s->step_keys, s->queue);
+    CKLAUNCH();
+    if (timed) mark(s, AEP_PHASE_MLP);
+    if (s->mlp) {
+        launch_mlp_finish(s->kp, P, s->P[nx], s->queue, s->dstats, mp, (float)s->learned_tol, (float)s->learned_abs,
+                          s->stream);
+        CKLAUNCH();
+    }
+    if (timed) mark(s, AEP_PHASE_CLOTH_G2P);
+    launch_cloth_g2p(s->kp, P, s->P[nx], s->G, M, (float)dt, s->keys, s->dstats, H, s->mlp ? &mp : nullptr,
+                     (float)s->learned_tol, (float)s->learned_abs, s->stream);
     CKLAUNCH();
     if (timed) {
         mark(s, AEP_NUM_PHASES);
@@ -1123,7 +1174,7 @@ const char* ckpt_invalid(const CkptHeader& h, const char* body, int nblocks) {
     if (p.mass_bits <= 0 || p.mass_bits > 50 || p.momentum_bits <= 0 || p.momentum_bits > 50)
         return "fixed-point bits out of range";
     if (p.reorder_interval < 0 || (p.friction_bug | 1) != 1 || (p.track_plastic_F | 1) != 1 ||
-        (p.full_sort | 1) != 1 || (p.cloth_volume_weighting | 1) != 1)
+        (p.full_sort | 1) != 1 || (p.cloth_volume_weighting | 1) != 1 || (p.fp64_apex | 1) != 1)
         return "bad parameter flags";
     if (h.steps < 0 || h.since_order < 0 || (h.prev_sorted | 1) != 1) return "bad step counters";
     for (int k = 0; k < h.nshapes; ++k)
@@ -1278,6 +1329,7 @@ aep_status aep_checkpoint_load(aep_solver* s, const void* buf, int64_t bytes) {
     if (h.nf > 0) {
         s->nv = h.nv;
         s->nf = h.nf;
+        s->mesh_m_max = h.m_max;  // not stored separately: the combined bound stands in
         for (int k = 0; k < 5; ++k) s->cloth[k] = h.cloth[k];
         CK(cudaMalloc(&s->faces, sizeof(int32_t) * 3 * h.nf));
         CK(cudaMalloc(&s->rest, sizeof(float) * 6 * h.nf));
@@ -1393,6 +1445,7 @@ aep_status aep_get_stats(aep_solver* s, aep_stats* out) {
     out->sort_movers = (int64_t)h.movers;
     out->learned_exact = (int64_t)h.learned_exact;
     out->orderings = s->orderings;
+    out->fp64_apex = (int64_t)h.fp64_apex;
     double im = std::ldexp(s->m_max, -s->prm.mass_bits), ip = std::ldexp(s->m_max, -s->prm.momentum_bits);
     out->total_mass = (double)(long long)h.mass * im;
     for (int a = 0; a < 3; ++a) out->total_momentum[a] = (double)(long long)h.mom[a] * ip;
@@ -1471,6 +1524,23 @@ aep_status aep_get_phase_times(aep_solver* s, double* ms, int64_t* steps) {
     for (int p = 0; p < AEP_NUM_PHASES; ++p) ms[p] = s->phase_ms[p];
     if (steps) *steps = s->timed_steps;
     return AEP_OK;
+}
+
+int64_t aep_sort_pairs_temp_bytes(int64_t n, int32_t key_bits) {
+    if (n < 0 || n > (int64_t)INT32_MAX / 2 || key_bits < 1 || key_bits > 32) return -1;
+    return (int64_t)sort_temp_bytes((int)n, key_bits);
+}
+
+aep_status aep_sort_pairs(const uint32_t* keys_in, uint32_t* keys_out, const int32_t* vals_in, int32_t* vals_out,
+                          int64_t n, int32_t key_bits, void* temp, int64_t temp_bytes, void* cuda_stream) {
+    if (n < 0 || n > (int64_t)INT32_MAX / 2 || key_bits < 1 || key_bits > 32) return AEP_INVALID_ARG;
+    if (n == 0) return AEP_OK;
+    if (!keys_in || !keys_out || !vals_in || !vals_out || !temp ||
+        temp_bytes < (int64_t)sort_temp_bytes((int)n, key_bits))
+        return AEP_INVALID_ARG;
+    const cudaError_t e = sort_pairs(temp, (size_t)temp_bytes, keys_in, keys_out, vals_in, vals_out, (int)n, key_bits,
+                                     static_cast<cudaStream_t>(cuda_stream));
+    return e == cudaSuccess ? AEP_OK : AEP_CUDA_ERROR;
 }
 
 const char* aep_last_error(aep_solver* s) {

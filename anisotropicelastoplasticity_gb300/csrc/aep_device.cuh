@@ -46,6 +46,7 @@ struct KParams {
     float particle_damp;
     float mesh_damp;  // APIC damping of cloth vertices and elements, reference 1 (HS:926,932)
     int track_fp;
+    int fp64_apex;        // redo sand return mappings near the Drucker-Prager apex in FP64
     int nshapes;
     DevShape shapes[kMaxShapes];
     float cell_volume;
@@ -131,6 +132,7 @@ struct DevStats {
     unsigned long long learned_rejected;  // learned outputs replaced by the exact mapping
     unsigned long long learned_exact;  // constant projections (sand apex, cloth tension) taken exactly
     long long movers;              // particles that changed key (incremental ordering), -1: full sort
+    unsigned long long fp64_apex;  // sand return mappings near the apex redone in FP64 (fp64_apex option)
     unsigned int force_fp64;       // entries of the force pass's FP64 list (k_force_fp64)
     unsigned int mlp_rows;         // rows queued for the learned return map (k_mlp_finish)
     // length of the active node-block list (GArrays::nactive points here: zeroed with
@@ -432,6 +434,108 @@ __device__ __forceinline__ bool svd3(const T A[9], T U[9], T s[3], T V[9], int m
         for (int r = 0; r < 3; ++r) U[3 * r + b] = W[3 * r + b] * inv;
     }
     return ok;
+}
+
+__device__ __forceinline__ float log1p_t(float x) { return log1pf(x); }
+__device__ __forceinline__ double log1p_t(double x) { return log1p(x); }
+__device__ __forceinline__ float expm1_t(float x) { return expm1f(x); }
+__device__ __forceinline__ double expm1_t(double x) { return expm1(x); }
+
+// One Jacobi rotation of a symmetric 3x3 matrix in the (p, q) plane, chosen to
+// zero a_pq (the t = tan(phi) form: a_pp -= t a_pq, a_qq += t a_pq), with r the
+// third index; V accumulates the rotations (columns p, q).  Skipped when a_pq
+// is already negligible against the diagonal pair.
+template <typename T>
+__device__ __forceinline__ bool jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& arq, T V[9], int p, int q, T tol) {
+    if (!(abs_t(apq) > tol * (abs_t(app) + abs_t(aqq)))) return false;
+    const T zeta = rot_div(aqq - app, T(2) * apq);
+    const T az = abs_t(zeta);
+    const T t = az > T(1e15) ? rot_div(T(0.5), zeta)
+                             : rot_div(zeta >= T(0) ? T(1) : T(-1), az + sqrt_t(T(1) + zeta * zeta));
+    const T c = rsqrt_t(T(1) + t * t), s = c * t;
+    app -= t * apq;
+    aqq += t * apq;
+    apq = T(0);
+    const T rp = arp, rq = arq;
+    arp = c * rp - s * rq;
+    arq = s * rp + c * rq;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const T vp = V[3 * r + p], vq = V[3 * r + q];
+        V[3 * r + p] = c * vp - s * vq;
+        V[3 * r + q] = s * vp + c * vq;
+    }
+    return true;
+}
+
+// Eigen-decomposition S = V diag(lam) V^T of the symmetric matrix
+// S = [[a00, a01, a02], [a01, a11, a12], [a02, a12, a22]] by cyclic Jacobi sweeps.
+template <typename T>
+__device__ __forceinline__ void sym_eig3(T a00, T a11, T a22, T a01, T a02, T a12, T lam[3], T V[9], int max_sweeps,
+                                         T tol) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) V[k] = (k % 4 == 0) ? T(1) : T(0);
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        bool r = jacobi_rot<T>(a00, a11, a01, a02, a12, V, 0, 1, tol);
+        r |= jacobi_rot<T>(a00, a22, a02, a01, a12, V, 0, 2, tol);
+        r |= jacobi_rot<T>(a11, a22, a12, a01, a02, V, 1, 2, tol);
+        if (!r) break;
+    }
+    lam[0] = a00;
+    lam[1] = a11;
+    lam[2] = a22;
+}
+
+// a + b = s + e exactly (Knuth's TwoSum; no multiplication, so nothing is fused)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// a0 b0 + a1 b1 + a2 b2 - c with the products split exactly (p + e = a b by fma)
+// and the sum carried in twice the working precision, rounded once at the end:
+// resolves F^T F - I to ~2^-48 where plain FP32 keeps ~2^-24 of the terms ~1.
+__device__ __forceinline__ float dot3_minus_exact(float a0, float b0, float a1, float b1, float a2, float b2, float c) {
+    const float p0 = __fmul_rn(a0, b0), p1 = __fmul_rn(a1, b1), p2 = __fmul_rn(a2, b2);
+    const float e0 = fmaf(a0, b0, -p0), e1 = fmaf(a1, b1, -p1), e2 = fmaf(a2, b2, -p2);
+    float s, t1, t2, t3;
+    two_sum(p0, p1, s, t1);
+    two_sum(s, p2, s, t2);
+    two_sum(s, -c, s, t3);
+    return __fadd_rn(s, __fadd_rn(__fadd_rn(__fadd_rn(e0, e1), e2), __fadd_rn(__fadd_rn(t1, t2), t3)));
+}
+
+// C - I = F_tr^T F_tr - I for F_tr = F + D (row-major 3x3), as its six entries
+// (e00, e11, e22, e01, e02, e12): (F^T F - I) + F^T D + D^T F + D^T D.  The first
+// term is where FP32 loses the state: F is near a rotation and its Gram matrix
+// differs from I by a few units of 2^-24, so it is summed without loss (float)
+// or in FP64 (double); the D terms are small and need no care.
+__device__ __forceinline__ void trial_stretch(const float F[9], const float D[9], float e[6]) {
+    const int I[6] = {0, 1, 2, 0, 0, 1}, J[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const int i = I[k], j = J[k];
+        const float g = dot3_minus_exact(F[i], F[j], F[3 + i], F[3 + j], F[6 + i], F[6 + j], i == j ? 1.0f : 0.0f);
+        // F^T D + D^T F + D^T D = F^T D + D^T (F + D)
+        float x = F[i] * D[j] + F[3 + i] * D[3 + j] + F[6 + i] * D[6 + j];
+        x += D[i] * (F[j] + D[j]) + D[3 + i] * (F[3 + j] + D[3 + j]) + D[6 + i] * (F[6 + j] + D[6 + j]);
+        e[k] = g + x;
+    }
+}
+__device__ __forceinline__ void trial_stretch(const float F[9], const float D[9], double e[6]) {
+    const int I[6] = {0, 1, 2, 0, 0, 1}, J[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const int i = I[k], j = J[k];
+        double x = -(i == j ? 1.0 : 0.0);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const double fi = F[3 * r + i] + (double)D[3 * r + i], fj = F[3 * r + j] + (double)D[3 * r + j];
+            x = fma(fi, fj, x);
+        }
+        e[k] = x;
+    }
 }
 
 // Complete U where a singular value vanished (FP64 path only).

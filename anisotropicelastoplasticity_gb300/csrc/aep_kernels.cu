@@ -949,6 +949,96 @@ __device__ __forceinline__ void return_map(const KParams& P, int mat, T s[3], T&
     }
 }
 
+// Return mapping (HybridSolver.cpp:612-677) in the stretch form, for a trial state
+// F_tr = F + D (D = dt grad v^bf F) whose stretch C - I = F_tr^T F_tr - I = V diag(lam) V^T
+// is below 1/2: ln s = log1p(lam) / 2, the projection in log space, and
+//   F_E = U diag(s_new) V^T = F_tr V diag(s_new / s) V^T = F + [D + F_tr V diag(rho) V^T],
+//   rho = expm1(ln s_new - ln s)        (U = F_tr V diag(1 / s)),
+// i.e. the state plus a small correction, rounded once.  Computing s and then ln s,
+// or U diag(s_new) V^T, loses the few units of 2^-24 that carry a small strain near
+// s = 1 (the sand apex, s_new = 1, turns them into stress); this form keeps them.
+// J_P (snow) is scaled by prod(s / s_new); sig = expm1(ln s - ln s_new) gives
+// F_P <- F_P + V diag(sig) V^T F_P (HS:676).  T = double runs the whole mapping in
+// FP64 from the same FP32 inputs.  Returns 0 elastic, 1 sand apex, 2 projected
+// (snow clamp, sand cone), -1 when the stretch is too large for this form (the
+// caller takes the SVD form); ln_tr / ln_new return the log singular values.
+template <typename T>
+__device__ __forceinline__ int stretch_return_map(const KParams& P, int mat, const float F[9], const float D[9],
+                                                  float& q, float Fe[9], float Vo[9], float sig[3], float ln_tr[3],
+                                                  float ln_new[3]) {
+    T e[6];
+    trial_stretch(F, D, e);
+    const T n2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + T(2) * (e[3] * e[3] + e[4] * e[4] + e[5] * e[5]);
+    if (!(n2 < T(0.25))) return -1;
+    T lam[3], V[9];
+    sym_eig3<T>(e[0], e[1], e[2], e[3], e[4], e[5], lam, V, 10, sizeof(T) == 4 ? T(0x1p-25) : T(0x1p-54));
+    T ln[3], lnn[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) lnn[a] = ln[a] = T(0.5) * log1p_t(lam[a]);
+    int kind = 0;
+    T qq = q;
+    if (mat == kSnow) {
+        const T lo = log_t(T(P.snow_lo)), hi = log_t(T(P.snow_hi));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const T c = fmin(fmax(ln[a], lo), hi);
+            if (c != ln[a]) kind = 2;
+            lnn[a] = c;
+        }
+    } else {
+        kind = dp_project<T>(lnn, qq, T(P.sand_h0), T(P.sand_h1), T(P.sand_h2), T(P.sand_h3), T(P.sand_k));
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        ln_tr[a] = (float)ln[a];
+        ln_new[a] = (float)lnn[a];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Vo[k] = (float)V[k];
+    if (kind == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fe[k] = F[k] + D[k];
+        sig[0] = sig[1] = sig[2] = 0.0f;
+        return 0;
+    }
+    T rho[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        rho[a] = expm1_t(lnn[a] - ln[a]);
+        sig[a] = (float)expm1_t(ln[a] - lnn[a]);
+    }
+    // M = V diag(rho) V^T, then F_E = F + (D + (F + D) M)
+    T M[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            M[3 * a + b] = V[3 * a] * rho[0] * V[3 * b] + V[3 * a + 1] * rho[1] * V[3 * b + 1] +
+                           V[3 * a + 2] * rho[2] * V[3 * b + 2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const T t0 = T(F[3 * a]) + T(D[3 * a]), t1 = T(F[3 * a + 1]) + T(D[3 * a + 1]),
+                t2 = T(F[3 * a + 2]) + T(D[3 * a + 2]);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const T corr = T(D[3 * a + b]) + t0 * M[b] + t1 * M[3 + b] + t2 * M[6 + b];
+            Fe[3 * a + b] = (float)(T(F[3 * a + b]) + corr);
+        }
+    }
+    if (mat == kSnow) q = (float)(T(q) * exp_t((ln[0] - lnn[0]) + (ln[1] - lnn[1]) + (ln[2] - lnn[2])));
+    else q = (float)qq;
+    return kind;
+}
+
+// A sand trial state within reach of the apex of the Drucker-Prager cone: projected
+// onto the apex, or |tr ln s| within 1e-3 of |ln s| of the switch between apex and
+// cone (HybridSolver.cpp:652-663).  With the FP64 option these mappings run again in FP64.
+__device__ __forceinline__ bool near_apex(int kind, const float ln[3]) {
+    if (kind == 1) return true;
+    const float tr = ln[0] + ln[1] + ln[2];
+    return fabsf(tr) <= 1e-3f * sqrtf(ln[0] * ln[0] + ln[1] * ln[1] + ln[2] * ln[2]);
+}
+
 // Gather of v (G2P velocity + APIC) and v^bf (advection + velocity gradient) over
 // the 4x4x4 stencil, contracted one axis at a time because the weights are tensor
 // products: x first (A), then z (B), then y.
@@ -1028,9 +1118,9 @@ __device__ __forceinline__ void apic_damp(const float C[9], float damp, float Bn
 // so are sand states within kHarvestMinLn of s = 1, whose ln s carry the FP32
 // rounding of s (2^-24 absolute) as more than 1e-3 of their size.
 constexpr float kHarvestMinLn = 1e-4f;
-__device__ __forceinline__ void harvest_record(const KParams& P, const Harvest& H, int mat, const float s_tr[3],
-                                               const float s_new[3], float q_old) {
-    float ln[3] = {logf(s_tr[0]), logf(s_tr[1]), logf(s_tr[2])}, srt[3], t[3];
+__device__ __forceinline__ void harvest_record(const KParams& P, const Harvest& H, int mat, const float ln[3],
+                                               const float ln_new[3], float q_old) {
+    float srt[3], t[3];
     int pm[3];
     sort3_desc(ln, srt, pm);
     if (mat == kSand) {
@@ -1040,7 +1130,7 @@ __device__ __forceinline__ void harvest_record(const KParams& P, const Harvest& 
         if (dp_project<float>(t, qq, P.sand_h0, P.sand_h1, P.sand_h2, P.sand_h3, P.sand_k) != 2) return;
     } else {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) t[k] = logf(s_new[pm[k]]);
+        for (int k = 0; k < 3; ++k) t[k] = ln_new[pm[k]];
     }
     const unsigned long long slot = atomicAdd(H.count, 1ull);
     if ((long long)slot >= H.capacity) return;
@@ -1154,14 +1244,17 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         cp_async_wait_all();
         return;
     }
-    // F update (HS:560-576)
+    // F update (HS:560-576): F_tr = F + D, D = dt grad v^bf F
     if (!kDefer) cp_async_wait_all();
-    float F[9], GF[9], Ftr[9];
+    float F[9], GF[9], Ftr[9], D[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) F[k] = kDefer ? cur.F[k][pj] : sF[k][threadIdx.x];
     mat_mul(Gb, F, GF);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Ftr[k] = F[k] + dt * GF[k];
+    for (int k = 0; k < 9; ++k) {
+        D[k] = dt * GF[k];
+        Ftr[k] = F[k] + D[k];
+    }
     // return mapping (HS:612-677)
     float q = kDefer ? cur.plastic[pj] : sq[threadIdx.x];
     float U[9], s[3], V[9];
@@ -1169,13 +1262,32 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
     float sprod = 1.0f;  // prod(s_trial / s_new) for J_P
     bool used_fp64 = false, deferred = false;
     double Ud[9], sd[3], Vd[9];
-    bool ok = svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
-    if (ok) {
+    // the stretch form (plain step): the state plus a correction; -1 for a trial
+    // stretch beyond its range, which takes the SVD form below
+    int skind = -1;
+    float sig[3];
+    if (!kDefer) {
+        float lt[3], lnw[3];
+        const float q_old = q;
+        skind = stretch_return_map<float>(P, mat, F, D, q, Fe, V, sig, lt, lnw);
+        if (skind >= 0 && P.fp64_apex && mat == kSand && near_apex(skind, lt)) {
+            q = q_old;  // the same mapping again, in FP64
+            skind = stretch_return_map<double>(P, mat, F, D, q, Fe, V, sig, lt, lnw);
+            cg::coalesced_group g = cg::coalesced_threads();
+            if (g.thread_rank() == 0) atomicAdd(&st->fp64_apex, (unsigned long long)g.size());
+        }
+        if (skind > 0 && H.buf && (j % H.stride) == 0) harvest_record(P, H, mat, lt, lnw, q_old);
+    }
+    bool ok = skind >= 0 || svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
+    if (skind >= 0) {
+    } else if (ok) {
         sn[0] = s[0]; sn[1] = s[1]; sn[2] = s[2];
         const float q_old = q;
         return_map<float>(P, mat, sn, q);
-        if (H.buf && (j % H.stride) == 0 && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2]))
-            harvest_record(P, H, mat, s, sn, q_old);  // plastic states only
+        if (H.buf && (j % H.stride) == 0 && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2])) {
+            const float lt[3] = {logf(s[0]), logf(s[1]), logf(s[2])}, lnw[3] = {logf(sn[0]), logf(sn[1]), logf(sn[2])};
+            harvest_record(P, H, mat, lt, lnw, q_old);  // plastic states only
+        }
         if (kDefer && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2])) {
             if (mat == kSand && sn[0] == 1.0f && sn[1] == 1.0f && sn[2] == 1.0f) {
                 cg::coalesced_group g = cg::coalesced_threads();  // the apex: exact, counted
@@ -1239,6 +1351,24 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         atomicAdd(&st->fallbacks, 1ull);
     }
     if (deferred) {
+    } else if (P.track_fp && skind >= 0) {
+        // F_P = V S_new^-1 U^T F_tr F_P = V diag(s / s_new) V^T F_P = F_P + V diag(sig) V^T F_P (HS:676)
+        float Fp[9], Fpn[9], W[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                W[3 * a + b] = V[3 * a] * sig[0] * V[3 * b] + V[3 * a + 1] * sig[1] * V[3 * b + 1] +
+                               V[3 * a + 2] * sig[2] * V[3 * b + 2];
+        mat_mul(W, Fp, Fpn);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            Fpn[k] += Fp[k];
+            nxt.Fp[k][j] = Fpn[k];
+        }
+        if (mat == kSnow) q = mat_det(Fpn);
     } else if (P.track_fp) {
         // F_P = V S^-1 U^T F_tr F_P (HS:676)
         float Fp[9], Ft[9];
@@ -1263,8 +1393,8 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
 #pragma unroll
         for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = Fpn[k];
         if (mat == kSnow) q = mat_det(Fpn);
-    } else if (mat == kSnow) {
-        q *= sprod;  // J_P = det F_P = det(F_tr) det(F_P) / det(S_new)
+    } else if (mat == kSnow && skind < 0) {
+        q *= sprod;  // J_P = det F_P = det(F_tr) det(F_P) / det(S_new); the stretch form scaled it already
     }
     // store in the new order
 #pragma unroll
@@ -1884,14 +2014,16 @@ void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, cons
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s) {
     launch_pdl(k_normalize, grid_blocks, 256, 0, s, P, G, st);
 }
-void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
-                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s,
-                  int32_t* fp64_list) {
-    long warps = (n + 31) / 32;
+void launch_cloth_force(const KParams& P, const PArrays& cur, const MeshArrays& M, float dt_force, cudaStream_t s) {
     // the cloth forces launch after the normalisation has completed: early, their
     // small blocks filled the SMs beside the one-wave normalisation and slowed the
     // 8,388,608-item sand + cloth step by 2% (and the cloth drape's by 3%)
     if (M.nf > 0) k_cloth_force<<<blocks_for(M.nf, 128), 128, 0, s>>>(P, cur, M, dt_force);
+}
+void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
+                  const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s,
+                  int32_t* fp64_list) {
+    long warps = (n + 31) / 32;
     if (n > 0) {
         launch_pdl(k_force, blocks_for(warps, kFrcThreads / 32), kFrcThreads, 0, s, P, cur, keys, perm, n, G, dt_force,
                    st, M, fp64_list, n);
@@ -1906,44 +2038,47 @@ void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s) {
     k_grid_clear<<<grid_blocks, 256, 0, s>>>(G);
 }
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
-                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s,
-                const Harvest& H, const MlpParams* mlp, float tol_rel, float tol_abs, const uint32_t* keys_sorted,
-                const MlpQueue& Qu) {
-    if (n > 0) {
-        if (mlp) {
-            launch_pdl(k_g2p<true>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
-                       keys_sorted, Qu);
-            constexpr int smem = kMlpSmemBytes + (kFinThreads / 32) * kMlpWarpBytes;
-            // resident finisher blocks of the device, looked up once (the attribute is
-            // set with it, before the first launch)
-            static const int resident = [] {
-                cudaFuncSetAttribute(k_mlp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-                int dev = 0, sms = 0, per_sm = 0;
-                cudaGetDevice(&dev);
-                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_finish, kFinThreads, smem);
-                return std::max(1, sms * std::max(per_sm, 1));
-            }();
-            const int blocks = std::min(blocks_for(Qu.cap, kFinThreads), resident);
-            launch_pdl(k_mlp_finish, blocks, kFinThreads, smem, s, P, cur, nxt, Qu, st, *mlp, tol_rel, tol_abs);
-        } else {
-            launch_pdl(k_g2p<false>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
-                       keys_sorted, Qu);
-        }
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, cudaStream_t s, const Harvest& H,
+                bool learned, const uint32_t* keys_sorted, const MlpQueue& Qu) {
+    if (n <= 0) return;
+    if (learned)
+        launch_pdl(k_g2p<true>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
+                   keys_sorted, Qu);
+    else
+        launch_pdl(k_g2p<false>, blocks_for(n, 128), 128, 0, s, P, cur, nxt, perm, n, G, dt, keys_next, st, H,
+                   keys_sorted, Qu);
+}
+void launch_mlp_finish(const KParams& P, const PArrays& cur, const PArrays& nxt, const MlpQueue& Qu, DevStats* st,
+                       const MlpParams& mlp, float tol_rel, float tol_abs, cudaStream_t s) {
+    constexpr int smem = kMlpSmemBytes + (kFinThreads / 32) * kMlpWarpBytes;
+    // resident finisher blocks of the device, looked up once (the attribute is set
+    // with it, before the first launch)
+    static const int resident = [] {
+        cudaFuncSetAttribute(k_mlp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_finish, kFinThreads, smem);
+        return std::max(1, sms * std::max(per_sm, 1));
+    }();
+    const int blocks = std::min(blocks_for(Qu.cap, kFinThreads), resident);
+    launch_pdl(k_mlp_finish, blocks, kFinThreads, smem, s, P, cur, nxt, Qu, st, mlp, tol_rel, tol_abs);
+}
+void launch_cloth_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const GArrays& G, const MeshArrays& M,
+                      float dt, uint32_t* keys_next, DevStats* st, const Harvest& H, const MlpParams* mlp,
+                      float tol_rel, float tol_abs, cudaStream_t s) {
+    if (M.nf <= 0) return;
+    constexpr int kClothMlpSmem = kMlpSmemBytes + 4 * kMlpWarpBytes;
+    const int smem = mlp ? kClothMlpSmem : 0;
+    if (mlp) {
+        static const bool attr_set = [] {  // once per process, before the first learned launch
+            cudaFuncSetAttribute(k_cloth_g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, kClothMlpSmem);
+            return true;
+        }();
+        (void)attr_set;
     }
-    if (M.nf > 0) {
-        constexpr int kClothMlpSmem = kMlpSmemBytes + 4 * kMlpWarpBytes;
-        const int smem = mlp ? kClothMlpSmem : 0;
-        if (mlp) {
-            static const bool attr_set = [] {  // once per process, before the first learned launch
-                cudaFuncSetAttribute(k_cloth_g2p, cudaFuncAttributeMaxDynamicSharedMemorySize, kClothMlpSmem);
-                return true;
-            }();
-            (void)attr_set;
-        }
-        launch_pdl(k_cloth_g2p, blocks_for(M.nf, 128), 128, smem, s, P, cur, nxt, G, M, dt, keys_next, st, H,
-                   mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, tol_rel, tol_abs);
-    }
+    launch_pdl(k_cloth_g2p, blocks_for(M.nf, 128), 128, smem, s, P, cur, nxt, G, M, dt, keys_next, st, H,
+               mlp ? *mlp : MlpParams{}, mlp ? 1 : 0, tol_rel, tol_abs);
 }
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s) {

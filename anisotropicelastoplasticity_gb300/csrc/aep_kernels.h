@@ -11,16 +11,23 @@ void launch_keys(const KParams& P, const PArrays& cur, int n, uint32_t* keys, De
 void launch_p2g(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
                 const GArrays& G, int32_t* slot_of, int32_t* curidx_of, cudaStream_t s);
 void launch_normalize(const KParams& P, const GArrays& G, DevStats* st, int grid_blocks, cudaStream_t s);
+void launch_cloth_force(const KParams& P, const PArrays& cur, const MeshArrays& M, float dt_force, cudaStream_t s);
 void launch_force(const KParams& P, const PArrays& cur, const uint32_t* keys, const int32_t* perm, int n,
                   const GArrays& G, float dt_force, DevStats* st, const MeshArrays& M, cudaStream_t s,
                   int32_t* fp64_list);
 void launch_grid(const KParams& P, const GArrays& G, float dt_force, int write_force, double* force_out,
                  int grid_blocks, cudaStream_t s);
 void launch_grid_clear(const GArrays& G, int grid_blocks, cudaStream_t s);
+// G2P of the particle system and the cloth vertices (learned: the plastic rows are
+// queued for the finisher), the learned map's finisher, the cloth elements' G2P
 void launch_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const int32_t* perm, int n,
-                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, const MeshArrays& M, cudaStream_t s,
-                const Harvest& H, const MlpParams* mlp, float tol_rel, float tol_abs, const uint32_t* keys_sorted,
-                const MlpQueue& queue);
+                const GArrays& G, float dt, uint32_t* keys_next, DevStats* st, cudaStream_t s, const Harvest& H,
+                bool learned, const uint32_t* keys_sorted, const MlpQueue& queue);
+void launch_mlp_finish(const KParams& P, const PArrays& cur, const PArrays& nxt, const MlpQueue& queue, DevStats* st,
+                       const MlpParams& mlp, float tol_rel, float tol_abs, cudaStream_t s);
+void launch_cloth_g2p(const KParams& P, const PArrays& cur, const PArrays& nxt, const GArrays& G, const MeshArrays& M,
+                      float dt, uint32_t* keys_next, DevStats* st, const Harvest& H, const MlpParams* mlp,
+                      float tol_rel, float tol_abs, cudaStream_t s);
 void launch_volumes(const KParams& P, const PArrays& cur, const int32_t* perm, int n, const GArrays& G,
                     cudaStream_t s);
 void launch_upload(int n, int mode, const double* src, float* const* dst, cudaStream_t s,
@@ -79,7 +86,7 @@ cudaError_t order_graph_build(void** out, cudaStream_t capture_stream, const Ord
 cudaError_t order_graph_launch(void* graph, cudaStream_t s);
 void order_graph_destroy(void* graph);
 
-// radix sort of (key, index) pairs; implemented with CUB in aep_sort.cu
+// stable LSD radix sort of (key, value) pairs on the low key_bits bits (aep_sort.cu)
 size_t sort_temp_bytes(int n, int key_bits);
 cudaError_t sort_pairs(void* temp, size_t temp_bytes, const uint32_t* keys_in, uint32_t* keys_out,
                        const int32_t* vals_in, int32_t* vals_out, int n, int key_bits, cudaStream_t s);

@@ -1,6 +1,6 @@
 // aep_sort.cu -- per-step particle ordering by (cell key, particle slot).
 //
-// Full sort: a stable LSD radix sort (CUB) of the key bits in use.  Stability
+// Full sort: a stable LSD radix sort of the key bits in use (below).  Stability
 // keeps particles that stay in their cell in their previous relative order, so
 // the permutation is close to the identity from step to step and the permuted
 // reads of the particle arrays stay nearly coalesced.
@@ -27,22 +27,183 @@
 // captured in a CUDA graph whose switch node runs (stayers | movers + stayers |
 // full sort).  The ordering is a deterministic function of the keys, so steps
 // repeat bit for bit, and no host synchronisation is needed.
-#include <cub/device/device_radix_sort.cuh>
+#include <algorithm>
 
 #include "aep_kernels.h"
 
 namespace aep {
 
+// ===================================================================================
+// Stable LSD radix sort of (uint32 key, int32 value) pairs on the low key_bits bits.
+// The bits are cut into P = ceil(key_bits / 8) digits of R = ceil(key_bits / P) <= 8
+// bits.  Each pass is three kernels over tiles of kRsTile pairs:
+//   k_rs_hist     per tile, the count of every digit value -> hist[digit][tile]
+//   k_rs_scan     per digit (one block each): exclusive scan of its row over the
+//                 tiles in place, and the digit's total
+//   k_rs_scatter  per tile: the digits' bases (exclusive scan of the totals) plus
+//                 the row offsets give each digit's first output slot for the tile;
+//                 the tile is read in rounds of one pair per thread in input order,
+//                 and a pair's rank among the tile's equal digits comes from
+//                 __match_any_sync inside its warp, the counts of the warps before
+//                 it in the round and the running count of earlier rounds, so equal
+//                 digits keep their input order (the sort is stable).
+// Passes alternate between the output arrays and a scratch copy, arranged so that
+// the last pass writes the output.  Traffic per pass: keys and values read twice
+// and written once.
+constexpr int kRsThreads = 256;
+constexpr int kRsRounds = 16;
+constexpr int kRsTile = kRsThreads * kRsRounds;  // 4096 pairs per tile
+constexpr int kRsBins = 256;
+constexpr int kRsWarps = kRsThreads / 32;
+
+struct RsPlan {
+    int passes, radix, tiles;
+};
+
+RsPlan rs_plan(int n, int key_bits) {
+    RsPlan p;
+    key_bits = std::max(1, std::min(32, key_bits));
+    p.passes = (key_bits + 7) / 8;
+    p.radix = (key_bits + p.passes - 1) / p.passes;
+    p.tiles = std::max(1, (n + kRsTile - 1) / kRsTile);
+    return p;
+}
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t* __restrict__ keys, int n, int shift,
+                                                        uint32_t mask, int tiles, int32_t* __restrict__ hist) {
+    __shared__ int32_t cnt[kRsBins];
+    for (int i = threadIdx.x; i < kRsBins; i += kRsThreads) cnt[i] = 0;
+    __syncthreads();
+    const long base = (long)blockIdx.x * kRsTile;
+    for (int r = 0; r < kRsRounds; ++r) {
+        const long i = base + (long)r * kRsThreads + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & mask], 1);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d <= (int)mask; d += kRsThreads) hist[(long)d * tiles + blockIdx.x] = cnt[d];
+}
+
+// block-wide exclusive scan of one value per thread; returns the block total
+__device__ __forceinline__ int32_t rs_block_scan(int32_t v, int32_t& total, int32_t* warp_tot) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    int32_t off = 0;
+    total = 0;
+    for (int k = 0; k < kRsWarps; ++k) {
+        const int32_t t = warp_tot[k];
+        if (k < w) off += t;
+        total += t;
+    }
+    __syncthreads();
+    return off + x - v;
+}
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_scan(int32_t* __restrict__ hist, int tiles,
+                                                        int32_t* __restrict__ totals) {
+    __shared__ int32_t warp_tot[kRsWarps];
+    int32_t* row = hist + (long)blockIdx.x * tiles;
+    int32_t carry = 0;
+    for (int t0 = 0; t0 < tiles; t0 += kRsThreads) {  // block-uniform trip count
+        const int t = t0 + threadIdx.x;
+        const int32_t v = t < tiles ? row[t] : 0;
+        int32_t total;
+        const int32_t ex = rs_block_scan(v, total, warp_tot);
+        if (t < tiles) row[t] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __restrict__ keys_in,
+                                                           const int32_t* __restrict__ vals_in, int n, int shift,
+                                                           uint32_t mask, int tiles,
+                                                           const int32_t* __restrict__ hist,
+                                                           const int32_t* __restrict__ totals,
+                                                           uint32_t* __restrict__ keys_out,
+                                                           int32_t* __restrict__ vals_out) {
+    __shared__ int32_t start[kRsBins];              // first output slot of each digit for this tile
+    __shared__ int32_t wcnt[kRsWarps][kRsBins];     // this round's count per warp and digit
+    __shared__ int32_t warp_tot[kRsWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nd = (int)mask + 1;
+    {  // digit bases: exclusive scan of the totals (nd <= 256 = one per thread)
+        const int d = threadIdx.x;
+        int32_t total;
+        const int32_t ex = rs_block_scan(d < nd ? totals[d] : 0, total, warp_tot);
+        if (d < nd) start[d] = ex + hist[(long)d * tiles + blockIdx.x];
+    }
+    for (int i = threadIdx.x; i < kRsWarps * kRsBins; i += kRsThreads) (&wcnt[0][0])[i] = 0;
+    __syncthreads();
+    const long base = (long)blockIdx.x * kRsTile;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int r = 0; r < kRsRounds; ++r) {
+        const long i = base + (long)r * kRsThreads + threadIdx.x;
+        const bool live = i < n;
+        const uint32_t k = live ? keys_in[i] : 0u;
+        const int32_t v = live ? vals_in[i] : 0;
+        const int d = live ? (int)((k >> shift) & mask) : kRsBins;  // past the end: its own group
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank_w = __popc(peers & lt);
+        const bool leader = rank_w == 0;
+        if (leader && live) wcnt[w][d] = __popc(peers);
+        __syncthreads();
+        if (live) {
+            int32_t pos = start[d] + rank_w;
+            for (int ww = 0; ww < w; ++ww) pos += wcnt[ww][d];
+            keys_out[pos] = k;
+            vals_out[pos] = v;
+        }
+        __syncthreads();
+        if (leader && live) {
+            atomicAdd(&start[d], wcnt[w][d]);
+            wcnt[w][d] = 0;
+        }
+        __syncthreads();
+    }
+}
+
 size_t sort_temp_bytes(int n, int key_bits) {
-    size_t bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
-                                    (const int32_t*)nullptr, (int32_t*)nullptr, n, 0, key_bits);
-    return bytes;
+    const RsPlan p = rs_plan(n, key_bits);
+    const size_t hist = sizeof(int32_t) * ((size_t)kRsBins * p.tiles + kRsBins);
+    const size_t pairs = (sizeof(uint32_t) + sizeof(int32_t)) * (size_t)std::max(n, 1);
+    return ((hist + 255) & ~(size_t)255) + pairs;
 }
 
 cudaError_t sort_pairs(void* temp, size_t temp_bytes, const uint32_t* keys_in, uint32_t* keys_out,
                        const int32_t* vals_in, int32_t* vals_out, int n, int key_bits, cudaStream_t s) {
-    return cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys_in, keys_out, vals_in, vals_out, n, 0, key_bits, s);
+    if (n <= 0) return cudaSuccess;
+    if (temp_bytes < sort_temp_bytes(n, key_bits)) return cudaErrorInvalidValue;
+    const RsPlan p = rs_plan(n, key_bits);
+    int32_t* hist = static_cast<int32_t*>(temp);
+    int32_t* totals = hist + (size_t)kRsBins * p.tiles;
+    const size_t hist_bytes = (sizeof(int32_t) * ((size_t)kRsBins * p.tiles + kRsBins) + 255) & ~(size_t)255;
+    uint32_t* tk = reinterpret_cast<uint32_t*>(static_cast<char*>(temp) + hist_bytes);
+    int32_t* tv = reinterpret_cast<int32_t*>(tk + n);
+    const uint32_t mask = (1u << p.radix) - 1u;
+    const uint32_t* ik = keys_in;
+    const int32_t* iv = vals_in;
+    for (int pass = 0; pass < p.passes; ++pass) {
+        // the last pass writes the output: passes alternate back from it
+        const bool to_out = ((p.passes - 1 - pass) & 1) == 0;
+        uint32_t* ok = to_out ? keys_out : tk;
+        int32_t* ov = to_out ? vals_out : tv;
+        const int shift = pass * p.radix;
+        k_rs_hist<<<p.tiles, kRsThreads, 0, s>>>(ik, n, shift, mask, p.tiles, hist);
+        k_rs_scan<<<(int)mask + 1, kRsThreads, 0, s>>>(hist, p.tiles, totals);
+        k_rs_scatter<<<p.tiles, kRsThreads, 0, s>>>(ik, iv, n, shift, mask, p.tiles, hist, totals, ok, ov);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        ik = ok;
+        iv = ov;
+    }
+    return cudaSuccess;
 }
 
 namespace {
@@ -293,10 +454,8 @@ cudaError_t order_graph_build(void** out, cudaStream_t cs, const OrderBuffers& b
         OG_CK(cudaGetLastError());
         OG_CK(cudaStreamEndCapture(cs, &ended));
     }
-    size_t sort_bytes = b.sort_bytes;  // CUB takes it by reference
     OG_CK(cudaStreamBeginCaptureToGraph(cs, body[2], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    OG_CK(cub::DeviceRadixSort::SortPairs(b.sort_tmp, sort_bytes, b.keys, b.keys_sorted, b.iota, b.perm, n, 0,
-                                          b.key_bits, cs));
+    OG_CK(sort_pairs(b.sort_tmp, b.sort_bytes, b.keys, b.keys_sorted, b.iota, b.perm, n, b.key_bits, cs));
     OG_CK(cudaStreamEndCapture(cs, &ended));
     OrderGraph* og = new OrderGraph();
     og->graph = g;

@@ -355,6 +355,16 @@ class HybridSolver:
                     element_velocities=vec_from_ref(ve, nf), element_affine_momenta=rows_from_ref(Be, nf),
                     element_directions=dirs_from_ref(d, nf))
 
+    def set_mesh_state(self, state: dict):
+        """Write the mesh's per-step members (the keys of get_mesh; missing keys are
+        kept) into the device state, keeping the device order (aep_set_mesh_state)."""
+        nv, nf = len(self.mesh.vertex_positions), len(self.mesh.faces)
+        conv = {"vertex_positions": vec_to_ref, "vertex_velocities": vec_to_ref, "vertex_affine_momenta": rows_to_ref,
+                "element_positions": vec_to_ref, "element_velocities": vec_to_ref,
+                "element_affine_momenta": rows_to_ref, "element_directions": dirs_to_ref}
+        arrs = [conv[k](state[k]) if state.get(k) is not None else None for k in conv]
+        self._check(self._lib.aep_set_mesh_state(self._h, nv, nf, *[_dp(a) for a in arrs]))
+
     def set_level_set(self, ls: LevelSet):
         arr, n = ls.to_c()
         self._check(self._lib.aep_set_levelset(self._h, arr, n))
@@ -537,5 +547,5 @@ class HybridSolver:
                     out_of_domain=s.out_of_domain, fp64_fallbacks=s.fp64_fallbacks, overflow=s.overflow,
                     active_nodes=s.active_nodes, learned_accepted=s.learned_accepted,
                     learned_fallbacks=s.learned_fallbacks, learned_exact=s.learned_exact,
-                    sort_movers=s.sort_movers, orderings=s.orderings,
+                    sort_movers=s.sort_movers, orderings=s.orderings, fp64_apex=s.fp64_apex,
                     total_mass=s.total_mass, total_momentum=list(s.total_momentum))

@@ -1,15 +1,22 @@
-"""Benchmark of the GB300 MPM step: particle-steps/s on the sand-column collapse
-(524,288 Drucker-Prager particles, 128^3 grid, dt = 5e-5), one GPU per rank.
+"""Benchmark of the GB300 MPM step: particle-steps/s of the learned and the plain
+return map on the sand + cloth scene at scale (8,388,608 items: 7,604,222
+Drucker-Prager sand particles under a 512x512-vertex cloth sheet, 512^3 grid,
+dt = 2e-5), one GPU per rank.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`value` is device throughput with the particle state resident in HBM; `e2e` is
-the same metric through the C-ABI with host buffers (pinned), the host->device
-upload and the device->host readback of the particle state inside every timed
-step.  The reference arm (`--impl reference`) runs the FP64 CPU restatement of
-the reference step (oracle/) on all host cores, because the reference itself
-(an MSVC application on Eigen + libigl) cannot be built here.  Multi-GPU runs
-are independent replicas (the step has no data exchange between GPUs).
+`value` is the learned step's device throughput with the state resident in HBM
+(L2 flushed between timed steps); `plain` and `fp64_unstable` are the same scene
+with the exact FP32 return mapping, and with the mappings near the Drucker-Prager
+apex redone in FP64.  `e2e` is the learned step through the C-ABI with the
+caller's host arrays as the state: every step uploads the particle and mesh state
+from page-locked host memory, steps, and reads both back.  The stress error of
+each arm is measured against the FP64 oracle on a window of the same scene.  The
+reference arm (`--impl reference`) runs the FP64 CPU restatement of the reference
+step (oracle/) on all host cores on the same scene, because the reference itself
+(an MSVC application on Eigen + libigl) cannot be built here; it never loads the
+GPU library.  Multi-GPU runs are independent replicas (the step has no data
+exchange between GPUs).
 """
 from __future__ import annotations
 
@@ -32,12 +39,35 @@ METRIC = "particle-steps/s, learned vs plain return map, 1 GB300, at <=1e-3 stre
 UNIT = "particle-steps/s"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
+# acceptance bounds of the learned return map's in-kernel check, (relative, absolute
+# in ln-strain units): "strict" keeps a prediction within 1e-3 of the exact
+# projection's magnitude (or within the FP32 resolution of ln s, 2^-23); "residual"
+# keeps it within 1e-4 of the exact projection
+LEARNED_BOUNDS = {"strict": (1e-3, 2.0 ** -23), "residual_1e-4": (0.0, 1e-4)}
 
-def algorithmic_bytes(phase: str, n_p: int, n_nodes: int) -> float:
-    """Algorithmic bytes per launch (FP32 state, per-particle and per-node terms)."""
-    per = {"p2g": (64, 32), "force": (56, 36), "g2p": (152, 24), "normalize": (0, 44), "grid": (0, 68)}
-    a, b = per[phase]
-    return a * n_p + b * n_nodes
+
+def algorithmic_bytes(kernel: str, counts: dict) -> float:
+    """Algorithmic bytes per launch (FP32 state): the state a kernel must read and
+    write once per item and per active node.  counts: particles (snow/sand), verts,
+    elems (cloth), nodes (active grid nodes), rows (learned-map queue rows)."""
+    p, v, e, nodes = counts["particles"], counts.get("verts", 0), counts.get("elems", 0), counts["nodes"]
+    if kernel == "p2g":  # x, v, B, m of every item; mass + momentum flush per node
+        return 64 * (p + v + e) + 32 * nodes
+    if kernel == "force":  # x, F_E, plastic, vol per particle; cloth: x + vertex force / element stress
+        return 56 * p + 36 * v + 48 * e + 36 * nodes
+    if kernel == "g2p":  # read x, F_E, plastic; write x, v, B, F_E, plastic (particles and vertices)
+        return 152 * (p + v) + 24 * nodes
+    if kernel == "cloth_g2p":  # per element: x, d3, faces, 3 vertex x + v; writes x, v, B, F, plastic
+        return 160 * e + 36 * e
+    if kernel == "mlp":  # a queue row in (37 words) and its F_E, plastic out
+        return counts.get("rows", 0) * (148 + 40)
+    if kernel == "normalize":
+        return 44 * nodes
+    if kernel == "grid":
+        return 68 * nodes
+    if kernel == "cloth_force":
+        return 160 * e
+    raise KeyError(kernel)
 
 
 def measured_peak_gbs():
@@ -122,285 +152,128 @@ def job_throughput(items_per_rank: int, steps: int, seconds: float, world: int, 
     return world * items_per_rank * steps / slowest, slowest
 
 
-def make_scene(args):
+def make_scene(name: str):
     from anisotropicelastoplasticity_gb300 import scenes
 
-    return scenes.sand_column(n=args.particles, res=args.res, seed=1)
+    return {"sand_cloth": scenes.sand_cloth, "snow_sand_collision": scenes.snow_sand_collision,
+            "sand_column": scenes.sand_column, "cloth_drape": scenes.cloth_drape,
+            "snow_block": scenes.snow_block}[name]()
 
 
-def cpu_baseline(args, steps: int):
-    """The oracle (FP64 restatement of the reference step) on all host cores, a bounded sample."""
+def scene_config(sc) -> dict:
+    cfg = {"workload": sc.name, "items": sc.num_items(), "grid": [int(r) for r in sc.grid.resolution], "dt": sc.dt}
+    if sc.particles is not None:
+        mat = sc.particles.material
+        cfg["sand"] = int((mat == 1).sum())
+        cfg["snow"] = int((mat == 0).sum())
+    if sc.mesh is not None:
+        cfg["cloth_vertices"] = len(sc.mesh.vertex_positions)
+        cfg["cloth_elements"] = len(sc.mesh.faces)
+    return cfg
+
+
+def item_counts(sc, nodes: int) -> dict:
+    return {"particles": len(sc.particles) if sc.particles is not None else 0,
+            "verts": len(sc.mesh.vertex_positions) if sc.mesh is not None else 0,
+            "elems": len(sc.mesh.faces) if sc.mesh is not None else 0, "nodes": nodes}
+
+
+def fp32_state(sc):
+    """The scene with its particle state rounded to FP32 values, so that the GPU and
+    the oracle start from identical numbers."""
+    ps = sc.particles
+    for k in ("positions", "velocities", "affine_momenta", "elastic_deformation_gradients", "masses",
+              "plastic_amount"):
+        setattr(ps, k, getattr(ps, k).astype(np.float32).astype(np.float64))
+    return sc
+
+
+def window(sc, half: float, strain: float, seed: int):
+    """The sand of a scene inside |x - 0.5|, |y - 0.5| < half (all heights), on the
+    scene's own grid, level set, parameters and time step, optionally with random
+    elastic strain of relative size `strain` (every particle stressed, the return
+    mappings active from the first step), in FP32 values."""
+    from anisotropicelastoplasticity_gb300.scenes import Scene
+
+    ps = sc.particles
+    sel = (np.abs(ps.positions[:, 0] - 0.5) < half) & (np.abs(ps.positions[:, 1] - 0.5) < half)
+    sub = ps.copy()
+    for k in ("positions", "velocities", "affine_momenta", "elastic_deformation_gradients",
+              "plastic_deformation_gradients", "masses", "volumes", "plastic_amount", "material"):
+        setattr(sub, k, np.ascontiguousarray(getattr(ps, k)[sel]))
+    if strain:
+        rng = np.random.default_rng(seed)
+        sub.elastic_deformation_gradients = np.eye(3) + strain * rng.standard_normal((len(sub), 3, 3))
+    out = Scene(sc.name + "_window", sc.grid, sub, sc.levelset, sc.params, sc.dt, sc.steps)
+    return fp32_state(out)
+
+
+# ---------------------------------------------------------------------------------------
+# reference arm and CPU baseline: the oracle on the host cores (never loads libaep.so)
+
+def oracle_steps(sc, warmup: int, steps: int, threads: int):
     from oracle.oracle import Oracle
 
-    sc = make_scene(args)
-    orc = Oracle(sc.grid, sc.params, threads=os.cpu_count() or 1)
-    orc.set_particle_system(sc.particles)
+    orc = Oracle(sc.grid, sc.params, threads=threads)
+    if sc.particles is not None:
+        orc.set_particle_system(sc.particles)
+    if sc.mesh is not None:
+        orc.set_lagrangian_mesh(sc.mesh)
     orc.set_level_set(sc.levelset)
     orc.init(volumes=True)
-    orc.step(sc.dt)  # warm-up
+    for _ in range(warmup):
+        orc.step(sc.dt)
     t0 = time.perf_counter()
     for _ in range(steps):
         orc.step(sc.dt)
-    dt = time.perf_counter() - t0
-    # one thread, as the reference runs: one step of the same scene
-    one = Oracle(sc.grid, sc.params, threads=1)
-    one.set_particle_system(sc.particles)
-    one.set_level_set(sc.levelset)
-    one.init(volumes=True)
-    t1 = time.perf_counter()
-    one.step(sc.dt)
-    dt1 = time.perf_counter() - t1
-    return {"value": len(sc.particles) * steps / dt, "unit": UNIT, "cores": orc.threads, "kind": "port",
-            "sample": f"{steps} full steps of the {len(sc.particles)}-particle sand column (128^3 grid), FP64, "
-                      f"{orc.threads} OpenMP threads, after 1 warm-up step",
-            "single_thread": {"value": len(sc.particles) / dt1, "unit": UNIT, "cores": 1,
-                              "sample": "1 full step of the same scene on one thread"}}
+    el = time.perf_counter() - t0
+    n_thr = orc.threads
+    orc.close()
+    return el, n_thr
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return None
-    from oracle.oracle import Oracle
-
-    sc = make_scene(args)
-    orc = Oracle(sc.grid, sc.params, threads=os.cpu_count() or 1)
-    orc.set_particle_system(sc.particles)
-    orc.set_level_set(sc.levelset)
-    orc.init(volumes=True)
-    for _ in range(args.warmup):
-        orc.step(sc.dt)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        orc.step(sc.dt)
-    el = time.perf_counter() - t0
-    v = len(sc.particles) * args.steps / el
+    sc = make_scene(args.workload)
+    warm, steps = min(args.warmup, args.ref_warmup), min(args.steps, args.ref_steps)
+    el, thr = oracle_steps(sc, warm, steps, os.cpu_count() or 1)
+    v = sc.num_items() * steps / el
+    sample = (f"{steps} full steps of the whole {sc.name} scene ({sc.num_items()} items) after {warm} warm-up "
+              f"step(s), FP64, {thr} OpenMP threads (each step as long as the reference's, so the run is capped "
+              f"at {args.ref_steps} timed steps)")
     return {
         "metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded sand column)",
-        "config": {"workload": "sand_column", "particles": len(sc.particles), "grid": [args.res] * 3,
-                   "dt": sc.dt, "material": "drucker_prager_sand"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": orc.threads, "kind": "port",
-                         "sample": f"{args.steps} full steps after {args.warmup} warm-up steps"},
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded {sc.name} scene)",
+        "config": scene_config(sc),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": thr, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference (MSVC + Eigen + libigl) cannot be built here; this arm times oracle/, the FP64 "
-                "C++ restatement of its step with the same sparse-matrix dataflow",
+                "C++ restatement of its step with the same sparse-matrix dataflow, built for the host CPU",
     }
 
 
-def run_ours(args):
-    import torch
+# ---------------------------------------------------------------------------------------
+# the GPU arms
 
-    from anisotropicelastoplasticity_gb300 import HybridSolver
-    from anisotropicelastoplasticity_gb300.solver import mats_to_ref, rows_to_ref, vec_to_ref  # noqa: F401
-
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
-    sc = make_scene(args)
-    n_p = len(sc.particles)
-    solver = HybridSolver(sc.particles, sc.grid, sc.params)
-    solver.set_level_set(sc.levelset)
-    stream = torch.cuda.Stream()
-    solver.set_stream(stream.cuda_stream)
-    solver.init_volumes()
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    for _ in range(args.warmup):
-        solver.step(sc.dt)
-    solver.synchronize()
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    orderings0 = solver.stats()["orderings"]
-    barrier()
-    with ClockSampler(local) as clk:
-        wall0 = time.perf_counter()
-        with torch.cuda.stream(stream):
-            for k in range(args.steps):
-                flush.zero_()  # L2 flush between timed steps (outside the events)
-                starts[k].record(stream)
-                solver.step(sc.dt)
-                ends[k].record(stream)
-        solver.synchronize()
-        barrier()
-        wall = time.perf_counter() - wall0
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    st = solver.stats()
-    orderings = st["orderings"] - orderings0
-    # per-kernel times: the same number of steps again with the library's CUDA events
-    # between its launches (each event adds ~2 us to the step, so the steps above
-    # are timed without them)
-    solver.set_profiling(True)
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.zero_()
-            solver.step(sc.dt)
-    solver.synchronize()
-    phase_ms, timed = solver.phase_times()
-    solver.set_profiling(False)
-    # the branch the ordering graph takes on this workload: step on (untimed) to the
-    # next ordering and read its mover count (up to 32 movers: 2 kernels; up to
-    # 8,192: 3; more: the CUB radix sort)
-    order_movers = None
-    for _ in range(int(sc.params.reorder_interval) + 1):
-        o0 = solver.stats()["orderings"]
-        solver.step(sc.dt)
-        st2 = solver.stats()
-        if st2["orderings"] > o0:
-            order_movers = int(st2["sort_movers"])
-            break
-    per_order = 3 if order_movers is not None and order_movers > 32 else 2
-    value, sec = job_throughput(n_p, args.steps, ms * 1e-3, world)
-    ms = sec * 1e3
-
-    # roofline of the dominant kernel (CUDA events on the launching stream)
-    per_launch = {k: v / max(timed, 1) for k, v in phase_ms.items()}
-    dom = max(("p2g", "force", "g2p"), key=lambda k: per_launch[k])
-    peak, peak_kind = measured_peak_gbs()
-    nodes = int(st["active_nodes"])
-    ach = algorithmic_bytes(dom, n_p, nodes) / (per_launch[dom] * 1e-3) / 1e9
-    traffic = None
-    tp = ROOT / "profiles" / "traffic.json"
-    if tp.exists():
-        try:
-            t = json.loads(tp.read_text()).get(dom)
-            if t:
-                traffic = t["bytes_per_particle"] * n_p + t.get("bytes_per_node", 0.0) * nodes
-        except Exception:
-            traffic = None
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": traffic, "peak_source": peak_kind,
-                "profiled_ms_per_step": sum(phase_ms.values()) / max(timed, 1),
-                "kernels": {k: {"ms_per_launch": per_launch[k],
-                                "algorithmic_GBps": (algorithmic_bytes(k, n_p, nodes) / (per_launch[k] * 1e-3) / 1e9)
-                                if k in ("p2g", "force", "g2p", "normalize", "grid") else None}
-                            for k in per_launch}}
-
-    # end to end through the C-ABI with pinned host buffers
-    e2e = None
-    if not args.no_e2e:
-        e2e = run_e2e(args, solver, sc, stream, world)
-
-    out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded sand column)",
-        "config": {"workload": "sand_column", "particles": n_p, "grid": [args.res] * 3, "dt": sc.dt,
-                   "material": "drucker_prager_sand", "return_map": "plain", "parallelism": f"replicas{world}",
-                   "reorder_interval": int(sc.params.reorder_interval), "orderings_timed": orderings,
-                   "l2": "flushed between timed steps (512 MB write)", "active_nodes": nodes,
-                   "active_blocks": int(st["active_blocks"])},
-        "roofline": roofline,
-        # per step k_p2g, k_normalize, k_force, k_force_fp64, k_grid, k_g2p; per ordering
-        # (every reorder_interval-th step) the ordering graph's k_flag_movers +
-        # k_place_stayers (+ k_place_movers when more than 32 particles changed cell;
-        # CUB radix-sort kernels instead when more than 8,192 did)
-        "gpu_launches": 6 * args.steps + per_order * orderings,
-        "launches_note": f"6 library kernels per step + {per_order} per ordering ({orderings} orderings in the "
-                         f"timed steps, every {int(sc.params.reorder_interval)}th step; an ordering moves "
-                         f"{order_movers} particles on this workload)",
-        "fp64_fallbacks_last_step": int(st["fp64_fallbacks"]),
-        "wall_s": wall,
-    }
-    out["clocks"] = clk.summary()
-    if e2e is not None:
-        out["e2e"] = e2e
-    if rank == 0 and not args.no_learned:
-        out["learned_vs_plain"] = run_learned_vs_plain(args, torch, flush)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, args.cpu_steps)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
-    return out if rank == 0 else None
-
-
-def stress(F, plastic, mat, prm, vol=1.0):
-    """Per-particle stress V P(F) F^T of the reference's two laws (HybridSolver.cpp:314-339)
-    evaluated in FP64 on the host, for error statistics; F: (N, 3, 3)."""
-    F = np.asarray(F, np.float64)
-    U, S, Vt = np.linalg.svd(F)
-    out = np.zeros_like(F)
-    snow = mat == 0
-    if snow.any():
-        E, nu, xi = prm.snow.E, prm.snow.nu, prm.snow.xi
-        lam0, mu0 = E * nu / (1 + nu) / (1 - 2 * nu), E / 2 / (1 + nu)
-        hard = np.exp(xi * (1 - plastic[snow]))
-        Fs = F[snow]
-        R = U[snow] @ Vt[snow]
-        J = np.linalg.det(Fs)
-        cof = np.linalg.inv(Fs).transpose(0, 2, 1) * J[:, None, None]
-        P = 2 * (mu0 * hard)[:, None, None] * (Fs - R) + ((lam0 * hard) * (J - 1))[:, None, None] * cof
-        out[snow] = P @ Fs.transpose(0, 2, 1)
-    sand = mat == 1
-    if sand.any():
-        E, nu = prm.sand.E, prm.sand.nu
-        lam, mu = E * nu / (1 + nu) / (1 - 2 * nu), E / 2 / (1 + nu)
-        ln = np.log(S[sand])
-        d = (2 * mu * ln + lam * ln.sum(1, keepdims=True)) / S[sand]
-        P = U[sand] @ (d[:, :, None] * Vt[sand])
-        out[sand] = P @ F[sand].transpose(0, 2, 1)
-    return out * np.asarray(vol, np.float64).reshape(-1, 1, 1)
-
-
-def rel_stats(a, b):
-    """Per-particle |P_gpu - P_fp64| / max(|P_fp64|, 1e-2 * rms |P_fp64|) (Frobenius), and
-    the same error relative to the rms stress of the sample (p99_rms, max_rms)."""
-    na = np.linalg.norm((a - b).reshape(len(a), -1), axis=1)
-    nb = np.linalg.norm(b.reshape(len(b), -1), axis=1)
-    rms = np.sqrt(np.mean(nb ** 2))
-    floor = 1e-2 * rms
-    r = na / np.maximum(nb, floor)
-    return {"median": float(np.median(r)), "p99": float(np.percentile(r, 99)), "max": float(r.max()),
-            "p99_rms": float(np.percentile(na, 99) / rms), "max_rms": float(na.max() / rms),
-            "particles": int(len(r)), "floor": float(floor)}
-
-
-# acceptance bounds of the learned return map's in-kernel check, (relative, absolute
-# in ln-strain units): "strict" keeps a prediction within 1e-3 of the exact
-# projection's magnitude (or within the FP32 resolution of ln s, 2^-23); "residual"
-# keeps it within 1e-4 of the exact projection, the residual bound of the
-# learned-map configuration
-LEARNED_BOUNDS = {"strict": (1e-3, 2.0 ** -23), "residual_1e-4": (0.0, 1e-4)}
-
-
-def strained(scene, seed):
-    """The scene with +-1% random elastic strain (seeded): every particle carries
-    stress and the return mappings are active from the first step."""
-    ps = scene.particles
-    rng = np.random.default_rng(seed)
-    ps.elastic_deformation_gradients = np.eye(3) + 0.01 * rng.standard_normal((len(ps), 3, 3))
-    return scene
-
-
-def run_learned_vs_plain(args, torch, flush):
+def train_mlp(args, torch):
     """Train the learned return map on (trial, projected) pairs that the plain mapping
-    produces on the snow block (from its ground impact on), the sand column and the
-    cloth drape (cloth rows); time the plain and the learned step on the snow+sand
-    collision (2,097,152 particles, 256^3) and on sand under cloth (8,388,608
-    items, 512^3) under the two acceptance bounds, and measure the stress error of
-    each against the FP64 oracle on a bounded sample of the collision."""
-    from anisotropicelastoplasticity_gb300 import HybridSolver, scenes
+    produces on the snow block (from its ground impact on), the sand column, the cloth
+    drape (cloth rows) and the snow + sand collision family (another seed)."""
+    from anisotropicelastoplasticity_gb300 import scenes
     from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP, harvest_records
 
     t0 = time.perf_counter()
     quarter = args.harvest // 4
-    # the snow block reaches the ground after ~1,750 steps of 1e-4 s; its plastic
-    # states come from the impact.  The collision's own family (another seed, a
-    # quarter of the particles, with and without the +-1% strain of the error
-    # sample) gives the states of the evaluated scenes.
+
+    def strained(sc, seed):
+        rng = np.random.default_rng(seed)
+        ps = sc.particles
+        ps.elastic_deformation_gradients = np.eye(3) + 0.01 * rng.standard_normal((len(ps), 3, 3))
+        return sc
+
     parts = {"snow_block": harvest_records(scenes.snow_block(), steps=600, capacity=quarter, stride=1,
                                            warm_steps=1700),
              "sand_column": harvest_records(scenes.sand_column(), steps=500, capacity=quarter, stride=8),
@@ -419,191 +292,358 @@ def run_learned_vs_plain(args, torch, flush):
     _, loss1 = mlp.gradient(recs.data_ptr(), n_rec)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    del recs
+    info = {"records": n_rec, "records_per_source": {k: len(v) for k, v in parts.items()},
+            "sources": "snow_block steps 1700-2300 (ground impact) + sand_column 500 steps (stride 8) + cloth_drape "
+                       "(128x128 sheet) 400 steps + snow_sand_collision (262,144 particles, 128^3, seed 5) 100 steps "
+                       "+ the same with +-1% strain (seed 12) 5 steps; plastic states without the constant "
+                       "projections (sand apex, cloth in tension)",
+            "steps": args.train_steps, "batch": 8192, "loss_before": loss0, "loss_after": loss1,
+            "harvest_s": t1 - t0, "train_s": t2 - t1}
+    return mlp, info
 
-    def timed(scene, bounds, steps):
-        s = HybridSolver(scene.particles, scene.grid, scene.params)
-        if scene.mesh is not None:
-            s.set_lagrangian_mesh(scene.mesh)
-        s.set_level_set(scene.levelset)
-        stream = torch.cuda.Stream()
+
+def with_fp64_apex(prm):
+    """A copy of the parameters with the FP64 redo of near-apex sand mappings on."""
+    p = type(prm).from_buffer_copy(prm)
+    p.fp64_apex = 1
+    return p
+
+
+def new_solver(sc, stream, prm=None, mlp=None, bounds=None):
+    from anisotropicelastoplasticity_gb300 import HybridSolver
+
+    s = HybridSolver(sc.particles, sc.grid, prm if prm is not None else sc.params)
+    if sc.mesh is not None:
+        s.set_lagrangian_mesh(sc.mesh)
+    s.set_level_set(sc.levelset)
+    if stream is not None:
         s.set_stream(stream.cuda_stream)
-        s.init_volumes()
-        if bounds is not None:
-            s.set_return_map(mlp, bounds[0], bounds[1])
-        for _ in range(3):
-            s.step(scene.dt)
-        s.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        cnt = {"accepted": 0, "fallbacks": 0, "exact_constant": 0}
+    s.init_volumes()
+    if mlp is not None:
+        s.set_return_map(mlp, bounds[0], bounds[1])
+    return s
+
+
+def time_arm(torch, sc, args, flush, world, prm=None, mlp=None, bounds=None, phases=True, clocks=None, keep=False):
+    """Warm-up, then exactly args.steps timed steps (CUDA events on the solver's stream,
+    L2 flushed between steps outside the events), barrier + max over ranks; then the
+    same number of steps again with the library's per-kernel events."""
+    stream = torch.cuda.Stream()
+    s = new_solver(sc, stream, prm, mlp, bounds)
+    for _ in range(args.warmup):
+        s.step(sc.dt)
+    s.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    cnt = {"accepted": 0, "fallbacks": 0, "exact_constant": 0, "fp64_apex": 0, "fp64_fallbacks": 0}
+    orderings0 = s.stats()["orderings"]
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    ctx = clocks if clocks is not None else _Null()
+    with ctx:
+        wall0 = time.perf_counter()
         with torch.cuda.stream(stream):
             for a, b in ev:
-                flush.zero_()
+                flush.zero_()  # L2 flush between timed steps (outside the events)
                 a.record(stream)
-                s.step(scene.dt)
+                s.step(sc.dt)
                 b.record(stream)
-                st = s.stats()
-                cnt["accepted"] += st["learned_accepted"]
-                cnt["fallbacks"] += st["learned_fallbacks"]
-                cnt["exact_constant"] += st["learned_exact"]
         s.synchronize()
-        ms = sum(a.elapsed_time(b) for a, b in ev)
+        barrier()
+        wall = time.perf_counter() - wall0
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    st = s.stats()
+    out = {"orderings_timed": st["orderings"] - orderings0, "wall_s": wall}
+    # counters per step are read in a second, untimed pass (reading them synchronises)
+    for _ in range(min(args.steps, 5)):
+        s.step(sc.dt)
+        st = s.stats()
+        cnt["accepted"] += st["learned_accepted"]
+        cnt["fallbacks"] += st["learned_fallbacks"]
+        cnt["exact_constant"] += st["learned_exact"]
+        cnt["fp64_apex"] += st["fp64_apex"]
+        cnt["fp64_fallbacks"] += st["fp64_fallbacks"]
+    value, sec = job_throughput(sc.num_items(), args.steps, ms * 1e-3, world)
+    out.update({"value": value, "ms_per_step": sec * 1e3 / args.steps, "counts_over_5_steps": cnt,
+                "active_nodes": int(st["active_nodes"]), "active_blocks": int(st["active_blocks"]),
+                "orderings_movers": int(st["sort_movers"])})
+    if mlp is not None:
+        out["fallback_rate"] = cnt["fallbacks"] / max(cnt["accepted"] + cnt["fallbacks"], 1)
+    if phases:
+        s.set_profiling(True)
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                flush.zero_()
+                s.step(sc.dt)
+        s.synchronize()
+        ph, timed = s.phase_times()
+        s.set_profiling(False)
+        out["kernel_ms"] = {k: v / max(timed, 1) for k, v in ph.items()}
+        out["profiled_ms_per_step"] = sum(ph.values()) / max(timed, 1)
+        out["mlp_rows_last_step"] = int(s.stats()["learned_accepted"] + s.stats()["learned_fallbacks"])
+    if keep:
+        out["_solver"] = s
+        out["_stream"] = stream
+    else:
         s.close()
-        return scene.num_items() * steps / (ms * 1e-3), cnt
-
-    def compare(scene):
-        plain, _ = timed(scene, None, args.learned_steps)
-        out = {"plain": plain}
-        for name, bounds in LEARNED_BOUNDS.items():
-            v, cnt = timed(scene, bounds, args.learned_steps)
-            out[name] = {"learned": v, "learned_over_plain": v / plain,
-                         "fallback_rate": cnt["fallbacks"] / max(cnt["accepted"] + cnt["fallbacks"], 1),
-                         "counts_over_timed_steps": cnt}
-        return out
-
-    big = scenes.snow_sand_collision()
-    res3 = compare(big)
-    n_big, dt_big = len(big.particles), big.dt
-    del big
-    # sand under cloth at 512^3 (8,388,608 particles: sand + cloth vertices + elements)
-    c4 = None
-    if not args.no_config4:
-        sc4 = scenes.sand_cloth()
-        c4 = {"workload": "sand_cloth", "particles": sc4.num_items(),
-              "sand": len(sc4.particles), "cloth_vertices": len(sc4.mesh.vertex_positions),
-              "cloth_elements": len(sc4.mesh.faces), "grid": [512] * 3, "dt": sc4.dt, "steps": args.learned_steps}
-        c4.update(compare(sc4))
-        del sc4
-
-    # stress error against the FP64 oracle on a bounded sample of the same scene
-    from oracle.oracle import Oracle
-
-    # start from strained states (+-1% random elastic strain) so that every particle
-    # carries stress and the return mappings of both materials are active from the
-    # first step
-    small = strained(scenes.snow_sand_collision(n=args.err_particles, res=128, seed=3), 11)
-    o = Oracle(small.grid, small.params, threads=os.cpu_count() or 1)
-    o.set_particle_system(small.particles)
-    o.set_level_set(small.levelset)
-    o.init(volumes=True)
-    runs = {}
-    for name, bounds in [("plain", None)] + list(LEARNED_BOUNDS.items()):
-        s = HybridSolver(small.particles, small.grid, small.params)
-        s.set_level_set(small.levelset)
-        s.init_volumes()
-        if bounds is not None:
-            s.set_return_map(mlp, bounds[0], bounds[1])
-        runs[name] = s
-    errs = {name: {} for name in runs}
-    errs["fp32_state_floor"] = {}
-    counts = {name: {"accepted": 0, "fallbacks": 0, "exact_constant": 0} for name in LEARNED_BOUNDS}
-    mat = small.particles.material
-    last = args.err_steps - 1
-    for k in range(args.err_steps):
-        o.step(small.dt)
-        op = o.get_particles()
-        ref = stress(op["elastic_deformation_gradients"], op["plastic"], mat, small.params, op["volumes"])
-        got = {name: None for name in runs}
-        for name, s in runs.items():
-            s.step(small.dt)
-            gp = s.get_particles()
-            got[name] = stress(gp["elastic_deformation_gradients"], gp["plastic"], mat, small.params, gp["volumes"])
-            if name in counts:
-                st = s.stats()
-                counts[name]["accepted"] += st["learned_accepted"]
-                counts[name]["fallbacks"] += st["learned_fallbacks"]
-                counts[name]["exact_constant"] += st["learned_exact"]
-        # the oracle's own state rounded to FP32: the error any FP32 state carries
-        got["fp32_state_floor"] = stress(op["elastic_deformation_gradients"].astype(np.float32),
-                                         op["plastic"].astype(np.float32), mat, small.params,
-                                         op["volumes"].astype(np.float32))
-        if k in (0, last):
-            for name, g in got.items():
-                if k == last:
-                    errs[name].update(rel_stats(g, ref))
-                # per material (sand's return mapping is discontinuous where it
-                # switches to the apex at tr(ln s) = 0, HS:655-663)
-                for mname, mval in (("snow", 0), ("sand", 1)):
-                    sel = mat == mval
-                    errs[name][f"{mname}_step{k + 1}"] = rel_stats(g[sel], ref[sel])
-    for s in runs.values():
-        s.close()
-    for name, c in counts.items():
-        errs[name]["counts"] = c
-    t3 = time.perf_counter()
-    return {
-        "workload": "snow_sand_collision", "particles": n_big, "grid": [256] * 3, "dt": dt_big,
-        "steps": args.learned_steps, **res3,
-        "bounds": {k: {"rel": v[0], "abs": v[1]} for k, v in LEARNED_BOUNDS.items()},
-        "stress_rel_err_vs_fp64": {**errs,
-                                   "sample": f"{args.err_particles} particles of the same scene on 128^3 with "
-                                             f"+-1% random initial elastic strain, after {args.err_steps} steps "
-                                             f"(per material also after 1), per-particle |dP| / max(|P|, 1e-2 "
-                                             f"rms|P|); fp32_state_floor = the oracle's state rounded to FP32"},
-        "training": {"records": n_rec, "records_per_source": {k: len(v) for k, v in parts.items()},
-                     "sources": "snow_block steps 1700-2300 (ground impact) + sand_column 500 steps (stride 8) + "
-                                "cloth_drape (128x128 sheet) 400 steps + snow_sand_collision (262,144 particles, "
-                                "128^3, seed 5) 100 steps + the same with +-1% strain (seed 12) 5 steps; plastic "
-                                "states without the constant projections (sand apex, cloth in tension) and "
-                                "without sand states within 1e-4 of ln s = 0",
-                     "steps": args.train_steps, "batch": 8192, "loss_before": loss0, "loss_after": loss1,
-                     "harvest_s": t1 - t0, "train_s": t2 - t1},
-        "sand_cloth": c4,
-        "note": "the network runs after the SVD and its output is checked against the exact projection in the "
-                "kernel, so it adds work to the step; reported as measured",
-        "wall_s": t3 - t0,
-    }
+    return out
 
 
-def run_e2e(args, solver, sc, stream, world=1):
-    import torch
+class _Null:
+    def __enter__(self):
+        return self
 
+    def __exit__(self, *a):
+        return False
+
+
+def roofline_of(arm: dict, counts: dict) -> dict:
+    """The dominant kernel of a step (slowest per launch among P2G, force, G2P) against
+    the measured HBM copy bandwidth."""
+    km = arm["kernel_ms"]
+    counts = dict(counts, rows=arm.get("mlp_rows_last_step", 0))
+    dom = max(("p2g", "force", "g2p"), key=lambda k: km[k])
+    peak, peak_kind = measured_peak_gbs()
+    ach = algorithmic_bytes(dom, counts) / (km[dom] * 1e-3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "traffic.json"
+    if tp.exists():
+        try:
+            t = json.loads(tp.read_text()).get(arm.get("workload", ""), {}).get(dom)
+            if t:
+                traffic = t["bytes_per_item"] * (counts["particles"] + counts["verts"]) + \
+                    t.get("bytes_per_node", 0.0) * counts["nodes"]
+        except Exception:
+            traffic = None
+    kernels = {}
+    for k, v in km.items():
+        try:
+            b = algorithmic_bytes(k, counts)
+        except KeyError:
+            b = None
+        kernels[k] = {"ms_per_launch": v, "algorithmic_GBps": (b / (v * 1e-3) / 1e9) if b and v > 0 else None}
+    return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "traffic": traffic, "peak_source": peak_kind, "profiled_ms_per_step": arm["profiled_ms_per_step"],
+            "kernels": kernels}
+
+
+def run_e2e(args, torch, arm, sc, world):
+    """The learned step through the C-ABI with the caller's page-locked host arrays as
+    the state: aep_set_particles + aep_set_mesh_state, aep_step, aep_get_particles +
+    aep_get_mesh every step."""
+    import ctypes as C
+
+    from anisotropicelastoplasticity_gb300.solver import dirs_to_ref, rows_to_ref, vec_to_ref
+
+    s = arm["_solver"]
+    lib, h = s._lib, s._h
     n = len(sc.particles)
-    ps = solver.sync()  # current state in the reference layout on the host
+    p = s.get_particles()
 
     def pinned(a):
+        a = np.ascontiguousarray(a, np.float64)
         t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
         t.numpy()[...] = a
         return t.numpy()
 
-    host = {
-        "positions": pinned(ps.positions), "velocities": pinned(ps.velocities),
-        "affine_momenta": pinned(ps.affine_momenta),
-        "elastic_deformation_gradients": pinned(ps.elastic_deformation_gradients),
-        "masses": pinned(ps.masses), "volumes": pinned(ps.volumes), "plastic_amount": pinned(ps.plastic_amount),
-    }
-    steps = max(1, min(args.steps, 10))
-    import ctypes as C
+    from anisotropicelastoplasticity_gb300.solver import mats_to_ref
 
-    lib = solver._lib
-    h = solver._h
-    from anisotropicelastoplasticity_gb300.solver import mats_to_ref, rows_to_ref, vec_to_ref
-
-    bufs = {
-        "x": pinned(vec_to_ref(host["positions"])), "v": pinned(vec_to_ref(host["velocities"])),
-        "B": pinned(rows_to_ref(host["affine_momenta"])), "F": pinned(mats_to_ref(host["elastic_deformation_gradients"])),
-        "m": host["masses"], "vol": host["volumes"], "q": pinned(np.asarray(ps.plastic_amount, float)),
-    }
-    mat = np.ascontiguousarray(ps.material, np.uint8)
+    part = [pinned(vec_to_ref(p["positions"])), pinned(vec_to_ref(p["velocities"])),
+            pinned(rows_to_ref(p["affine_momenta"])), pinned(mats_to_ref(p["elastic_deformation_gradients"])),
+            pinned(sc.particles.masses), pinned(p["volumes"]), pinned(p["plastic"])]
+    mat = np.ascontiguousarray(sc.particles.material, np.uint8)
+    mesh = None
+    if sc.mesh is not None:
+        m = s.get_mesh()
+        mesh = [pinned(vec_to_ref(m["vertex_positions"])), pinned(vec_to_ref(m["vertex_velocities"])),
+                pinned(rows_to_ref(m["vertex_affine_momenta"])), pinned(vec_to_ref(m["element_positions"])),
+                pinned(vec_to_ref(m["element_velocities"])), pinned(rows_to_ref(m["element_affine_momenta"])),
+                pinned(dirs_to_ref(m["element_directions"]))]
+        nv, nf = len(sc.mesh.vertex_positions), len(sc.mesh.faces)
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
     h2d = 8 * (3 + 3 + 9 + 9 + 1 + 1 + 1) * n + n
     d2h = 8 * (3 + 3 + 9 + 9 + 1 + 1) * n
+    if mesh is not None:
+        mesh_bytes = 8 * ((3 + 3 + 9) * nv + (3 + 3 + 9 + 9) * nf)
+        h2d += mesh_bytes
+        d2h += mesh_bytes
+    steps = max(1, min(args.steps, args.e2e_steps))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        st = lib.aep_set_particles(h, n, dp(bufs["x"]), dp(bufs["v"]), dp(bufs["B"]), dp(bufs["F"]), None,
-                                   dp(bufs["m"]), dp(bufs["vol"]), dp(bufs["q"]),
-                                   mat.ctypes.data_as(C.POINTER(C.c_uint8)))
+        st = lib.aep_set_particles(h, n, dp(part[0]), dp(part[1]), dp(part[2]), dp(part[3]), None, dp(part[4]),
+                                   dp(part[5]), dp(part[6]), mat.ctypes.data_as(C.POINTER(C.c_uint8)))
         assert st == 0, st
+        if mesh is not None:
+            assert lib.aep_set_mesh_state(h, nv, nf, *[dp(a) for a in mesh]) == 0
         assert lib.aep_step(h, sc.dt) == 0
-        st = lib.aep_get_particles(h, n, dp(bufs["x"]), dp(bufs["v"]), dp(bufs["B"]), dp(bufs["F"]), None,
-                                   dp(bufs["vol"]), dp(bufs["q"]))
-        assert st == 0, st
+        assert lib.aep_get_particles(h, n, dp(part[0]), dp(part[1]), dp(part[2]), dp(part[3]), None, dp(part[5]),
+                                     dp(part[6])) == 0
+        if mesh is not None:
+            assert lib.aep_get_mesh(h, *[dp(a) for a in mesh]) == 0
     el = time.perf_counter() - t0
-    value, _ = job_throughput(n, steps, el, world)
-    return {"value": value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "steps": steps, "path": "aep_set_particles + aep_step + aep_get_particles, pinned FP64 host arrays "
-                                    "in the reference layouts"}
+    value, _ = job_throughput(sc.num_items(), steps, el, world)
+    return {"value": value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": steps,
+            "path": "aep_set_particles + aep_set_mesh_state + aep_step (learned return map) + aep_get_particles + "
+                    "aep_get_mesh, page-locked FP64 host arrays in the reference layouts"}
+
+
+def stress_errors(args, torch, sc_full, mlp, bounds):
+    """Stress error of the plain, FP64-near-apex and learned steps against the FP64
+    oracle on a window of the scene's own sand, with +-1% random elastic strain, and
+    the error of the oracle's state rounded to FP32 (the floor of any FP32 state)."""
+    from oracle.oracle import Oracle
+    from oracle.stress import rel_stats, stress
+
+    sc = window(sc_full, args.err_half, 0.01, 11)
+    o = Oracle(sc.grid, sc.params, threads=os.cpu_count() or 1)
+    o.set_particle_system(sc.particles)
+    o.set_level_set(sc.levelset)
+    o.init(volumes=True)
+    arms = {"plain": new_solver(sc, None),
+            "fp64_unstable": new_solver(sc, None, with_fp64_apex(sc.params)),
+            "learned": new_solver(sc, None, mlp=mlp, bounds=bounds)}
+    mat = sc.particles.material
+    errs = {k: {} for k in list(arms) + ["fp32_state_floor"]}
+    t_orc = 0.0
+    for k in range(args.err_steps):
+        t0 = time.perf_counter()
+        o.step(sc.dt)
+        t_orc += time.perf_counter() - t0
+        op = o.get_particles()
+        ref = stress(op["elastic_deformation_gradients"], op["plastic"], mat, sc.params, op["volumes"])
+        got = {"fp32_state_floor": stress(op["elastic_deformation_gradients"].astype(np.float32),
+                                          op["plastic"].astype(np.float32), mat, sc.params,
+                                          op["volumes"].astype(np.float32))}
+        for name, s in arms.items():
+            s.step(sc.dt)
+            gp = s.get_particles()
+            got[name] = stress(gp["elastic_deformation_gradients"], gp["plastic"], mat, sc.params, gp["volumes"])
+        if k in (0, args.err_steps - 1):
+            for name, g in got.items():
+                errs[name][f"step{k + 1}"] = rel_stats(g, ref)
+    for s in arms.values():
+        s.close()
+    o.close()
+    return {"errors": errs, "sample": f"{len(mat)} sand particles of the {sc_full.name} scene inside |x-0.5|, |y-0.5| "
+                                       f"< {args.err_half} (its 512^3 grid, level set and dt), +-1% random elastic "
+                                       f"strain, FP32-representable inputs for both sides; per-particle |dP| / "
+                                       f"max(|P|, 1e-2 rms|P|) after 1 and {args.err_steps} steps",
+            "bound": 1e-3, "oracle_s": t_orc, "oracle_particle_steps_per_s": len(mat) * args.err_steps / t_orc,
+            "oracle_threads": os.cpu_count() or 1}
+
+
+def cpu_single_thread(args):
+    """One step of a small window of the scene on one thread, as the reference runs."""
+    sc = window(make_scene(args.workload), 0.01, 0.0, 0)
+    el, thr = oracle_steps(sc, 0, 1, 1)
+    return {"value": len(sc.particles) / el, "unit": UNIT, "cores": 1,
+            "sample": f"1 step of {len(sc.particles)} sand particles of the scene inside |x-0.5|, |y-0.5| < 0.01 "
+                      f"on its 512^3 grid, one thread"}
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    mlp, training = (None, None) if args.no_learned else train_mlp(args, torch)
+    bounds = LEARNED_BOUNDS[args.bound]
+    sc = make_scene(args.workload)
+    clk = ClockSampler(local)
+    # the headline: the learned step (the plain step when --no-learned)
+    head = time_arm(torch, sc, args, flush, world, mlp=mlp, bounds=bounds, clocks=clk, keep=not args.no_e2e)
+    head["workload"] = sc.name
+    e2e = run_e2e(args, torch, head, sc, world) if not args.no_e2e else None
+    if "_solver" in head:
+        head.pop("_solver").close()
+        head.pop("_stream")
+    plain = time_arm(torch, sc, args, flush, world) if mlp is not None else head
+    fp64 = time_arm(torch, sc, args, flush, world, prm=with_fp64_apex(sc.params), phases=False)
+    nodes = head["active_nodes"]
+    counts = item_counts(sc, nodes)
+    plain["workload"] = sc.name
+    roofline = roofline_of(head, counts)
+    # per step: P2G, normalise, cloth forces, force, FP64 force redo, grid update, G2P,
+    # (learned: the finisher), cloth G2P; per ordering the ordering graph's kernels
+    per_step = 9 if mlp is not None else 8
+    if sc.mesh is None:
+        per_step -= 2
+    out = {
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded {sc.name} scene)",
+        "config": dict(scene_config(sc), return_map="learned" if mlp is not None else "plain",
+                       learned_bound={"name": args.bound, "rel": bounds[0], "abs": bounds[1]},
+                       parallelism=f"replicas{world}", reorder_interval=int(sc.params.reorder_interval),
+                       l2="flushed between timed steps (512 MB write)", active_nodes=nodes,
+                       active_blocks=head["active_blocks"], orderings_timed=head["orderings_timed"]),
+        "roofline": roofline,
+        "gpu_launches": per_step * args.steps + 3 * head["orderings_timed"],
+        "launches_note": f"{per_step} library kernels per step + up to 3 per ordering ({head['orderings_timed']} "
+                         f"orderings in the timed steps, every {int(sc.params.reorder_interval)}th step)",
+        "plain": {k: plain[k] for k in ("value", "ms_per_step", "kernel_ms", "counts_over_5_steps") if k in plain},
+        "fp64_unstable": {k: fp64[k] for k in ("value", "ms_per_step", "counts_over_5_steps")},
+        "learned_over_plain": head["value"] / plain["value"] if mlp is not None else None,
+        "fallback_rate": head.get("fallback_rate"),
+        "learned_counts_over_5_steps": head["counts_over_5_steps"] if mlp is not None else None,
+        "wall_s": head["wall_s"],
+    }
+    out["clocks"] = clk.summary()
+    if e2e is not None:
+        out["e2e"] = e2e
+    if training is not None:
+        out["training"] = training
+    if rank == 0 and not args.no_error:
+        out["stress_rel_err_vs_fp64"] = stress_errors(args, torch, sc, mlp, bounds) if mlp is not None else None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        el, thr = oracle_steps(sc, 0, args.cpu_steps, os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": sc.num_items() * args.cpu_steps / el, "unit": UNIT, "cores": thr,
+                               "kind": "port",
+                               "sample": f"{args.cpu_steps} full step(s) of the whole {sc.name} scene "
+                                         f"({sc.num_items()} items), FP64, {thr} OpenMP threads",
+                               "single_thread": cpu_single_thread(args)}
+    if rank == 0 and not args.no_extra:
+        out["other_workloads"] = other_workloads(args, torch, flush, mlp, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def other_workloads(args, torch, flush, mlp, world):
+    """The sand column (plain) and the snow + sand collision (plain and learned under
+    both acceptance bounds), same timing rules."""
+    out = {}
+    sc = make_scene("sand_column")
+    a = time_arm(torch, sc, args, flush, world)
+    a["workload"] = sc.name
+    out["sand_column"] = {"config": scene_config(sc), "plain": a["value"], "ms_per_step": a["ms_per_step"],
+                          "roofline": roofline_of(a, item_counts(sc, a["active_nodes"]))}
+    sc = make_scene("snow_sand_collision")
+    p = time_arm(torch, sc, args, flush, world, phases=False)
+    res = {"config": scene_config(sc), "plain": p["value"]}
+    if mlp is not None:
+        for name, bounds in LEARNED_BOUNDS.items():
+            a = time_arm(torch, sc, args, flush, world, mlp=mlp, bounds=bounds, phases=name == args.bound)
+            res[name] = {"learned": a["value"], "learned_over_plain": a["value"] / p["value"],
+                         "fallback_rate": a["fallback_rate"], "counts_over_5_steps": a["counts_over_5_steps"]}
+            if "kernel_ms" in a:
+                res[name]["kernel_ms"] = a["kernel_ms"]
+    out["snow_sand_collision"] = res
+    return out
 
 
 def main():
@@ -612,17 +652,21 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--particles", type=int, default=524288)
-    ap.add_argument("--res", type=int, default=128)
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--workload", default="sand_cloth",
+                    choices=["sand_cloth", "snow_sand_collision", "sand_column", "cloth_drape", "snow_block"])
+    ap.add_argument("--bound", choices=sorted(LEARNED_BOUNDS), default="strict")
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--ref-steps", type=int, default=3, help="reference arm: timed steps at most")
+    ap.add_argument("--ref-warmup", type=int, default=1, help="reference arm: warm-up steps at most")
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
-    ap.add_argument("--learned-steps", type=int, default=10)
-    ap.add_argument("--no-config4", action="store_true")
+    ap.add_argument("--no-error", action="store_true")
+    ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--train-steps", type=int, default=200000)
     ap.add_argument("--harvest", type=int, default=4000000)
-    ap.add_argument("--err-particles", type=int, default=65536)
+    ap.add_argument("--err-half", type=float, default=0.02)
     ap.add_argument("--err-steps", type=int, default=5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AEP_ABI_VERSION 1
+#define AEP_ABI_VERSION 2
 
 /* Opaque solver handle: device state of one particle system on one grid. */
 typedef struct aep_solver aep_solver;
@@ -125,7 +125,10 @@ typedef struct aep_params {
                                 the few particles that changed cell since are scattered
                                 and gathered out of order (same physics; the FP32 sums
                                 of a run take its particles in another order)           */
-    int32_t reserved_i;
+    int32_t fp64_apex;       /* 1: sand return mappings near the Drucker-Prager apex (projected
+                                onto it, or |tr ln s| within 1e-3 |ln s| of the switch between
+                                apex and cone, HybridSolver.cpp:652-663) run again in FP64,
+                                counted in aep_stats.fp64_apex; 0 (default): FP32 throughout */
     int64_t reserved[5];
 } aep_params;
 
@@ -147,7 +150,9 @@ typedef struct aep_stats {
     int64_t learned_exact;      /* plastic states with a constant projection (sand apex,
                                    cloth in tension), taken exactly by the learned path  */
     int64_t orderings;          /* particle orderings run by this handle (reorder_interval) */
-    double reserved[2];
+    int64_t fp64_apex;          /* sand return mappings redone in FP64 near the apex
+                                   (aep_params.fp64_apex) in the last step               */
+    double reserved[1];
 } aep_stats;
 
 /* ---- version / defaults ------------------------------------------------------- */
@@ -174,7 +179,8 @@ aep_status aep_solver_destroy(aep_solver* s);
  * plasticAmount (ParticleSystem.h:31), may be NULL (zero); material: N tags.
  * For snow particles the scalar J_P is det(Fp) when Fp is given, else `plastic`
  * (what aep_get_particles returns for snow), else 1.  Re-uploading the same
- * number of particles keeps the device's current particle order.             */
+ * number of particles keeps the device's current particle order and an attached
+ * mesh (a different number removes the mesh: attach it again after the upload). */
 aep_status aep_set_particles(aep_solver* s, int64_t n,
                              const double* x, const double* v, const double* B,
                              const double* Fe, const double* Fp,
@@ -191,7 +197,8 @@ aep_status aep_set_particles(aep_solver* s, int64_t n,
  * and normal stiffness of the normal-direction response; friction_coeff: the
  * frictional cap of the cloth return mapping.  Element positions start at the
  * centroids of their vertices.  Call after aep_set_particles (or without
- * particles) and before the first step; aep_set_particles removes the mesh.    */
+ * particles) and before the first step; aep_set_particles with a different
+ * particle count removes the mesh.                                             */
 aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv, const int32_t* faces,
                         const double* vv, const double* ve, const double* mv, const double* volv,
                         const double* me, const double* vole, const double* d, const double* drest,
@@ -204,6 +211,15 @@ aep_status aep_set_mesh(aep_solver* s, int64_t nv, int64_t nf, const double* xv,
  * pointer may be NULL.                                                          */
 aep_status aep_get_mesh(aep_solver* s, double* xv, double* vv, double* Bv, double* xe,
                         double* ve, double* Be, double* d);
+
+/* Replaces writing LagrangianMesh's public members between steps (LagrangianMesh.h:
+ * 37-61, which the reference's caller may edit in place): the same arrays and layouts
+ * as aep_get_mesh; nv, nf must be the attached mesh's sizes; any pointer may be NULL
+ * (that member is kept).  Masses, volumes, rest directions and faces stay as
+ * aep_set_mesh set them; the device order of the items is kept.                 */
+aep_status aep_set_mesh_state(aep_solver* s, int64_t nv, int64_t nf, const double* xv,
+                              const double* vv, const double* Bv, const double* xe,
+                              const double* ve, const double* Be, const double* d);
 
 /* Replaces LagrangianMesh::bindConstraints(VectorXd* vertexIsFixed)
  * (LagrangianMesh.cpp:354-363): one value per mesh vertex, nonzero = fixed
@@ -344,15 +360,19 @@ aep_status aep_step_stage(aep_solver* s, double dt, int32_t stage);
  * no counterpart (it is single-threaded CPU code).                            */
 aep_status aep_set_stream(aep_solver* s, void* cuda_stream);
 
-/* Kernel phases of one step, in launch order. */
+/* Kernel phases of one step, in launch order (a phase without work, e.g. the
+ * cloth phases without a mesh, takes ~0 ms). */
 enum {
-    AEP_PHASE_SORT = 0,      /* radix sort of the particle keys                  */
-    AEP_PHASE_P2G = 1,       /* mass + APIC momentum scatter                     */
-    AEP_PHASE_NORMALIZE = 2, /* v = p / m on touched nodes                       */
-    AEP_PHASE_FORCE = 3,     /* grad v gather, SVD, stress, impulse scatter      */
-    AEP_PHASE_GRID = 4,      /* grid update, gravity, collision                  */
-    AEP_PHASE_G2P = 5,       /* G2P, APIC, advection, F update, return mapping   */
-    AEP_NUM_PHASES = 6
+    AEP_PHASE_SORT = 0,        /* particle ordering by grid block                     */
+    AEP_PHASE_P2G = 1,         /* mass + APIC momentum scatter                        */
+    AEP_PHASE_NORMALIZE = 2,   /* v = p / m on touched nodes                          */
+    AEP_PHASE_CLOTH_FORCE = 3, /* per-element cloth in-plane forces, normal stress    */
+    AEP_PHASE_FORCE = 4,       /* grad v gather, SVD, stress, impulse scatter         */
+    AEP_PHASE_GRID = 5,        /* grid update, gravity, collision (+ fixed vertices)  */
+    AEP_PHASE_G2P = 6,         /* G2P, APIC, advection, F update, return mapping      */
+    AEP_PHASE_MLP = 7,         /* learned return map: network, check, finish          */
+    AEP_PHASE_CLOTH_G2P = 8,   /* cloth elements: G2P, directions, QR return mapping  */
+    AEP_NUM_PHASES = 9
 };
 
 /* Enable (1) or disable (0) CUDA-event timing of every phase on the handle's
@@ -446,6 +466,20 @@ aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_t
 aep_status aep_p2g_noalloc(const aep_grid_desc* grid, int64_t n,
                            const float* x, const float* v, const float* B, const float* m,
                            double mass_ref, float* mass_out, float* vel_out, void* cuda_stream);
+
+/* ---- ordering -------------------------------------------------------------------------- */
+
+/* The stable radix sort that orders the particles by grid block every
+ * reorder_interval-th step (its counterpart in the reference is the sort inside
+ * Eigen's setFromTriplets, HybridSolver.cpp:92-95), for device arrays: sorts n
+ * (key, value) pairs by the low key_bits bits of the key (1..32), pairs with equal
+ * keys keeping their input order.  Inputs and outputs must not overlap; temp is a
+ * device buffer of aep_sort_pairs_temp_bytes(n, key_bits) bytes.  Queued on
+ * cuda_stream (NULL = the default stream), returns without waiting.               */
+int64_t aep_sort_pairs_temp_bytes(int64_t n, int32_t key_bits);
+aep_status aep_sort_pairs(const uint32_t* keys_in, uint32_t* keys_out, const int32_t* vals_in,
+                          int32_t* vals_out, int64_t n, int32_t key_bits, void* temp,
+                          int64_t temp_bytes, void* cuda_stream);
 
 /* Human-readable text of the last error on this handle (static storage). */
 const char* aep_last_error(aep_solver* s);

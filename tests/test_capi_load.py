@@ -36,7 +36,7 @@ def test_exports_every_declared_symbol():
 
 def test_no_device_calls_without_gpu_are_safe():
     lib = capi.load()
-    assert lib.aep_abi_version() == 1
+    assert lib.aep_abi_version() == 2
     p = capi.default_params()
     assert p.gravity[2] == -9.8 and p.friction == 0.2 and p.friction_bug == 1
     assert p.sand.h0 == 35.0 and p.snow.xi == 10.0

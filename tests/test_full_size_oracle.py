@@ -1,0 +1,117 @@
+"""The benchmark configurations at their own full sizes, GPU step against the FP64
+oracle on identical seeded inputs (HybridSolver.cpp:867-989):
+
+* the grid after the first step's P2G and after its grid update + collision;
+* the particle (and cloth) state after 1 and after 10 steps;
+
+on the 524,288-particle sand column (128^3), the 65,536-vertex cloth drape
+(195,586 items, 128^3) and the 2,097,152-particle snow + sand collision (256^3).
+The bounds are those of the res-32 parity suite (tests/test_parity_gpu.py,
+tests/test_cloth_gpu.py) unless stated at the assertion; every measured
+difference is printed.  The whole-run comparisons (mass, momentum and centre of
+mass every 10 steps) are in tests/test_snow_block_full_run.py.
+"""
+import numpy as np
+import pytest
+
+from anisotropicelastoplasticity_gb300 import HybridSolver, capi, scenes
+
+from oracle.oracle import Oracle
+
+from .parity_util import mass_weighted_rel, max_rel
+
+pytestmark = pytest.mark.gpu
+
+CONFIGS = {"sand_column": scenes.sand_column, "cloth_drape": scenes.cloth_drape,
+           "snow_sand_collision": scenes.snow_sand_collision}
+SIZES = {"sand_column": 524288, "cloth_drape": 195586, "snow_sand_collision": 2097152}
+
+
+def _pair(sc):
+    gpu = HybridSolver(sc.particles, sc.grid, sc.params)
+    orc = Oracle(sc.grid, sc.params)
+    if sc.mesh is not None:
+        gpu.set_lagrangian_mesh(sc.mesh)
+        orc.set_lagrangian_mesh(sc.mesh)
+    if sc.particles is not None:
+        orc.set_particle_system(sc.particles)
+    gpu.set_level_set(sc.levelset)
+    orc.set_level_set(sc.levelset)
+    return gpu, orc
+
+
+def _particle_errors(gp, op, h):
+    bscale = max(np.abs(op["affine_momenta"]).max(), np.abs(op["velocities"]).max() * h)
+    return {"x": float(np.abs(gp["positions"] - op["positions"]).max()),
+            "v": max_rel(gp["velocities"], op["velocities"]),
+            "F": float(np.abs(gp["elastic_deformation_gradients"] - op["elastic_deformation_gradients"]).max()),
+            "B": float(np.abs(gp["affine_momenta"] - op["affine_momenta"]).max() / bscale),
+            "q": float(np.abs(gp["plastic"] - op["plastic"]).max())}
+
+
+def _mesh_errors(gm, om):
+    vs = np.abs(om["vertex_velocities"]).max() / 32
+    return {"x": float(max(np.abs(gm["vertex_positions"] - om["vertex_positions"]).max(),
+                           np.abs(gm["element_positions"] - om["element_positions"]).max())),
+            "v": max(max_rel(gm["vertex_velocities"], om["vertex_velocities"]),
+                     max_rel(gm["element_velocities"], om["element_velocities"])),
+            "d": float(np.abs(gm["element_directions"] - om["element_directions"]).max()),
+            "B": float(max(np.abs(gm["vertex_affine_momenta"] - om["vertex_affine_momenta"]).max(),
+                           np.abs(gm["element_affine_momenta"] - om["element_affine_momenta"]).max()) / vs)}
+
+
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_first_step_grid_matches_oracle_at_full_size(name):
+    sc = CONFIGS[name]()
+    assert sc.num_items() == SIZES[name]
+    for stage in (capi.AEP_STAGE_P2G, capi.AEP_STAGE_GRID):
+        gpu, orc = _pair(sc)
+        gpu.step_stage(sc.dt, stage)
+        orc.init(volumes=False)
+        if stage != capi.AEP_STAGE_P2G:
+            orc.step(sc.dt, stage=stage)
+        g, o = gpu.get_grid(), orc.get_grid()
+        gpu.close()
+        orc.close()
+        dm = max_rel(g["masses"], o["masses"])
+        dv = mass_weighted_rel(g["velocities"], o["velocities"], o["masses"])
+        msg = f"{name} stage {stage}: mass {dm:.3g}, velocity {dv:.3g}"
+        if stage == capi.AEP_STAGE_GRID:
+            dvb = mass_weighted_rel(g["velocities_before_friction"], o["velocities_before_friction"], o["masses"])
+            msg += f", before friction {dvb:.3g}"
+            assert dvb < 1e-4, msg
+        print(msg)
+        assert dm < 2e-6, msg
+        assert dv < (2e-5 if stage == capi.AEP_STAGE_P2G else 1e-4), msg
+
+
+@pytest.mark.parametrize("name", sorted(CONFIGS))
+def test_one_and_ten_steps_match_oracle_at_full_size(name):
+    sc = CONFIGS[name]()
+    gpu, orc = _pair(sc)
+    gpu.init_volumes()
+    orc.init(volumes=True)
+    h = float(sc.grid.h.min())
+    for k in range(1, 11):
+        gpu.step(sc.dt)
+        orc.step(sc.dt)
+        if k not in (1, 10):
+            continue
+        # bounds: (x, v, F, B, q) of the parity suite after 1 and after 10 steps
+        tol = {"x": 5e-7, "v": 1e-4, "F": 2e-6, "B": 1e-3, "q": 2e-6} if k == 1 else \
+            {"x": 1e-6, "v": 2e-4, "F": 1e-5, "B": 2e-3, "q": 1e-5}
+        if sc.particles is not None:
+            e = _particle_errors(gpu.get_particles(), orc.get_particles(), h)
+            print(f"{name} step {k} particles: " + ", ".join(f"{a} {b:.3g}" for a, b in e.items()))
+            for key, bound in tol.items():
+                assert e[key] < bound, (name, k, key, e)
+        if sc.mesh is not None:
+            e = _mesh_errors(gpu.get_mesh(), orc.get_mesh())
+            print(f"{name} step {k} cloth: " + ", ".join(f"{a} {b:.3g}" for a, b in e.items()))
+            mtol = {"x": 5e-7, "v": 2e-4, "d": 5e-6, "B": 2e-3} if k == 1 else \
+                {"x": 2e-6, "v": 1e-3, "d": 2e-5, "B": 5e-3}
+            for key, bound in mtol.items():
+                assert e[key] < bound, (name, k, key, e)
+    assert gpu.stats()["overflow"] == 0
+    gpu.close()
+    orc.close()

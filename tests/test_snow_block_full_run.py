@@ -39,3 +39,56 @@ def test_snow_block_200_steps_match_oracle():
     z0 = float(np.mean(sc.particles.positions[:, 2]))
     fall = 1.0 * sc.dt * n + 9.8 * sc.dt * sc.dt * n * (n + 1) / 2
     assert abs((z0 - float(np.mean(g["positions"][:, 2]))) - fall) < 1e-4 * fall
+
+
+def _moments(p, m):
+    """Total momentum and centre of mass of a particle state."""
+    return (m[:, None] * p["velocities"]).sum(axis=0), (m[:, None] * p["positions"]).sum(axis=0) / m.sum()
+
+
+def test_snow_block_through_ground_impact_matches_oracle():
+    """The same drop run on to 2,300 steps: the block reaches the ground after about
+    1,750 steps, so the last ~550 steps exercise the collision with friction, the
+    snow clamp and its hardening (J_P departs from 1).  Every 10 steps the total
+    mass (exact on the GPU), the total momentum and the centre of mass are
+    compared with the oracle's; the final state is compared at the end."""
+    sc = scenes.snow_block()
+    gpu, orc = make_pair(sc)
+    gpu.init_volumes()
+    orc.init(volumes=True)
+    m = sc.particles.masses
+    mass0 = None
+    worst = {"momentum": 0.0, "com": 0.0}
+    steps = 2300
+    for k in range(1, steps + 1):
+        gpu.step(sc.dt)
+        orc.step(sc.dt)
+        if k % 10:
+            continue
+        st = gpu.stats()
+        mass0 = st["total_mass"] if mass0 is None else mass0
+        assert st["total_mass"] == mass0 and st["overflow"] == 0  # fixed point: exactly conserved
+        g, o = gpu.get_particles(), orc.get_particles()
+        pg, cg = _moments(g, m)
+        po, co = _moments(o, m)
+        worst["momentum"] = max(worst["momentum"], float(np.abs(pg - po).max() / np.abs(po).max()))
+        worst["com"] = max(worst["com"], float(np.abs(cg - co).max()))
+    assert abs(mass0 - m.sum()) < 1e-6 * m.sum()
+    g, o = gpu.get_particles(), orc.get_particles()
+    gpu.close()
+    dx = np.abs(g["positions"] - o["positions"]).max()
+    dv = max_rel(g["velocities"], o["velocities"])
+    dF = np.abs(g["elastic_deformation_gradients"] - o["elastic_deformation_gradients"]).max()
+    dq = np.abs(g["plastic"] - o["plastic"]).max()
+    jp = o["plastic"]
+    print(f"{steps} steps: |dx| {dx:.3g}, |dv|/|v| {dv:.3g}, |dF| {dF:.3g}, |dJp| {dq:.3g}; "
+          f"J_P in [{jp.min():.4f}, {jp.max():.4f}]; worst momentum {worst['momentum']:.3g}, "
+          f"worst centre of mass {worst['com']:.3g}")
+    assert jp.min() < 0.999 or jp.max() > 1.001  # the clamp and hardening did act
+    assert float(np.min(o["positions"][:, 2])) < 0.06  # the block is on the ground
+    assert worst["momentum"] < 1e-3
+    assert worst["com"] < 1e-5
+    assert dx < 1e-4
+    assert dv < 5e-2
+    assert dF < 1e-3
+    assert dq < 1e-3

@@ -156,3 +156,40 @@ def test_weights_match_oracle_rows():
         assert np.abs(w[r][keep] - ow).max() < 1e-6
         assert np.abs(g[r][keep] - og).max() < 1e-6 * 32 * 4
         assert abs(w[r].sum() - 1.0) < 1e-5
+
+
+def test_host_round_trip_of_particles_and_mesh_state_is_exact():
+    """The end-to-end form of a step (the caller's arrays are the state: upload,
+    step, read back) equals stepping on the device: re-uploading the same number of
+    particles keeps the attached mesh and the device order, and aep_set_mesh_state
+    writes the mesh members aep_get_mesh reads."""
+    from .test_cloth_gpu import small_cloth
+
+    grid, ps, mesh, ls, prm = small_cloth(True, seed=6)
+    runs = []
+    for round_trip in (False, True):
+        s = HybridSolver(None, grid, prm)
+        s.set_particle_system(ps)
+        s.set_lagrangian_mesh(mesh)
+        s.set_level_set(ls)
+        s.init_volumes()
+        for k in range(6):
+            s.step(2e-5)
+            if round_trip and k % 2 == 0:
+                p = s.get_particles()
+                lib, h, n = s._lib, s._h, len(ps)
+                from anisotropicelastoplasticity_gb300.solver import mats_to_ref, rows_to_ref, vec_to_ref
+
+                arrs = [vec_to_ref(p["positions"]), vec_to_ref(p["velocities"]), rows_to_ref(p["affine_momenta"]),
+                        mats_to_ref(p["elastic_deformation_gradients"]), None, np.ascontiguousarray(ps.masses),
+                        p["volumes"], p["plastic"]]
+                mat = np.ascontiguousarray(ps.material, np.uint8)
+                dp = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+                assert lib.aep_set_particles(h, n, *[dp(a) for a in arrs],
+                                             mat.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))) == capi.AEP_OK
+                s.set_mesh_state(s.get_mesh())
+        runs.append((s.get_particles(), s.get_mesh()))
+    for k in runs[0][0]:
+        assert np.array_equal(runs[0][0][k], runs[1][0][k]), k
+    for k in runs[0][1]:
+        assert np.array_equal(runs[0][1][k], runs[1][1][k]), k
