@@ -959,47 +959,50 @@ __device__ __forceinline__ void return_map(const KParams& P, int mat, T s[3], T&
 // s = 1 (the sand apex, s_new = 1, turns them into stress); this form keeps them.
 // J_P (snow) is scaled by prod(s / s_new); sig = expm1(ln s - ln s_new) gives
 // F_P <- F_P + V diag(sig) V^T F_P (HS:676).  T = double runs the whole mapping in
-// FP64 from the same FP32 inputs.  Returns 0 elastic, 1 sand apex, 2 projected
-// (snow clamp, sand cone), -1 when the stretch is too large for this form (the
-// caller takes the SVD form); ln_tr / ln_new return the log singular values.
+// FP64 from the same FP32 inputs.  Three parts: the trial state (ln s, V; false when
+// the stretch is too large for this form), the projection (0 elastic, 1 sand apex,
+// 2 snow clamp / sand cone), and F_E from the projected ln s.
 template <typename T>
-__device__ __forceinline__ int stretch_return_map(const KParams& P, int mat, const float F[9], const float D[9],
-                                                  float& q, float Fe[9], float Vo[9], float sig[3], float ln_tr[3],
-                                                  float ln_new[3]) {
+__device__ __forceinline__ bool stretch_trial(const float F[9], const float D[9], T ln[3], T V[9]) {
     T e[6];
     trial_stretch(F, D, e);
     const T n2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + T(2) * (e[3] * e[3] + e[4] * e[4] + e[5] * e[5]);
-    if (!(n2 < T(0.25))) return -1;
-    T lam[3], V[9];
+    if (!(n2 < T(0.25))) return false;
+    T lam[3];
     sym_eig3<T>(e[0], e[1], e[2], e[3], e[4], e[5], lam, V, 10, sizeof(T) == 4 ? T(0x1p-25) : T(0x1p-54));
-    T ln[3], lnn[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) lnn[a] = ln[a] = T(0.5) * log1p_t(lam[a]);
-    int kind = 0;
-    T qq = q;
+    for (int a = 0; a < 3; ++a) ln[a] = T(0.5) * log1p_t(lam[a]);
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ int stretch_project(const KParams& P, int mat, const T ln[3], T lnn[3], T& q) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) lnn[a] = ln[a];
     if (mat == kSnow) {
         const T lo = log_t(T(P.snow_lo)), hi = log_t(T(P.snow_hi));
+        int kind = 0;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const T c = fmin(fmax(ln[a], lo), hi);
             if (c != ln[a]) kind = 2;
             lnn[a] = c;
         }
-    } else {
-        kind = dp_project<T>(lnn, qq, T(P.sand_h0), T(P.sand_h1), T(P.sand_h2), T(P.sand_h3), T(P.sand_k));
+        return kind;
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        ln_tr[a] = (float)ln[a];
-        ln_new[a] = (float)lnn[a];
-    }
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Vo[k] = (float)V[k];
-    if (kind == 0) {
+    return dp_project<T>(lnn, q, T(P.sand_h0), T(P.sand_h1), T(P.sand_h2), T(P.sand_h3), T(P.sand_k));
+}
+
+// F_E, the plastic scalar and sig from the trial and projected log singular values
+template <typename T>
+__device__ __forceinline__ void stretch_finish(int mat, const float F[9], const float D[9], const T V[9],
+                                               const T ln[3], const T lnn[3], bool plastic, T q_new, float& q,
+                                               float Fe[9], float sig[3]) {
+    if (!plastic) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fe[k] = F[k] + D[k];
         sig[0] = sig[1] = sig[2] = 0.0f;
-        return 0;
+        return;
     }
     T rho[3];
 #pragma unroll
@@ -1026,8 +1029,52 @@ __device__ __forceinline__ int stretch_return_map(const KParams& P, int mat, con
         }
     }
     if (mat == kSnow) q = (float)(T(q) * exp_t((ln[0] - lnn[0]) + (ln[1] - lnn[1]) + (ln[2] - lnn[2])));
-    else q = (float)qq;
+    else q = (float)q_new;
+}
+
+// The whole mapping; returns the projection's kind, or -1 when the stretch is too
+// large for this form (the caller takes the SVD form); ln_tr / ln_new return the
+// log singular values, Vo the right singular vectors.
+template <typename T>
+__device__ __forceinline__ int stretch_return_map(const KParams& P, int mat, const float F[9], const float D[9],
+                                                  float& q, float Fe[9], float Vo[9], float sig[3], float ln_tr[3],
+                                                  float ln_new[3]) {
+    T ln[3], lnn[3], V[9];
+    if (!stretch_trial<T>(F, D, ln, V)) return -1;
+    T qq = q;
+    const int kind = stretch_project<T>(P, mat, ln, lnn, qq);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        ln_tr[a] = (float)ln[a];
+        ln_new[a] = (float)lnn[a];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Vo[k] = (float)V[k];
+    stretch_finish<T>(mat, F, D, V, ln, lnn, kind != 0, qq, q, Fe, sig);
     return kind;
+}
+
+// Drucker-Prager cone coefficient k alpha(q) of the yield function
+// |dev ln s| + k alpha tr ln s (HybridSolver.cpp:641-653)
+__device__ __forceinline__ float dp_k_alpha(const KParams& P, float q) {
+    const float phi = (P.sand_h0 + (P.sand_h1 * q - P.sand_h3) * expf(-P.sand_h2 * q)) * (3.14159265358979f / 180.0f);
+    const float sphi = sinf(phi);
+    return P.sand_k * 0.81649658092772603f * 2.0f * sphi / (3.0f - sphi);
+}
+
+// Trial yield check of the learned path (HybridSolver.cpp:626-663), without the
+// projection: 0 elastic, 1 sand apex (a constant projection), 2 plastic (the snow
+// clamp or the sand cone, which the network predicts).
+__device__ __forceinline__ int trial_kind(const KParams& P, int mat, const float ln[3], float q) {
+    if (mat == kSnow) {
+        const float lo = logf(P.snow_lo), hi = logf(P.snow_hi);
+        return (ln[0] < lo || ln[0] > hi || ln[1] < lo || ln[1] > hi || ln[2] < lo || ln[2] > hi) ? 2 : 0;
+    }
+    const float tr = ln[0] + ln[1] + ln[2];
+    const float d0 = ln[0] - tr / 3.0f, d1 = ln[1] - tr / 3.0f, d2 = ln[2] - tr / 3.0f;
+    const float nd = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+    if (nd + dp_k_alpha(P, q) * tr <= 0.0f) return 0;
+    return (nd == 0.0f || tr > 0.0f) ? 1 : 2;
 }
 
 // A sand trial state within reach of the apex of the Drucker-Prager cone: projected
@@ -1143,9 +1190,10 @@ __device__ __forceinline__ void harvest_record(const KParams& P, const Harvest& 
 }
 
 // G2P + APIC + advection + F update + return mapping, one thread per particle.
-// kDefer (the learned return map): a plastic snow or sand state whose projection
-// is not a constant is queued with its SVD and exact projection for k_mlp_finish,
-// which writes its F_E, F_P and plastic scalar; the sand apex is taken exactly.
+// kDefer (the learned return map): the trial state's yield check runs here; a
+// plastic snow or sand state whose projection is not a constant is queued (trial
+// ln s, q, F, D, V) for k_mlp_finish, which writes its F_E, F_P and plastic scalar;
+// elastic states and the sand apex are mapped exactly here.
 template <bool kDefer>
 __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
                                              int n, GArrays G, float dt, uint32_t* __restrict__ keys_next,
@@ -1277,6 +1325,49 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
             if (g.thread_rank() == 0) atomicAdd(&st->fp64_apex, (unsigned long long)g.size());
         }
         if (skind > 0 && H.buf && (j % H.stride) == 0) harvest_record(P, H, mat, lt, lnw, q_old);
+    } else {
+        // the learned return map: the trial state and its yield check here; a plastic
+        // state with a projection the network predicts is queued for k_mlp_finish
+        // (trial ln s, q, F, D, V), everything else is mapped exactly in place
+        float ln[3];
+        if (stretch_trial<float>(F, D, ln, V)) {
+            const int tk = trial_kind(P, mat, ln, q);
+            if (tk == 2) {
+                cg::coalesced_group g = cg::coalesced_threads();  // warp-aggregated queue append
+                unsigned qbase = 0;
+                if (g.thread_rank() == 0) qbase = atomicAdd(&st->mlp_rows, g.size());
+                const int r = (int)(g.shfl(qbase, 0) + g.thread_rank());
+                if (r < Qu.cap) {
+                    deferred = true;
+                    const long cap = Qu.cap;
+                    float* f = Qu.f + r;
+                    Qu.j[r] = j;
+                    Qu.pj[r] = pj;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) f[(kQLn + a) * cap] = ln[a];
+                    f[kQQ * cap] = q;
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) {
+                        f[(kQF + k) * cap] = F[k];
+                        f[(kQD + k) * cap] = D[k];
+                        f[(kQV + k) * cap] = V[k];
+                    }
+                }
+            }
+            if (!deferred) {
+                float lnn[3], qq = q;
+                const int kind = stretch_project<float>(P, mat, ln, lnn, qq);
+                stretch_finish<float>(mat, F, D, V, ln, lnn, kind != 0, qq, q, Fe, sig);
+                if (kind == 1) {
+                    cg::coalesced_group g = cg::coalesced_threads();  // the apex: exact, counted
+                    if (g.thread_rank() == 0) atomicAdd(&st->learned_exact, (unsigned long long)g.size());
+                }
+            }
+            skind = 0;  // handled: no SVD form below
+        } else {
+            cg::coalesced_group g = cg::coalesced_threads();  // beyond the stretch form: exact SVD form
+            if (g.thread_rank() == 0) atomicAdd(&st->learned_exact, (unsigned long long)g.size());
+        }
     }
     bool ok = skind >= 0 || svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
     if (skind >= 0) {
@@ -1287,39 +1378,6 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         if (H.buf && (j % H.stride) == 0 && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2])) {
             const float lt[3] = {logf(s[0]), logf(s[1]), logf(s[2])}, lnw[3] = {logf(sn[0]), logf(sn[1]), logf(sn[2])};
             harvest_record(P, H, mat, lt, lnw, q_old);  // plastic states only
-        }
-        if (kDefer && (sn[0] != s[0] || sn[1] != s[1] || sn[2] != s[2])) {
-            if (mat == kSand && sn[0] == 1.0f && sn[1] == 1.0f && sn[2] == 1.0f) {
-                cg::coalesced_group g = cg::coalesced_threads();  // the apex: exact, counted
-                if (g.thread_rank() == 0) atomicAdd(&st->learned_exact, (unsigned long long)g.size());
-            } else {
-                cg::coalesced_group g = cg::coalesced_threads();  // warp-aggregated queue append
-                unsigned base = 0;
-                if (g.thread_rank() == 0) base = atomicAdd(&st->mlp_rows, g.size());
-                const int r = (int)(g.shfl(base, 0) + g.thread_rank());
-                if (r < Qu.cap) {
-                    deferred = true;
-                    const long cap = Qu.cap;
-                    float* f = Qu.f + r;
-                    Qu.j[r] = j;
-                    Qu.pj[r] = pj;
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) {
-                        f[(kQU + k) * cap] = U[k];
-                        f[(kQV + k) * cap] = V[k];
-                    }
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        f[(kQS + a) * cap] = s[a];
-                        f[(kQSx + a) * cap] = sn[a];
-                    }
-                    f[kQQ * cap] = q_old;
-                    f[kQQx * cap] = q;
-                    if (P.track_fp)
-#pragma unroll
-                        for (int k = 0; k < 9; ++k) f[(kQFtr + k) * cap] = Ftr[k];
-                }
-            }
         }
         if (!deferred) {
             sprod = (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]);
@@ -1420,51 +1478,57 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
     if (clamped) atomicAdd(&st->out_of_domain, 1ull);
 }
 
-// F_E = U diag(sn) V^T into the new order, the plastic scalar and (with
-// track_plastic_F) F_P = V diag(1/sn) U^T F_tr F_P (HybridSolver.cpp:675-677);
-// sprod = prod(s_trial / sn) updates J_P of snow without F_P.
-__device__ __forceinline__ void finish_return_map(const KParams& P, const PArrays& nxt, const PArrays& cur, int j,
-                                                  int pj, int mat, const float Ftr[9], const float U[9],
-                                                  const float V[9], const float s[3], const float sn[3], float q,
-                                                  float sprod) {
-    float US[9], Fe[9];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) US[3 * r + c] = U[3 * r + c] * sn[c];
-    mat_mul_bt(US, V, Fe);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) nxt.F[k][j] = Fe[k];
-    if (P.track_fp) {
-        float Fp[9], Ft[9], VS[9], M[9], Fpn[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
-        mat_mul(Ftr, Fp, Ft);
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) VS[3 * r + c] = V[3 * r + c] / sn[c];
-        mat_mul_bt(VS, U, M);
-        mat_mul(M, Ft, Fpn);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) nxt.Fp[k][j] = Fpn[k];
-        if (mat == kSnow) q = mat_det(Fpn);
-    } else if (mat == kSnow) {
-        q *= sprod;  // J_P = det F_P = det(F_tr) det(F_P) / det(S_new)
-    }
-    nxt.plastic[j] = q;
-}
-
 // ===================================================================================
 // The learned return map of the rows that k_g2p<true> queued: one warp per 32
 // consecutive rows runs the MLP (aep_mlp.cuh) on the tensor cores on the sorted
-// trial log singular values, and each prediction is checked against the exact
-// projection that the G2P pass computed (the point of the yield surface that the
-// flow rule reaches, HybridSolver.cpp:626-674): within max(tol_rel x its largest
-// magnitude, tol_abs) it is kept, otherwise the exact value is used and counted
-// as a fallback.  Then F_E = U diag(s_new) V^T, F_P and the plastic scalar into the
-// new order.  Persistent: the weights are loaded once per block.
+// trial log singular values, and each prediction is checked against the optimality
+// conditions of the projection it stands for (HybridSolver.cpp:626-674), with the
+// residuals in ln-strain units and accepted within max(tol_rel |ln s_trial|, tol_abs):
+//   sand (the cone; the apex never reaches the network): the yield condition at the
+//     prediction, |dev| + k alpha(q) tr = 0, and the flow rule: the trace kept and the
+//     deviatoric part a shrunk copy of the trial's (0 <= c <= 1);
+//   snow (the clamp of each log singular value to [ln(1 - theta_c), ln(1 + theta_s)]):
+//     every predicted value inside the bounds, equal to its trial value where that is
+//     inside and to the bound it crossed where it is outside.
+// A rejected prediction is replaced by the exact projection (learned_fallbacks).
+// F_E, F_P and the plastic scalar follow in the stretch form.  Persistent: the
+// weights are loaded once per block.
 constexpr int kFinThreads = 128;
+
+// The residual of a predicted projection (ln units); q_new: the plastic scalar it implies
+__device__ __forceinline__ float learned_residual(const KParams& P, int mat, const float ln[3], const float pred[3],
+                                                  float q, float& q_new) {
+    q_new = q;
+    if (mat == kSnow) {
+        const float lo = logf(P.snow_lo), hi = logf(P.snow_hi);
+        float r = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float target = ln[a] < lo ? lo : (ln[a] > hi ? hi : ln[a]);
+            r = fmaxf(r, fabsf(pred[a] - target));
+        }
+        return r;
+    }
+    const float tr = ln[0] + ln[1] + ln[2], trp = pred[0] + pred[1] + pred[2];
+    float dev[3], devp[3], nd = 0.0f, ndp = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        dev[a] = ln[a] - tr / 3.0f;
+        devp[a] = pred[a] - trp / 3.0f;
+        nd += dev[a] * dev[a];
+        ndp += devp[a] * devp[a];
+    }
+    nd = sqrtf(nd);
+    ndp = sqrtf(ndp);
+    const float c = nd > 0.0f ? ndp / nd : 0.0f;
+    float r = fabsf(ndp + dp_k_alpha(P, q) * trp);  // yield condition at the prediction
+    r = fmaxf(r, fabsf(trp - tr));                   // flow rule: the trace is kept,
+#pragma unroll
+    for (int a = 0; a < 3; ++a) r = fmaxf(r, fabsf(devp[a] - c * dev[a]));  // dev shrinks radially
+    if (c > 1.0f) r = fmaxf(r, (c - 1.0f) * nd);
+    q_new = q + (nd - ndp);  // the plastic amount grows by the projection distance dg
+    return r;
+}
 
 __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays cur, PArrays nxt, MlpQueue Qu,
                                                             DevStats* st, MlpParams mlp, float tol_rel,
@@ -1492,53 +1556,60 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
         const float* f = Qu.f + rr;
         const int pj = Qu.pj[rr];
         const int mat = (int)cur.mat[pj];
-        float s[3], lns[3], srt[3];
+        float ln[3], srt[3];
         int pm[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            s[a] = f[(kQS + a) * cap];
-            lns[a] = logf(s[a]);
-        }
-        sort3_desc(lns, srt, pm);
+        for (int a = 0; a < 3; ++a) ln[a] = f[(kQLn + a) * cap];
+        sort3_desc(ln, srt, pm);
         float q = f[kQQ * cap];
         const float osc = mlp_features(srt, q, mat, X + lane * kStrideIn);
         mlp_forward_warp(W, X, H0, H1, Y, lane);
         if (live) {
-            float pred_ln[3], ex[3];
+            float pred[3];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) pred_ln[pm[k]] = srt[k] + Y[lane * kMlpOut + k] / osc;
-            float err = 0.0f, ref = 0.0f;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                ex[a] = f[(kQSx + a) * cap];
-                const float le = logf(ex[a]);
-                err = fmaxf(err, fabsf(pred_ln[a] - le));
-                ref = fmaxf(ref, fabsf(le));
-            }
-            const float qe = f[kQQx * cap];
-            float sn[3];
-            if (err <= fmaxf(tol_rel * ref, tol_abs)) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a) sn[a] = expf(pred_ln[a]);
-                if (mat == kSand && qe != q) {  // q grows by the projection distance
-                    const float d0 = pred_ln[0] - lns[0], d1 = pred_ln[1] - lns[1], d2 = pred_ln[2] - lns[2];
-                    q += sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-                }
+            for (int k = 0; k < 3; ++k) pred[pm[k]] = srt[k] + Y[lane * kMlpOut + k] / osc;
+            float q_new;
+            const float res = learned_residual(P, mat, ln, pred, q, q_new);
+            const float lnorm = sqrtf(ln[0] * ln[0] + ln[1] * ln[1] + ln[2] * ln[2]);
+            float lnn[3];
+            if (res <= fmaxf(tol_rel * lnorm, tol_abs)) {
+                lnn[0] = pred[0]; lnn[1] = pred[1]; lnn[2] = pred[2];
                 ++n_ok;
-            } else {
-                sn[0] = ex[0]; sn[1] = ex[1]; sn[2] = ex[2];
-                q = qe;
+            } else {  // the exact projection
+                q_new = q;
+                stretch_project<float>(P, mat, ln, lnn, q_new);
                 ++n_rej;
             }
-            float U[9], V[9], Ftr[9];
+            float F[9], D[9], V[9], Fe[9], sig[3];
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                U[k] = f[(kQU + k) * cap];
+                F[k] = f[(kQF + k) * cap];
+                D[k] = f[(kQD + k) * cap];
                 V[k] = f[(kQV + k) * cap];
-                Ftr[k] = P.track_fp ? f[(kQFtr + k) * cap] : 0.0f;
             }
-            finish_return_map(P, nxt, cur, Qu.j[r], pj, mat, Ftr, U, V, s, sn, q,
-                              (s[0] / sn[0]) * (s[1] / sn[1]) * (s[2] / sn[2]));
+            stretch_finish<float>(mat, F, D, V, ln, lnn, true, q_new, q, Fe, sig);
+            const int j = Qu.j[r];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) nxt.F[k][j] = Fe[k];
+            if (P.track_fp) {  // F_P <- F_P + V diag(sig) V^T F_P (HS:676)
+                float Fp[9], Wm[9], Fpn[9];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b)
+                        Wm[3 * a + b] = V[3 * a] * sig[0] * V[3 * b] + V[3 * a + 1] * sig[1] * V[3 * b + 1] +
+                                        V[3 * a + 2] * sig[2] * V[3 * b + 2];
+                mat_mul(Wm, Fp, Fpn);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    Fpn[k] += Fp[k];
+                    nxt.Fp[k][j] = Fpn[k];
+                }
+                if (mat == kSnow) q = mat_det(Fpn);
+            }
+            nxt.plastic[j] = q;
         }
     }
     n_ok = __reduce_add_sync(0xffffffffu, n_ok);
@@ -1555,11 +1626,12 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
 // velocities (HS:749-756), position = centroid of the new vertex positions
 // (LagrangianMesh.cpp:371-380), directions d1, d2 from the vertices and
 // d3 += dt grad v^bf d3 (HS:584-607), then the QR return mapping (HS:686-720).
-// With an MLP (use_mlp), the cloth return mapping of plastic elements is predicted
-// by the learned map (cloth rows of the same network) and checked against the
-// exact projection as in k_mlp_finish; the warp runs the network when any of its
-// elements is plastic.  With a harvest buffer, plastic elements record
-// [r13, r23, r33 - 1, 0, 2, projected - trial (3)].
+// With an MLP (use_mlp), the cloth return mapping of plastic elements (shear beyond
+// the frictional cap) is predicted by the learned map (cloth rows of the same
+// network) and checked against the cap's optimality conditions, the exact
+// projection replacing a rejected prediction; the warp runs the network when any
+// of its elements is plastic.  With a harvest buffer (plain steps), plastic
+// elements record [r13, r23, r33 - 1, cap ratio, 2, projected - trial (3)].
 __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArrays nxt, GArrays G, MeshArrays M,
                                                    float dt, uint32_t* __restrict__ keys_next, DevStats* st,
                                                    Harvest H, MlpParams mlp, int use_mlp, float tol_rel,
@@ -1621,16 +1693,16 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
         gram_schmidt(D, Q, R);
         r[0] = R[2]; r[1] = R[5]; r[2] = R[8];
         rp[0] = r[0]; rp[1] = r[1]; rp[2] = r[2];
-        cloth_project(rp, M.shear, M.stiffness, M.friction);
-        plastic = rp[0] != r[0] || rp[1] != r[1] || rp[2] != r[2];
-        if (plastic && r[2] > 1.0f) {  // tension: the constant r = e3, taken exactly
-            plastic = false;
-            tension = true;
-        }
+        // the trial yield check (HybridSolver.cpp:701-716): tension (r33 > 1, the
+        // constant r = e3) or a shear beyond the frictional cap (plastic)
+        tension = r[2] > 1.0f;
         cap = cloth_cap_ratio(r, M.shear, M.stiffness, M.friction);
+        plastic = !tension && cap < 1.0f;
+        // the exact projection, unless the learned map predicts this row
+        if (!(use_mlp && plastic)) cloth_project(rp, M.shear, M.stiffness, M.friction);
         // records of states within 1e-5 of r = e3 would carry the FP32 rounding of
         // r33 as more than 1e-2 of their size: skipped
-        if (H.buf && plastic && (e % H.stride) == 0 &&
+        if (H.buf && !use_mlp && plastic && (e % H.stride) == 0 &&
             fmaxf(fmaxf(fabsf(r[0]), fabsf(r[1])), fabsf(r[2] - 1.0f)) >= 1e-5f) {
             const unsigned long long slot = atomicAdd(H.count, 1ull);
             if ((long long)slot < H.capacity) {
@@ -1675,18 +1747,24 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
             const float sc = mlp_features(in, cap, plastic ? kMlpCloth : 0, MX + lane * kStrideIn);
             mlp_forward_warp(W, MX, MH0, MH1, MY, lane);
             if (plastic) {
-                // residual relative to the projected shear and normal strain
-                // (r13, r23, r33 - 1), whose size sets the cloth stresses
-                float pred[3], err = 0.0f;
+                // optimality conditions of the frictional cap: r33 kept, the shear
+                // (r13, r23) a shrunk copy of the trial's, its length on the cap
+                // friction * stiffness (r33 - 1)^2 / shear; residuals in r units,
+                // relative to the trial's (r13, r23, r33 - 1)
+                float pred[3];
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    pred[a] = r[a] + MY[lane * kMlpOut + a] / sc;
-                    err = fmaxf(err, fabsf(pred[a] - rp[a]));
-                }
-                const float ref = fmaxf(fmaxf(fabsf(rp[0]), fabsf(rp[1])), fabsf(rp[2] - 1.0f));
-                ok = err <= fmaxf(tol_rel * ref, tol_abs);
+                for (int a = 0; a < 3; ++a) pred[a] = r[a] + MY[lane * kMlpOut + a] / sc;
+                const float ns = sqrtf(r[0] * r[0] + r[1] * r[1]), nsp = sqrtf(pred[0] * pred[0] + pred[1] * pred[1]);
+                const float c = ns > 0.0f ? nsp / ns : 0.0f;
+                const float on_cap = M.friction * M.stiffness * (r[2] - 1.0f) * (r[2] - 1.0f) / M.shear;
+                float res = fmaxf(fabsf(pred[2] - r[2]), fabsf(nsp - on_cap));
+                res = fmaxf(res, fmaxf(fabsf(pred[0] - c * r[0]), fabsf(pred[1] - c * r[1])));
+                const float ref = sqrtf(ns * ns + (r[2] - 1.0f) * (r[2] - 1.0f));
+                ok = res <= fmaxf(tol_rel * ref, tol_abs);
                 if (ok) {
                     rp[0] = pred[0]; rp[1] = pred[1]; rp[2] = pred[2];
+                } else {
+                    cloth_project(rp, M.shear, M.stiffness, M.friction);  // the exact projection
                 }
             }
         }

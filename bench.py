@@ -39,11 +39,13 @@ METRIC = "particle-steps/s, learned vs plain return map, 1 GB300, at <=1e-3 stre
 UNIT = "particle-steps/s"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
-# acceptance bounds of the learned return map's in-kernel check, (relative, absolute
-# in ln-strain units): "strict" keeps a prediction within 1e-3 of the exact
-# projection's magnitude (or within the FP32 resolution of ln s, 2^-23); "residual"
-# keeps it within 1e-4 of the exact projection
-LEARNED_BOUNDS = {"strict": (1e-3, 2.0 ** -23), "residual_1e-4": (0.0, 1e-4)}
+# acceptance bounds of the learned return map's in-kernel check (the residuals of
+# the projection's yield condition and flow rule, ln-strain units), as (relative to
+# |ln s_trial|, absolute): "strict" accepts residuals within 1e-4 of the trial
+# strain (or the FP32 resolution of ln s, 2^-23), which keeps an accepted state's
+# stress within ~1e-3; "residual_1e-4" accepts an absolute residual of 1e-4, the
+# bound the learned-map configuration states
+LEARNED_BOUNDS = {"strict": (1e-4, 2.0 ** -23), "residual_1e-4": (0.0, 1e-4)}
 
 
 def algorithmic_bytes(kernel: str, counts: dict) -> float:
@@ -292,14 +294,42 @@ def train_mlp(args, torch):
     _, loss1 = mlp.gradient(recs.data_ptr(), n_rec)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
+    fit = fit_error(torch, mlp, recs)
     info = {"records": n_rec, "records_per_source": {k: len(v) for k, v in parts.items()},
             "sources": "snow_block steps 1700-2300 (ground impact) + sand_column 500 steps (stride 8) + cloth_drape "
                        "(128x128 sheet) 400 steps + snow_sand_collision (262,144 particles, 128^3, seed 5) 100 steps "
                        "+ the same with +-1% strain (seed 12) 5 steps; plastic states without the constant "
                        "projections (sand apex, cloth in tension)",
             "steps": args.train_steps, "batch": 8192, "loss_before": loss0, "loss_after": loss1,
-            "harvest_s": t1 - t0, "train_s": t2 - t1}
+            "harvest_s": t1 - t0, "train_s": t2 - t1, "fit_error": fit}
     return mlp, info
+
+
+def fit_error(torch, mlp, recs, count=262144):
+    """How close the trained network comes to the exact projections it was trained
+    on: per record max |d_pred - d| / |ln s_projected| (ln units), per material."""
+    n = min(count, len(recs))
+    idx = torch.randperm(len(recs), generator=torch.Generator().manual_seed(0))[:n].to(recs.device)
+    sub = recs[idx].contiguous()
+    out = torch.empty((n, 3), dtype=torch.float32, device=recs.device)
+    mlp.forward(sub.data_ptr(), n, out.data_ptr())
+    torch.cuda.synchronize()
+    r = sub.cpu().numpy().astype(np.float64)
+    d_pred = out.cpu().numpy().astype(np.float64)
+    # relative to the projected ln s (cloth: to the trial (r13, r23, r33 - 1), whose
+    # projection is ~0 for an element on its cap)
+    proj = r[:, 0:3] + r[:, 5:8]
+    cloth = r[:, 4] == 2
+    proj[cloth] = r[cloth, 0:3]
+    err = np.abs(d_pred - r[:, 5:8]).max(axis=1) / np.maximum(np.linalg.norm(proj, axis=1), 1e-12)
+    out_d = {}
+    for m, name in ((0, "snow"), (1, "sand"), (2, "cloth")):
+        e = err[r[:, 4] == m]
+        if len(e):
+            out_d[name] = {"records": int(len(e)), "median": float(np.median(e)), "p90": float(np.percentile(e, 90)),
+                           "p99": float(np.percentile(e, 99)), "within_1e-4": float((e < 1e-4).mean()),
+                           "within_1e-3": float((e < 1e-3).mean())}
+    return out_d
 
 
 def with_fp64_apex(prm):

@@ -419,18 +419,24 @@ const char* aep_mlp_last_error(aep_mlp* m);
 aep_status aep_set_harvest(aep_solver* s, float* d_records, int64_t capacity, int32_t stride);
 /* Number of records written so far (capped at the capacity). */
 aep_status aep_get_harvest_count(aep_solver* s, int64_t* count);
-/* Use the learned return map in later steps (NULL: the exact mapping).  Every
- * prediction is checked in the kernel against the exact projection (the point of
- * the yield surface that the flow rule reaches); if the projected log singular
- * values (cloth: r13, r23, r33) differ from it by more than
- * max(tolerance x their largest magnitude, 2^-23), the exact value is used
+/* Use the learned return map in later steps (NULL: the exact mapping).  The G2P
+ * pass checks each trial state's yield condition; a plastic state whose projection
+ * is not a constant is predicted by the network, and the prediction is checked in
+ * the kernel against the optimality conditions of the projection it stands for:
+ * sand, the yield condition at the prediction (|dev ln s| + k alpha(q) tr ln s = 0)
+ * and the flow rule (trace kept, deviatoric part shrunk radially); snow, each value
+ * inside the clamp bounds, kept where the trial is inside and on the bound it
+ * crossed; cloth, r33 kept and the shear shrunk radially onto the frictional cap.
+ * A prediction whose largest residual (ln-strain units; cloth: QR units) exceeds
+ * max(tolerance x |trial|, 2^-23) is replaced by the exact projection
  * (aep_stats.learned_fallbacks).  Constant projections (sand apex, cloth in
  * tension) are taken exactly (aep_stats.learned_exact).  The handle must outlive
  * its use.                                                                     */
 aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance);
-/* The two bounds of that check: relative (rel_tol) and absolute (abs_tol, in
- * ln-strain units; 2^-23 after aep_set_return_map, the FP32 resolution of ln s
- * near s = 1).  A residual bound of 1e-4 is rel_tol = 0, abs_tol = 1e-4.       */
+/* The two bounds of that check: relative to the trial strain (rel_tol) and
+ * absolute (abs_tol, in ln-strain units; 2^-23 after aep_set_return_map, the FP32
+ * resolution of ln s near s = 1).  A residual bound of 1e-4 is rel_tol = 0,
+ * abs_tol = 1e-4.                                                               */
 aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_tol);
 
 /* ---- particle-to-grid without allocation --------------------------------------------- */

@@ -122,3 +122,15 @@ def loss_and_grad(p, rec, bf=True):
 def predict(p, rec, bf=True):
     """Predicted corrections d (ln units), [n, 3]."""
     return forward(p, rec, bf)["Y"][:, :3] / scales(rec)[:, None].astype(np.float64)
+
+
+def adam_step(p, g, m, v, t, lr, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam update in FP64 (the optimiser of aep_mlp_train, step t >= 1):
+    m <- b1 m + (1 - b1) g, v <- b2 v + (1 - b2) g^2,
+    p <- p - lr (m / (1 - b1^t)) / (sqrt(v / (1 - b2^t)) + eps).  Returns (p, m, v)."""
+    g = np.asarray(g, np.float64)
+    m = b1 * np.asarray(m, np.float64) + (1.0 - b1) * g
+    v = b2 * np.asarray(v, np.float64) + (1.0 - b2) * g * g
+    c1, c2 = 1.0 - b1 ** t, 1.0 - b2 ** t
+    p = np.asarray(p, np.float64) - lr * (m / c1) / (np.sqrt(v / c2) + eps)
+    return p, m, v

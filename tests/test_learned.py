@@ -84,7 +84,40 @@ def test_gpu_gradient_matches_oracle():
         else:
             got = gg[name]
         err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
-        assert err < 1e-2, (name, err)
+        print(f"{name}: relative gradient difference {err:.2e}")
+        # the two round to bfloat16 at the same points; an activation or gradient
+        # whose FP32 value lands on the other side of a rounding boundary (the
+        # accumulation orders differ) moves by 2^-9 of itself, which a few such
+        # entries per layer turn into ~1e-4 of the layer's gradient
+        assert err < 2e-3, (name, err)
+
+
+@pytest.mark.gpu
+def test_gpu_adam_steps_match_fp64_adam():
+    """Three Adam steps of aep_mlp_train (one batch = every record, so each step's
+    gradient is the one aep_mlp_gradient returns for the same parameters) against
+    FP64 Adam applied to those gradients: the parameters agree to FP32 rounding."""
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP
+
+    rec = random_records(2048, seed=12)
+    d = torch.from_numpy(rec).cuda()
+    m = ReturnMapMLP(seed=0)
+    m.set_params(random_params(13))
+    p = m.get_params().astype(np.float64)
+    mo_m, mo_v = np.zeros(NP), np.zeros(NP)
+    lr = 2e-3
+    for t in (1, 2, 3):
+        g, _ = m.gradient(d.data_ptr(), len(rec))
+        m.train(d.data_ptr(), len(rec), steps=1, batch=len(rec), lr=lr, lr_final=lr)
+        got = m.get_params().astype(np.float64)
+        p_want, mo_m, mo_v = mo.adam_step(p, g, mo_m, mo_v, t, lr)
+        err = np.abs(got - p_want)
+        # FP32 update arithmetic: a few units of FP32 spacing of the parameter, or
+        # 1e-5 of the step for parameters near zero
+        bound = 4 * np.spacing(np.abs(p_want).astype(np.float32)).astype(np.float64) + 1e-5 * lr
+        assert np.all(err <= bound), (t, float((err / bound).max()))
+        p = got
 
 
 @pytest.mark.gpu
