@@ -169,6 +169,8 @@ void fill_kparams(aep_solver* s) {
     k.snow_xi = (float)p.snow.xi;
     k.snow_lo = (float)(1.0 - p.snow.theta_c);
     k.snow_hi = (float)(1.0 + p.snow.theta_s);
+    k.snow_lnlo = (float)std::log((double)k.snow_lo);
+    k.snow_lnhi = (float)std::log((double)k.snow_hi);
     lame(p.sand.E, p.sand.nu, l, m);
     k.sand_mu = (float)m;
     k.sand_lambda = (float)l;

@@ -39,6 +39,7 @@ struct KParams {
     float mass_scale, inv_mass_scale;
     float mom_scale, inv_mom_scale;
     float snow_mu, snow_lambda, snow_xi, snow_lo, snow_hi;
+    float snow_lnlo, snow_lnhi;  // ln of the clamp bounds, rounded once from FP64
     float sand_mu, sand_lambda, sand_h0, sand_h1, sand_h2, sand_h3, sand_k;  // k = (3l+2m)/(2m)
     float gravity[3];
     float friction;
@@ -380,6 +381,10 @@ __device__ __forceinline__ float rot_div(float a, float b) { return __fdividef(a
 __device__ __forceinline__ double rot_div(double a, double b) { return a / b; }
 __device__ __forceinline__ float abs_t(float x) { return fabsf(x); }
 __device__ __forceinline__ double abs_t(double x) { return fabs(x); }
+// square root for the Jacobi rotation angle (argument >= 1): the angle only has to
+// be close, as for rot_div, so FP32 takes x rsqrt(x)
+__device__ __forceinline__ float rot_sqrt(float x) { return x * rsqrtf(x); }
+__device__ __forceinline__ double rot_sqrt(double x) { return sqrt(x); }
 
 // 3x3 SVD by one-sided (Hestenes) Jacobi rotations on the columns of A:
 // A V = U diag(s), s >= 0 (unsorted).  Every quantity the step needs from an
@@ -446,14 +451,14 @@ __device__ __forceinline__ double expm1_t(double x) { return expm1(x); }
 // One Jacobi rotation of a symmetric 3x3 matrix in the (p, q) plane, chosen to
 // zero a_pq (the t = tan(phi) form: a_pp -= t a_pq, a_qq += t a_pq), with r the
 // third index; V accumulates the rotations (columns p, q).  Skipped when a_pq
-// is already negligible against the diagonal pair.
+// is at most `thresh`.
 template <typename T>
-__device__ __forceinline__ bool jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& arq, T V[9], int p, int q, T tol) {
-    if (!(abs_t(apq) > tol * (abs_t(app) + abs_t(aqq)))) return false;
+__device__ __forceinline__ bool jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& arq, T V[9], int p, int q, T thresh) {
+    if (!(abs_t(apq) > thresh)) return false;
     const T zeta = rot_div(aqq - app, T(2) * apq);
     const T az = abs_t(zeta);
     const T t = az > T(1e15) ? rot_div(T(0.5), zeta)
-                             : rot_div(zeta >= T(0) ? T(1) : T(-1), az + sqrt_t(T(1) + zeta * zeta));
+                             : rot_div(zeta >= T(0) ? T(1) : T(-1), az + rot_sqrt(T(1) + zeta * zeta));
     const T c = rsqrt_t(T(1) + t * t), s = c * t;
     app -= t * apq;
     aqq += t * apq;
@@ -471,16 +476,20 @@ __device__ __forceinline__ bool jacobi_rot(T& app, T& aqq, T& apq, T& arp, T& ar
 }
 
 // Eigen-decomposition S = V diag(lam) V^T of the symmetric matrix
-// S = [[a00, a01, a02], [a01, a11, a12], [a02, a12, a22]] by cyclic Jacobi sweeps.
+// S = [[a00, a01, a02], [a01, a11, a12], [a02, a12, a22]] by cyclic Jacobi sweeps,
+// until every off-diagonal entry is at most tol |S|_F (rotations keep |S|_F): the
+// eigenvalues are then exact to ~tol |S|_F, all the step needs of them.
 template <typename T>
 __device__ __forceinline__ void sym_eig3(T a00, T a11, T a22, T a01, T a02, T a12, T lam[3], T V[9], int max_sweeps,
                                          T tol) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) V[k] = (k % 4 == 0) ? T(1) : T(0);
+    const T thresh =
+        tol * sqrt_t(a00 * a00 + a11 * a11 + a22 * a22 + T(2) * (a01 * a01 + a02 * a02 + a12 * a12));
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-        bool r = jacobi_rot<T>(a00, a11, a01, a02, a12, V, 0, 1, tol);
-        r |= jacobi_rot<T>(a00, a22, a02, a01, a12, V, 0, 2, tol);
-        r |= jacobi_rot<T>(a11, a22, a12, a01, a02, V, 1, 2, tol);
+        bool r = jacobi_rot<T>(a00, a11, a01, a02, a12, V, 0, 1, thresh);
+        r |= jacobi_rot<T>(a00, a22, a02, a01, a12, V, 0, 2, thresh);
+        r |= jacobi_rot<T>(a11, a22, a12, a01, a02, V, 1, 2, thresh);
         if (!r) break;
     }
     lam[0] = a00;
@@ -580,11 +589,18 @@ __device__ inline void svd3_complete(double U[9], const double s[3]) {
 // Drucker-Prager projection in log-strain space (HybridSolver.cpp:632-674).
 // ln: trial log singular values (in/out), q: plasticAmount (in/out).
 // Returns 0 elastic, 1 apex (s = 1), 2 projected.
+// the friction-angle hardening's exp and sin: FP32 takes the fast hardware forms
+// (a few ulps; the cone coefficient they set enters the projection linearly)
+__device__ __forceinline__ float dp_exp(float x) { return __expf(x); }
+__device__ __forceinline__ double dp_exp(double x) { return exp(x); }
+__device__ __forceinline__ float dp_sin(float x) { return __sinf(x); }
+__device__ __forceinline__ double dp_sin(double x) { return sin(x); }
+
 template <typename T>
 __device__ __forceinline__ int dp_project(T ln[3], T& q, T h0, T h1, T h2, T h3, T k) {
     const T deg = T(3.14159265358979323846 / 180.0);
-    T phi = (h0 + (h1 * q - h3) * exp_t(-h2 * q)) * deg;
-    T sphi = sin_t(phi);
+    T phi = (h0 + (h1 * q - h3) * dp_exp(-h2 * q)) * deg;
+    T sphi = dp_sin(phi);
     T alpha = T(0.81649658092772603273) * T(2) * sphi / (T(3) - sphi);  // sqrt(2/3)
     T tr = ln[0] + ln[1] + ln[2];
     T dev[3] = {ln[0] - tr / T(3), ln[1] - tr / T(3), ln[2] - tr / T(3)};

@@ -969,7 +969,7 @@ __device__ __forceinline__ bool stretch_trial(const float F[9], const float D[9]
     const T n2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + T(2) * (e[3] * e[3] + e[4] * e[4] + e[5] * e[5]);
     if (!(n2 < T(0.25))) return false;
     T lam[3];
-    sym_eig3<T>(e[0], e[1], e[2], e[3], e[4], e[5], lam, V, 10, sizeof(T) == 4 ? T(0x1p-25) : T(0x1p-54));
+    sym_eig3<T>(e[0], e[1], e[2], e[3], e[4], e[5], lam, V, 10, sizeof(T) == 4 ? T(0x1p-24) : T(0x1p-52));
 #pragma unroll
     for (int a = 0; a < 3; ++a) ln[a] = T(0.5) * log1p_t(lam[a]);
     return true;
@@ -980,7 +980,8 @@ __device__ __forceinline__ int stretch_project(const KParams& P, int mat, const 
 #pragma unroll
     for (int a = 0; a < 3; ++a) lnn[a] = ln[a];
     if (mat == kSnow) {
-        const T lo = log_t(T(P.snow_lo)), hi = log_t(T(P.snow_hi));
+        const T lo = sizeof(T) == 4 ? T(P.snow_lnlo) : log_t(T(P.snow_lo));
+        const T hi = sizeof(T) == 4 ? T(P.snow_lnhi) : log_t(T(P.snow_hi));
         int kind = 0;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -1057,8 +1058,8 @@ __device__ __forceinline__ int stretch_return_map(const KParams& P, int mat, con
 // Drucker-Prager cone coefficient k alpha(q) of the yield function
 // |dev ln s| + k alpha tr ln s (HybridSolver.cpp:641-653)
 __device__ __forceinline__ float dp_k_alpha(const KParams& P, float q) {
-    const float phi = (P.sand_h0 + (P.sand_h1 * q - P.sand_h3) * expf(-P.sand_h2 * q)) * (3.14159265358979f / 180.0f);
-    const float sphi = sinf(phi);
+    const float phi = (P.sand_h0 + (P.sand_h1 * q - P.sand_h3) * dp_exp(-P.sand_h2 * q)) * (3.14159265358979f / 180.0f);
+    const float sphi = dp_sin(phi);
     return P.sand_k * 0.81649658092772603f * 2.0f * sphi / (3.0f - sphi);
 }
 
@@ -1067,7 +1068,7 @@ __device__ __forceinline__ float dp_k_alpha(const KParams& P, float q) {
 // clamp or the sand cone, which the network predicts).
 __device__ __forceinline__ int trial_kind(const KParams& P, int mat, const float ln[3], float q) {
     if (mat == kSnow) {
-        const float lo = logf(P.snow_lo), hi = logf(P.snow_hi);
+        const float lo = P.snow_lnlo, hi = P.snow_lnhi;
         return (ln[0] < lo || ln[0] > hi || ln[1] < lo || ln[1] > hi || ln[2] < lo || ln[2] > hi) ? 2 : 0;
     }
     const float tr = ln[0] + ln[1] + ln[2];
@@ -1500,7 +1501,7 @@ __device__ __forceinline__ float learned_residual(const KParams& P, int mat, con
                                                   float q, float& q_new) {
     q_new = q;
     if (mat == kSnow) {
-        const float lo = logf(P.snow_lo), hi = logf(P.snow_hi);
+        const float lo = P.snow_lnlo, hi = P.snow_lnhi;
         float r = 0.0f;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {

@@ -2,13 +2,15 @@
 the step time and the per-kernel CUDA-event times:
 
     python -m anisotropicelastoplasticity_gb300.run_scene cloth_drape --steps 20
+    python -m anisotropicelastoplasticity_gb300.run_scene sand_cloth --arg res=256 --arg nside=256 --arg n_sand=950000
 
 Scenes: snow_block (32,768 particles, 64^3), sand_column (524,288, 128^3),
 cloth_drape (65,536 vertices + 130,050 elements, 128^3), snow_sand_collision
 (2,097,152, 256^3), sand_cloth (8,388,608 items, 512^3).  The steps are timed
 twice: once with a start and an end event each, then again with the library's
 events between its kernels (which add a few microseconds per step) for the
-per-kernel times."""
+per-kernel times.  `--arg name=value` passes a size argument to the scene's
+factory (scenes.py), for a smaller case of the same scene."""
 import argparse
 import json
 import sys
@@ -29,10 +31,18 @@ def main(argv=None) -> int:
     ap.add_argument("scene", choices=sorted(SCENES))
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--arg", action="append", default=[], metavar="NAME=VALUE",
+                    help="integer size argument of the scene factory (n, res, nside, n_sand, seed)")
     args = ap.parse_args(argv)
+    kw = {}
+    for a in args.arg:
+        name, _, value = a.partition("=")
+        if name not in ("n", "res", "nside", "n_sand", "seed") or not value.lstrip("-").isdigit():
+            ap.error(f"bad --arg {a!r}")
+        kw[name] = int(value)
     import torch
 
-    sc = SCENES[args.scene]()
+    sc = SCENES[args.scene](**kw)
     s = HybridSolver(sc.particles, sc.grid, sc.params)
     if sc.mesh is not None:
         s.set_lagrangian_mesh(sc.mesh)

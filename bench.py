@@ -446,9 +446,8 @@ def roofline_of(arm: dict, counts: dict) -> dict:
     if tp.exists():
         try:
             t = json.loads(tp.read_text()).get(arm.get("workload", ""), {}).get(dom)
-            if t:
-                traffic = t["bytes_per_item"] * (counts["particles"] + counts["verts"]) + \
-                    t.get("bytes_per_node", 0.0) * counts["nodes"]
+            if t:  # DRAM bytes per item of an ncu capture of a smaller case, scaled to the items
+                traffic = t["bytes_per_item"] * (counts["particles"] + counts["verts"] + counts["elems"])
         except Exception:
             traffic = None
     kernels = {}
