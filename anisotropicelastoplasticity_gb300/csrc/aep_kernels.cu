@@ -1484,7 +1484,9 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
 // consecutive rows runs the MLP (aep_mlp.cuh) on the tensor cores on the sorted
 // trial log singular values, and each prediction is checked against the optimality
 // conditions of the projection it stands for (HybridSolver.cpp:626-674), with the
-// residuals in ln-strain units and accepted within max(tol_rel |ln s_trial|, tol_abs):
+// residuals in ln-strain units and accepted within max(tol_rel |ln s_pred|, tol_abs),
+// relative to the projected strain the prediction gives (the stress is linear in it,
+// so an accepted state's stress carries a relative error of a few tol_rel):
 //   sand (the cone; the apex never reaches the network): the yield condition at the
 //     prediction, |dev| + k alpha(q) tr = 0, and the flow rule: the trace kept and the
 //     deviatoric part a shrunk copy of the trial's (0 <= c <= 1);
@@ -1544,9 +1546,7 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char* wbase = smem_raw + kMlpSmemBytes + warp * kMlpWarpBytes;
     __nv_bfloat16* X = reinterpret_cast<__nv_bfloat16*>(wbase);
-    __nv_bfloat16* H0 = X + kMlpWarpX;
-    __nv_bfloat16* H1 = H0 + kMlpWarpH;
-    float* Y = reinterpret_cast<float*>(H1 + kMlpWarpH);
+    float* Y = reinterpret_cast<float*>(X + kMlpWarpX);
     const long cap = Qu.cap;
     unsigned n_ok = 0, n_rej = 0;
     const int nwarps = gridDim.x * (kFinThreads / 32);
@@ -1564,16 +1564,16 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
         sort3_desc(ln, srt, pm);
         float q = f[kQQ * cap];
         const float osc = mlp_features(srt, q, mat, X + lane * kStrideIn);
-        mlp_forward_warp(W, X, H0, H1, Y, lane);
+        mlp_forward_warp(W, X, Y, lane);
         if (live) {
             float pred[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) pred[pm[k]] = srt[k] + Y[lane * kMlpOut + k] / osc;
             float q_new;
             const float res = learned_residual(P, mat, ln, pred, q, q_new);
-            const float lnorm = sqrtf(ln[0] * ln[0] + ln[1] * ln[1] + ln[2] * ln[2]);
+            const float pnorm = sqrtf(pred[0] * pred[0] + pred[1] * pred[1] + pred[2] * pred[2]);
             float lnn[3];
-            if (res <= fmaxf(tol_rel * lnorm, tol_abs)) {
+            if (res <= fmaxf(tol_rel * pnorm, tol_abs)) {
                 lnn[0] = pred[0]; lnn[1] = pred[1]; lnn[2] = pred[2];
                 ++n_ok;
             } else {  // the exact projection
@@ -1739,19 +1739,17 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         unsigned char* wbase = smem_raw + kMlpSmemBytes + warp * kMlpWarpBytes;
         __nv_bfloat16* MX = reinterpret_cast<__nv_bfloat16*>(wbase);
-        __nv_bfloat16* MH0 = MX + kMlpWarpX;
-        __nv_bfloat16* MH1 = MH0 + kMlpWarpH;
-        float* MY = reinterpret_cast<float*>(MH1 + kMlpWarpH);
+        float* MY = reinterpret_cast<float*>(MX + kMlpWarpX);
         bool ok = false;
         if (__any_sync(0xffffffffu, plastic)) {  // warp-uniform
             const float in[3] = {r[0], r[1], r[2] - 1.0f};
             const float sc = mlp_features(in, cap, plastic ? kMlpCloth : 0, MX + lane * kStrideIn);
-            mlp_forward_warp(W, MX, MH0, MH1, MY, lane);
+            mlp_forward_warp(W, MX, MY, lane);
             if (plastic) {
                 // optimality conditions of the frictional cap: r33 kept, the shear
                 // (r13, r23) a shrunk copy of the trial's, its length on the cap
                 // friction * stiffness (r33 - 1)^2 / shear; residuals in r units,
-                // relative to the trial's (r13, r23, r33 - 1)
+                // relative to the predicted (r13, r23, r33 - 1)
                 float pred[3];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) pred[a] = r[a] + MY[lane * kMlpOut + a] / sc;
@@ -1760,7 +1758,7 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
                 const float on_cap = M.friction * M.stiffness * (r[2] - 1.0f) * (r[2] - 1.0f) / M.shear;
                 float res = fmaxf(fabsf(pred[2] - r[2]), fabsf(nsp - on_cap));
                 res = fmaxf(res, fmaxf(fabsf(pred[0] - c * r[0]), fabsf(pred[1] - c * r[1])));
-                const float ref = sqrtf(ns * ns + (r[2] - 1.0f) * (r[2] - 1.0f));
+                const float ref = sqrtf(nsp * nsp + (pred[2] - 1.0f) * (pred[2] - 1.0f));
                 ok = res <= fmaxf(tol_rel * ref, tol_abs);
                 if (ok) {
                     rp[0] = pred[0]; rp[1] = pred[1]; rp[2] = pred[2];

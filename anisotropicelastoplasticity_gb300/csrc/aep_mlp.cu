@@ -288,9 +288,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(MlpParams P, const float* __r
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char* wbase = smem_raw + kMlpSmemBytes + warp * kMlpWarpBytes;
     bf16* X = reinterpret_cast<bf16*>(wbase);
-    bf16* H0 = X + kMlpWarpX;
-    bf16* H1 = H0 + kMlpWarpH;
-    float* Y = reinterpret_cast<float*>(H1 + kMlpWarpH);
+    float* Y = reinterpret_cast<float*>(X + kMlpWarpX);
     const long r = ((long)blockIdx.x * 4 + warp) * 32 + lane;
     float sc = 1.0f;
     if (r < n) {
@@ -301,7 +299,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(MlpParams P, const float* __r
         float ln[3] = {0, 0, 0};
         mlp_features(ln, 0.0f, 0, X + lane * kStrideIn);
     }
-    mlp_forward_warp(W, X, H0, H1, Y, lane);
+    mlp_forward_warp(W, X, Y, lane);
     if (r < n)
         for (int k = 0; k < 3; ++k) out[3 * r + k] = Y[lane * kMlpOut + k] / sc;
 }

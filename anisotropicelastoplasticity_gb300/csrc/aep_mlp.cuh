@@ -77,20 +77,29 @@ __device__ __forceinline__ MlpSmem mlp_smem_carve(void* base) {
 }
 constexpr int kMlpSmemBytes = kMlpSmemWeightsBf16 * 2 + kMlpSmemBias * 4;
 
-// cooperative copy of the weights into padded shared rows (all threads of the block)
+// cooperative copy of the weights into padded shared rows (all threads of the block),
+// 16 bytes at a time: every block in global memory starts on a 16-byte boundary
+// (offsets of 1024, 5120, 9216 halves and 9728.. floats into 256-byte aligned
+// allocations), and the padded rows (48 and 144 bytes) keep 16-byte alignment
 __device__ __forceinline__ void mlp_load_smem(const MlpParams& p, const MlpSmem& s, int tid, int nthreads) {
-    for (int i = tid; i < 64 * 16; i += nthreads) s.w1t[(i / 16) * kStrideIn + (i % 16)] = p.w1t[i];
-    for (int i = tid; i < 64 * 64; i += nthreads) {
-        s.w2t[(i / 64) * kStrideH + (i % 64)] = p.w2t[i];
-        s.w3t[(i / 64) * kStrideH + (i % 64)] = p.w3t[i];
+    const uint4* g1 = reinterpret_cast<const uint4*>(p.w1t);
+    const uint4* g2 = reinterpret_cast<const uint4*>(p.w2t);
+    const uint4* g3 = reinterpret_cast<const uint4*>(p.w3t);
+    const uint4* g4 = reinterpret_cast<const uint4*>(p.w4t);
+    for (int i = tid; i < 64 * 2; i += nthreads)
+        *reinterpret_cast<uint4*>(s.w1t + (i >> 1) * kStrideIn + (i & 1) * 8) = g1[i];
+    for (int i = tid; i < 64 * 8; i += nthreads) {
+        *reinterpret_cast<uint4*>(s.w2t + (i >> 3) * kStrideH + (i & 7) * 8) = g2[i];
+        *reinterpret_cast<uint4*>(s.w3t + (i >> 3) * kStrideH + (i & 7) * 8) = g3[i];
     }
-    for (int i = tid; i < 8 * 64; i += nthreads) s.w4t[(i / 64) * kStrideH + (i % 64)] = p.w4t[i];
-    for (int i = tid; i < 64; i += nthreads) {
-        s.b1[i] = p.b1[i];
-        s.b2[i] = p.b2[i];
-        s.b3[i] = p.b3[i];
+    for (int i = tid; i < 8 * 8; i += nthreads)
+        *reinterpret_cast<uint4*>(s.w4t + (i >> 3) * kStrideH + (i & 7) * 8) = g4[i];
+    for (int i = tid; i < 16; i += nthreads) {
+        reinterpret_cast<float4*>(s.b1)[i] = reinterpret_cast<const float4*>(p.b1)[i];
+        reinterpret_cast<float4*>(s.b2)[i] = reinterpret_cast<const float4*>(p.b2)[i];
+        reinterpret_cast<float4*>(s.b3)[i] = reinterpret_cast<const float4*>(p.b3)[i];
     }
-    for (int i = tid; i < 8; i += nthreads) s.b4[i] = p.b4[i];
+    for (int i = tid; i < 2; i += nthreads) reinterpret_cast<float4*>(s.b4)[i] = reinterpret_cast<const float4*>(p.b4)[i];
 }
 
 __device__ __forceinline__ void mma_bf16(float c[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
@@ -110,64 +119,120 @@ __device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16* p) {
 // are rounded to bfloat16 right after, 2^-8 relative, far above their error)
 __device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 
-// One dense layer for the 32 rows of a warp: out[32][N] = act(A[32][K] W + b).
-// A: bf16 rows of stride sa; Wt: bf16 [N][K] rows of stride sw.  ACT: apply SiLU and
-// store bf16 to `out` (stride so); otherwise store f32 to `outf` (stride sof).
-template <int K, int N, bool ACT>
-__device__ __forceinline__ void mlp_layer_warp(const __nv_bfloat16* A, int sa, const __nv_bfloat16* Wt, int sw,
-                                               const float* bias, __nv_bfloat16* out, int so, float* outf, int sof,
-                                               int lane) {
-    const int g = lane >> 2, t = lane & 3;
+// Per-warp scratch for one 32-row inference (halves / floats): the input rows and
+// the output rows; the hidden activations stay in registers (mlp_forward_warp)
+constexpr int kMlpWarpX = 32 * kStrideIn;   // bf16
+constexpr int kMlpWarpY = 32 * kMlpOut;     // f32
+constexpr int kMlpWarpBytes = kMlpWarpX * 2 + kMlpWarpY * 4;
+
+// four 8x8 bf16 matrices from shared memory (lane i gives the row address of
+// matrix i/8, row i%8; register j of lane l holds matrix j's row l/4, columns
+// 2(l%4), 2(l%4)+1)
+__device__ __forceinline__ void ldmatrix_x4(const __nv_bfloat16* p, uint32_t& r0, uint32_t& r1, uint32_t& r2,
+                                            uint32_t& r3) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// One hidden layer (64 -> 64, SiLU) of the warp's 32 rows with the activations in
+// registers: a[mt][kt][.] is the m16n8k16 A fragment of rows mt*16.., columns
+// kt*16.. of the input; the layer writes the same fragment of its output to o.
+// The C fragment of output columns nt*8.. (rows g, g+8; columns 2t, 2t+1) is the A
+// fragment's register pair {0,1} (nt even) or {2,3} (nt odd) of k tile nt/2, so the
+// epilogue packs it in place.  B fragments come from the padded rows of W^T by
+// ldmatrix (two k tiles of one n tile per instruction).
+__device__ __forceinline__ void mlp_hidden_layer_reg(const uint32_t (&a)[2][4][4], uint32_t (&o)[2][4][4],
+                                                     const __nv_bfloat16* Wt, const float* bias, int lane) {
+    const int t = lane & 3;
+    // ldmatrix row address of this lane: matrix (lane>>3) = (k tile pair member lane>>4,
+    // k half (lane>>3)&1), row lane&7 of the n tile
+    const __nv_bfloat16* wrow = Wt + (lane & 7) * kStrideH + (lane >> 4) * 16 + ((lane >> 3) & 1) * 8;
 #pragma unroll
-    for (int nt = 0; nt < N / 8; ++nt) {
+    for (int nt = 0; nt < 8; ++nt) {
         float c[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
 #pragma unroll
-        for (int k0 = 0; k0 < K; k0 += 16) {
-            const __nv_bfloat16* wb = Wt + (nt * 8 + g) * sw + k0 + 2 * t;
-            const uint32_t b0 = ld_pair(wb), b1 = ld_pair(wb + 8);
+        for (int kp = 0; kp < 2; ++kp) {  // k tiles 2kp, 2kp+1
+            uint32_t b00, b01, b10, b11;
+            ldmatrix_x4(wrow + nt * 8 * kStrideH + kp * 32, b00, b01, b10, b11);
 #pragma unroll
             for (int mt = 0; mt < 2; ++mt) {
-                const __nv_bfloat16* ab = A + (mt * 16 + g) * sa + k0 + 2 * t;
-                mma_bf16(c[mt], ld_pair(ab), ld_pair(ab + 8 * sa), ld_pair(ab + 8), ld_pair(ab + 8 * sa + 8), b0, b1);
+                mma_bf16(c[mt], a[mt][2 * kp][0], a[mt][2 * kp][1], a[mt][2 * kp][2], a[mt][2 * kp][3], b00, b01);
+                mma_bf16(c[mt], a[mt][2 * kp + 1][0], a[mt][2 * kp + 1][1], a[mt][2 * kp + 1][2],
+                         a[mt][2 * kp + 1][3], b10, b11);
             }
         }
         const int n0 = nt * 8 + 2 * t;
         const float bb0 = bias[n0], bb1 = bias[n0 + 1];
 #pragma unroll
         for (int mt = 0; mt < 2; ++mt) {
-            const int r0 = mt * 16 + g, r1 = r0 + 8;
-            float v00 = c[mt][0] + bb0, v01 = c[mt][1] + bb1, v10 = c[mt][2] + bb0, v11 = c[mt][3] + bb1;
-            if (ACT) {
-                *reinterpret_cast<__nv_bfloat162*>(out + r0 * so + n0) = __floats2bfloat162_rn(silu(v00), silu(v01));
-                *reinterpret_cast<__nv_bfloat162*>(out + r1 * so + n0) = __floats2bfloat162_rn(silu(v10), silu(v11));
-            } else {
-                outf[r0 * sof + n0] = v00;
-                outf[r0 * sof + n0 + 1] = v01;
-                outf[r1 * sof + n0] = v10;
-                outf[r1 * sof + n0 + 1] = v11;
-            }
+            o[mt][nt >> 1][(nt & 1) * 2] = pack_bf16x2(silu(c[mt][0] + bb0), silu(c[mt][1] + bb1));
+            o[mt][nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(silu(c[mt][2] + bb0), silu(c[mt][3] + bb1));
         }
     }
 }
 
-// Per-warp scratch for one 32-row inference (halves / floats)
-constexpr int kMlpWarpX = 32 * kStrideIn;   // bf16
-constexpr int kMlpWarpH = 32 * kStrideH;    // bf16, two buffers
-constexpr int kMlpWarpY = 32 * kMlpOut;     // f32
-constexpr int kMlpWarpBytes = (kMlpWarpX + 2 * kMlpWarpH) * 2 + kMlpWarpY * 4;
-
 // Forward pass of the 32 rows a warp holds in X (row r written by lane r); result
-// rows in Y (row r read back by lane r).  All 32 lanes must call it.
-__device__ __forceinline__ void mlp_forward_warp(const MlpSmem& W, __nv_bfloat16* X, __nv_bfloat16* H0,
-                                                 __nv_bfloat16* H1, float* Y, int lane) {
+// rows in Y (row r read back by lane r).  All 32 lanes must call it.  Each layer
+// accumulates its 16-wide k tiles in order in FP32 and rounds its SiLU outputs to
+// bfloat16 (the rounding points of the oracle's forward); the hidden activations
+// stay in registers between layers.
+__device__ __forceinline__ void mlp_forward_warp(const MlpSmem& W, __nv_bfloat16* X, float* Y, int lane) {
+    const int g = lane >> 2, t = lane & 3;
     __syncwarp();
-    mlp_layer_warp<kMlpIn, kMlpHidden, true>(X, kStrideIn, W.w1t, kStrideIn, W.b1, H0, kStrideH, nullptr, 0, lane);
-    __syncwarp();
-    mlp_layer_warp<kMlpHidden, kMlpHidden, true>(H0, kStrideH, W.w2t, kStrideH, W.b2, H1, kStrideH, nullptr, 0, lane);
-    __syncwarp();
-    mlp_layer_warp<kMlpHidden, kMlpHidden, true>(H1, kStrideH, W.w3t, kStrideH, W.b3, H0, kStrideH, nullptr, 0, lane);
-    __syncwarp();
-    mlp_layer_warp<kMlpHidden, kMlpOut, false>(H0, kStrideH, W.w4t, kStrideH, W.b4, nullptr, 0, Y, kMlpOut, lane);
+    uint32_t h0[2][4][4], h1[2][4][4];
+    {  // layer 1 (16 -> 64): A fragments from X, B fragments by pairs of 32-bit loads
+        uint32_t x[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            const __nv_bfloat16* ab = X + (mt * 16 + g) * kStrideIn + 2 * t;
+            x[mt][0] = ld_pair(ab);
+            x[mt][1] = ld_pair(ab + 8 * kStrideIn);
+            x[mt][2] = ld_pair(ab + 8);
+            x[mt][3] = ld_pair(ab + 8 * kStrideIn + 8);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const __nv_bfloat16* wb = W.w1t + (nt * 8 + g) * kStrideIn + 2 * t;
+            const uint32_t b0 = ld_pair(wb), b1 = ld_pair(wb + 8);
+            const int n0 = nt * 8 + 2 * t;
+            const float bb0 = W.b1[n0], bb1 = W.b1[n0 + 1];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                float c[4] = {0, 0, 0, 0};
+                mma_bf16(c, x[mt][0], x[mt][1], x[mt][2], x[mt][3], b0, b1);
+                h0[mt][nt >> 1][(nt & 1) * 2] = pack_bf16x2(silu(c[0] + bb0), silu(c[1] + bb1));
+                h0[mt][nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(silu(c[2] + bb0), silu(c[3] + bb1));
+            }
+        }
+    }
+    mlp_hidden_layer_reg(h0, h1, W.w2t, W.b2, lane);
+    mlp_hidden_layer_reg(h1, h0, W.w3t, W.b3, lane);
+    {  // output layer (64 -> 8), FP32 rows to Y
+        float c[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            const __nv_bfloat16* wb = W.w4t + g * kStrideH + kt * 16 + 2 * t;
+            const uint32_t b0 = ld_pair(wb), b1 = ld_pair(wb + 8);
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) mma_bf16(c[mt], h0[mt][kt][0], h0[mt][kt][1], h0[mt][kt][2], h0[mt][kt][3], b0, b1);
+        }
+        const float bb0 = W.b4[2 * t], bb1 = W.b4[2 * t + 1];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            const int r0 = mt * 16 + g, r1 = r0 + 8;
+            Y[r0 * kMlpOut + 2 * t] = c[mt][0] + bb0;
+            Y[r0 * kMlpOut + 2 * t + 1] = c[mt][1] + bb1;
+            Y[r1 * kMlpOut + 2 * t] = c[mt][2] + bb0;
+            Y[r1 * kMlpOut + 2 * t + 1] = c[mt][3] + bb1;
+        }
+    }
     __syncwarp();
 }
 

@@ -85,14 +85,34 @@ class ReturnMapMLP:
                                               C.c_void_p(stream_ptr)))
 
 
-def harvest_records(scene, steps: int, capacity: int, stride: int = 1, warm_steps: int = 0):
-    """Run the exact (plain) step on `scene` and return a torch CUDA tensor of the
-    harvested records [count, 8]."""
+def canonical_order(recs):
+    """The records sorted lexicographically by their 32-bit patterns: the kernels
+    append records in whatever order their atomics run, so this fixes one order
+    for a set of records (and with it the batches training draws)."""
+    import torch
+
+    bits = recs.view(torch.int32)
+    order = torch.arange(len(recs), device=recs.device)
+    for c in reversed(range(recs.shape[1])):  # least significant column first, stable sorts
+        order = order[torch.sort(bits[order, c], stable=True).indices]
+    return recs[order]
+
+
+def harvest_records(scene, steps: int, capacity: int, stride: int = 1, warm_steps: int = 0, seed: int = 0):
+    """Run the exact (plain) step on `scene` and return a torch CUDA tensor of at most
+    `capacity` harvested records [count, 8], the same records on every run: the buffer
+    holds every record the steps can produce (one per particle slot of stride and step,
+    one per cloth element and step), the records are put in canonical order and, when
+    there are more than `capacity`, a seeded uniform sample of them over all steps is
+    kept."""
     import torch
 
     from .solver import HybridSolver
 
-    buf = torch.empty((capacity, 8), dtype=torch.float32, device="cuda")
+    n_items = scene.num_items()
+    n_elem = len(scene.mesh.faces) if scene.mesh is not None else 0
+    room = steps * (-(-n_items // stride) + n_elem)
+    buf = torch.empty((room, 8), dtype=torch.float32, device="cuda")
     s = HybridSolver(scene.particles, scene.grid, scene.params)
     if scene.mesh is not None:
         s.set_lagrangian_mesh(scene.mesh)
@@ -100,10 +120,17 @@ def harvest_records(scene, steps: int, capacity: int, stride: int = 1, warm_step
     s.init_volumes()
     for _ in range(warm_steps):
         s.step(scene.dt)
-    s.set_harvest(buf.data_ptr(), capacity, stride)
+    s.set_harvest(buf.data_ptr(), room, stride)
     for _ in range(steps):
         s.step(scene.dt)
     cnt = s.harvest_count()
     s.set_harvest(None)
     s.close()
-    return buf[:cnt]
+    if cnt >= room:
+        raise RuntimeError(f"harvest buffer of {room} records filled")
+    recs = canonical_order(buf[:cnt])
+    del buf
+    if cnt > capacity:
+        keep = torch.randperm(cnt, generator=torch.Generator().manual_seed(seed))[:capacity]
+        recs = recs[torch.sort(keep).values.to(recs.device)]
+    return recs.contiguous()

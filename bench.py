@@ -41,10 +41,11 @@ L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 
 # acceptance bounds of the learned return map's in-kernel check (the residuals of
 # the projection's yield condition and flow rule, ln-strain units), as (relative to
-# |ln s_trial|, absolute): "strict" accepts residuals within 1e-4 of the trial
-# strain (or the FP32 resolution of ln s, 2^-23), which keeps an accepted state's
-# stress within ~1e-3; "residual_1e-4" accepts an absolute residual of 1e-4, the
-# bound the learned-map configuration states
+# the predicted |ln s|, absolute): "strict" accepts residuals within 1e-4 of the
+# projected strain the prediction gives (or the FP32 resolution of ln s, 2^-23),
+# which keeps an accepted state's stress within a few 1e-4 of the exact one;
+# "residual_1e-4" accepts an absolute residual of 1e-4, the bound the learned-map
+# configuration states
 LEARNED_BOUNDS = {"strict": (1e-4, 2.0 ** -23), "residual_1e-4": (0.0, 1e-4)}
 
 

@@ -87,9 +87,9 @@ def test_gpu_gradient_matches_oracle():
         print(f"{name}: relative gradient difference {err:.2e}")
         # the two round to bfloat16 at the same points; an activation or gradient
         # whose FP32 value lands on the other side of a rounding boundary (the
-        # accumulation orders differ) moves by 2^-9 of itself, which a few such
-        # entries per layer turn into ~1e-4 of the layer's gradient
-        assert err < 2e-3, (name, err)
+        # accumulation orders differ) moves by 2^-9 of itself.  Measured on GB300:
+        # at most 2.7e-6 (the biases of layers 1 and 2), 1e-7..8e-7 for the weights
+        assert err < 5e-5, (name, err)
 
 
 @pytest.mark.gpu
@@ -155,6 +155,36 @@ def _harvest_small(torch):
             harvest_records(_strained(scenes.sand_column(n=12000, res=32, seed=2), 7), steps=40, capacity=200000,
                             stride=1)]
     return torch.cat(recs)
+
+
+def test_canonical_order_does_not_depend_on_the_input_order():
+    """The harvest kernels append records in the order their atomics run; the
+    canonical order (lexicographic by bit pattern) is the same for any permutation
+    of one record set, duplicates included."""
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import canonical_order
+
+    rec = torch.from_numpy(random_records(5000, seed=21))
+    rec = torch.cat([rec, rec[:100]])
+    a = canonical_order(rec)
+    b = canonical_order(rec[torch.randperm(len(rec), generator=torch.Generator().manual_seed(3))])
+    assert torch.equal(a, b)
+    bits = a.view(torch.int32).numpy()
+    keys = [tuple(r) for r in bits[:200]]
+    assert keys == sorted(keys)
+
+
+@pytest.mark.gpu
+def test_harvest_is_the_same_on_every_run():
+    """Two harvests of the same scene give the same records in the same order, also
+    when more records arrive than are kept (a seeded sample over all steps)."""
+    torch = pytest.importorskip("torch")
+    from anisotropicelastoplasticity_gb300.learned import harvest_records
+
+    runs = [harvest_records(_strained(scenes.sand_column(n=12000, res=32, seed=2), 7), steps=20, capacity=50000,
+                            stride=1) for _ in range(2)]
+    assert len(runs[0]) == 50000
+    assert torch.equal(runs[0], runs[1])
 
 
 @pytest.mark.gpu
