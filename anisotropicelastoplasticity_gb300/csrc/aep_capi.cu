@@ -963,7 +963,7 @@ aep_status step_impl(aep_solver* s, double dt_force, double dt, int32_t stage, b
     MlpParams mp{};
     if (s->mlp) {
         mp = mlp_device_params(s->mlp);
-        if (s->queue.cap < s->n) {  // room for every particle: (int32 j, pj, 35 floats) per row
+        if (s->queue.cap < s->n) {  // room for every particle: (int32 j, pj, kQueueFields floats) per row
             CK(cudaStreamSynchronize(s->stream));
             cudaFree(s->queue_mem);
             s->queue_mem = nullptr;

@@ -145,16 +145,16 @@ struct DevStats {
 // Rows of the learned return map that the G2P pass queues for k_mlp_finish
 // (plastic snow and sand states whose projection is not a constant): field-major
 // float arrays of `cap` rows, the fields below: the trial log singular values, the
-// plastic scalar, the state F, the F update D and the right singular vectors V of
-// F + D (the stretch form of the return mapping).
+// F update D and the right singular vectors V of F + D (the stretch form of the
+// return mapping); F and the plastic scalar stay in the current state arrays.
 struct MlpQueue {
     int32_t* j;   // slot in the new order
     int32_t* pj;  // slot in the current order
     float* f;     // [kQueueFields][cap]
     int cap;
 };
-constexpr int kQLn = 0, kQQ = 3, kQF = 4, kQD = 13, kQV = 22;
-constexpr int kQueueFields = 31;
+constexpr int kQLn = 0, kQD = 3, kQV = 12;
+constexpr int kQueueFields = 21;
 
 // Training-pair harvest from the exact return mapping (plain G2P): records of 8
 // floats [ln s trial sorted desc (3), q, material, ln s_new - ln s trial (3)].

@@ -1193,7 +1193,7 @@ __device__ __forceinline__ void harvest_record(const KParams& P, const Harvest& 
 // G2P + APIC + advection + F update + return mapping, one thread per particle.
 // kDefer (the learned return map): the trial state's yield check runs here; a
 // plastic snow or sand state whose projection is not a constant is queued (trial
-// ln s, q, F, D, V) for k_mlp_finish, which writes its F_E, F_P and plastic scalar;
+// ln s, D, V) for k_mlp_finish, which writes its F_E, F_P and plastic scalar;
 // elastic states and the sand apex are mapped exactly here.
 template <bool kDefer>
 __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays nxt, const int32_t* __restrict__ perm,
@@ -1346,10 +1346,8 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
                     Qu.pj[r] = pj;
 #pragma unroll
                     for (int a = 0; a < 3; ++a) f[(kQLn + a) * cap] = ln[a];
-                    f[kQQ * cap] = q;
 #pragma unroll
                     for (int k = 0; k < 9; ++k) {
-                        f[(kQF + k) * cap] = F[k];
                         f[(kQD + k) * cap] = D[k];
                         f[(kQV + k) * cap] = V[k];
                     }
@@ -1562,7 +1560,7 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
 #pragma unroll
         for (int a = 0; a < 3; ++a) ln[a] = f[(kQLn + a) * cap];
         sort3_desc(ln, srt, pm);
-        float q = f[kQQ * cap];
+        float q = cur.plastic[pj];
         const float osc = mlp_features(srt, q, mat, X + lane * kStrideIn);
         mlp_forward_warp(W, X, Y, lane);
         if (live) {
@@ -1584,7 +1582,7 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
             float F[9], D[9], V[9], Fe[9], sig[3];
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                F[k] = f[(kQF + k) * cap];
+                F[k] = cur.F[k][pj];
                 D[k] = f[(kQD + k) * cap];
                 V[k] = f[(kQV + k) * cap];
             }

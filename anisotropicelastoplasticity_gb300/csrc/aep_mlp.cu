@@ -41,7 +41,8 @@ static_assert(kNumParams == AEP_MLP_NUM_PARAMS, "parameter count");
 
 constexpr int kTrainRows = 64;
 constexpr int kPartBlocks = 256;  // blocks of one gradient pass (16,384 rows)
-constexpr int kTrainThreads = 128;
+constexpr int kTrainThreads = 256;
+constexpr int kTrainWarps = kTrainThreads / 32;
 
 using bf16 = __nv_bfloat16;
 
@@ -69,17 +70,17 @@ __device__ __forceinline__ void tile_mma(float c[4], const bf16* A, int ars, int
     }
 }
 
+// 114,480 bytes: two blocks fit on an SM
 struct TrainSmem {
-    bf16 W1[64 * 16], W2[64 * 64], W3[64 * 64], W4[8 * 64];  // W^T, dense rows
+    bf16 W1[64 * 16], W2[64 * 64], W3[64 * 64], W4[8 * 64];  // W^T, dense rows (the layout of the bf16 copy)
     float b[200];
     bf16 X[kTrainRows * 16];
     bf16 H[3][kTrainRows * 64];   // post-activations
     float Z[3][kTrainRows * 64];  // pre-activations
-    float Y[kTrainRows * 8];
     float T[kTrainRows * 4];
     bf16 dY[kTrainRows * 8];
     bf16 dZ[2][kTrainRows * 64];  // ping-pong
-    float wloss[kTrainThreads / 32];
+    float wloss[kTrainWarps];
 };
 
 __device__ __forceinline__ float dsilu(float z) {
@@ -90,22 +91,22 @@ __device__ __forceinline__ float dsilu(float z) {
 // Forward and backward of one block of rows.  The block's gradient (f32, packed)
 // goes to its own row of `part` and its loss to part_loss[block]; k_mlp_reduce
 // sums the rows in block order, so training repeats bit for bit.
-__global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* __restrict__ params,
-                                                                  const float* __restrict__ rec, int n, int row0,
-                                                                  int row_end, int rows_total, float* __restrict__ part,
-                                                                  float* __restrict__ part_loss) {
+__global__ void __launch_bounds__(kTrainThreads, 2) k_mlp_train_tile(const float* __restrict__ params,
+                                                                     const bf16* __restrict__ wb,
+                                                                     const float* __restrict__ rec, int n, int row0,
+                                                                     int row_end, int rows_total,
+                                                                     float* __restrict__ part,
+                                                                     float* __restrict__ part_loss) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int base = row0 + blockIdx.x * kTrainRows;
     float* const grad = part + (long)blockIdx.x * kNumParams;
-    for (int i = tid; i < kOffB1; i += kTrainThreads) {
-        const bf16 w = __float2bfloat16(params[i]);
-        if (i < kOffW2) S.W1[i - kOffW1] = w;
-        else if (i < kOffW3) S.W2[i - kOffW2] = w;
-        else if (i < kOffW4) S.W3[i - kOffW3] = w;
-        else S.W4[i - kOffW4] = w;
-    }
+    // the bf16 copy of the weights (refreshed by every Adam step) has the layout of
+    // W1..W4 here: one 16-byte copy per 8 weights
+    static_assert(kNumWeights % 8 == 0, "weight copy in 16-byte pieces");
+    for (int i = tid; i < kNumWeights / 8; i += kTrainThreads)
+        reinterpret_cast<uint4*>(S.W1)[i] = reinterpret_cast<const uint4*>(wb)[i];
     for (int i = tid; i < 200; i += kTrainThreads) S.b[i] = params[kOffB1 + i];
     for (int r = tid; r < kTrainRows; r += kTrainThreads) {
         const long gi = (long)(base + r) % n;  // wrap around the record set
@@ -122,7 +123,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
     const bf16* Wl[3] = {S.W1, S.W2, S.W3};
     const int Kin[3] = {16, 64, 64};
     for (int l = 0; l < 3; ++l) {
-        for (int tt = warp; tt < 32; tt += 4) {  // 4 m-tiles x 8 n-tiles
+        for (int tt = warp; tt < 32; tt += kTrainWarps) {  // 4 m-tiles x 8 n-tiles
             const int m0 = (tt >> 3) * 16, n0 = (tt & 7) * 8;
             float c[4] = {0, 0, 0, 0};
             if (l == 0) tile_mma<16>(c, Hin[0], 16, 1, kTrainRows, Wl[0], 1, 16, 16, m0, n0, lane);
@@ -138,7 +139,9 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         __syncthreads();
         (void)Kin;
     }
-    {   // output layer: 4 m-tiles x 1 n-tile
+    if (warp >= 4) {
+        if (lane == 0) S.wloss[warp] = 0.0f;
+    } else {  // output layer: 4 m-tiles x 1 n-tile, one per warp
         const int m0 = warp * 16;
         float c[4] = {0, 0, 0, 0};
         tile_mma<64>(c, S.H[2], 64, 1, kTrainRows, S.W4, 1, 64, 64, m0, 0, lane);
@@ -147,7 +150,6 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         for (int e = 0; e < 4; ++e) {
             const int r = m0 + g + (e >> 1) * 8, col = 2 * t + (e & 1);
             const float y = c[e] + S.b[192 + col];
-            S.Y[r * 8 + col] = y;
             float d = 0.0f;
             if (col < 3) {
                 const float diff = y - S.T[r * 4 + col];
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
     __syncthreads();
     // ---- backward
     // dW4t[j][k] = sum_r dY[r][j] H3[r][k]; db4[j] = sum_r dY[r][j]
-    for (int tt = warp; tt < 8; tt += 4) {
+    for (int tt = warp; tt < 8; tt += kTrainWarps) {
         const int n0 = tt * 8;
         float c[4] = {0, 0, 0, 0};
         tile_mma<64>(c, S.dY, 1, 8, 8, S.H[2], 64, 1, kTrainRows, 0, n0, lane);
@@ -180,7 +182,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         grad[kOffB4 + tid] = s;
     }
     // dZ3 = (dY W4^T) * silu'(Z3):  dH3[r][k] = sum_j dY[r][j] W4t[j][k]
-    for (int tt = warp; tt < 32; tt += 4) {
+    for (int tt = warp; tt < 32; tt += kTrainWarps) {
         const int m0 = (tt >> 3) * 16, n0 = (tt & 7) * 8;
         float c[4] = {0, 0, 0, 0};
         tile_mma<16>(c, S.dY, 8, 1, kTrainRows, S.W4, 64, 1, 8, m0, n0, lane);
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         const bf16* Hp = l == 0 ? S.X : S.H[l - 1];
         const int kin = l == 0 ? 16 : 64;
         const int ntiles = (64 / 16) * (kin / 8);
-        for (int tt = warp; tt < ntiles; tt += 4) {
+        for (int tt = warp; tt < ntiles; tt += kTrainWarps) {
             const int m0 = (tt / (kin / 8)) * 16, n0 = (tt % (kin / 8)) * 8;
             float c[4] = {0, 0, 0, 0};
             tile_mma<kTrainRows>(c, dZ, 1, 64, 64, Hp, kin, 1, kTrainRows, m0, n0, lane);
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
         }
         if (l > 0) {
             bf16* dZn = S.dZ[1 - cur];
-            for (int tt = warp; tt < 32; tt += 4) {
+            for (int tt = warp; tt < 32; tt += kTrainWarps) {
                 const int m0 = (tt >> 3) * 16, n0 = (tt & 7) * 8;
                 float c[4] = {0, 0, 0, 0};
                 // dH_{l-1}[r][k] = sum_n dZ_l[r][n] W_l^T[n][k]
@@ -235,21 +237,38 @@ __global__ void __launch_bounds__(kTrainThreads) k_mlp_train_tile(const float* _
     }
     if (tid == 0) {
         float l = 0.0f;
-        for (int w = 0; w < kTrainThreads / 32; ++w) l += S.wloss[w];
+        for (int w = 0; w < kTrainWarps; ++w) l += S.wloss[w];
         part_loss[blockIdx.x] = l / (3.0f * rows_total);
     }
 }
 
-// grad[i] (+)= sum over the blocks of part[b][i] in block order; loss likewise
-__global__ void k_mlp_reduce(const float* __restrict__ part, const float* __restrict__ part_loss, int blocks,
-                             float* __restrict__ grad, float* __restrict__ loss, int accumulate) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < kNumParams) {
-        float s = accumulate ? grad[i] : 0.0f;
-        for (int b = 0; b < blocks; ++b) s += part[(long)b * kNumParams + i];
-        grad[i] = s;
+// grad[i] (+)= sum over the blocks of part[b][i]; loss likewise.  A block of 256
+// threads takes 32 parameters: thread (q, i) sums the blocks q*c .. q*c + c - 1 of
+// parameter i in order (c = ceil(blocks / 8)), and the eight partial sums are added
+// in q order, so the result is the same on every run.
+constexpr int kReduceParams = 32;
+constexpr int kReduceSplit = 8;
+__global__ void __launch_bounds__(kReduceParams * kReduceSplit) k_mlp_reduce(const float* __restrict__ part,
+                                                                            const float* __restrict__ part_loss,
+                                                                            int blocks, float* __restrict__ grad,
+                                                                            float* __restrict__ loss, int accumulate) {
+    __shared__ float ps[kReduceSplit][kReduceParams + 1];
+    const int ii = threadIdx.x % kReduceParams, q = threadIdx.x / kReduceParams;
+    const int i = blockIdx.x * kReduceParams + ii;
+    const int c = (blocks + kReduceSplit - 1) / kReduceSplit;
+    const int b0 = q * c, b1 = min(blocks, b0 + c);
+    float s = 0.0f;
+    if (i < kNumParams)
+        for (int b = b0; b < b1; ++b) s += part[(long)b * kNumParams + i];
+    ps[q][ii] = s;
+    __syncthreads();
+    if (q == 0 && i < kNumParams) {
+        float t = accumulate ? grad[i] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < kReduceSplit; ++k) t += ps[k][ii];
+        grad[i] = t;
     }
-    if (i == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         float l = accumulate ? *loss : 0.0f;
         for (int b = 0; b < blocks; ++b) l += part_loss[b];
         *loss = l;
@@ -424,13 +443,13 @@ static aep_status grad_pass(aep_mlp* mlp, const float* rec, int64_t n, int64_t r
     const int blocks = (rows + kTrainRows - 1) / kTrainRows;
     for (int b0 = 0; b0 < blocks; b0 += kPartBlocks) {
         const int nb = std::min(kPartBlocks, blocks - b0);
-        k_mlp_train_tile<<<nb, kTrainThreads, sizeof(TrainSmem), s>>>(mlp->p, rec, (int)n,
+        k_mlp_train_tile<<<nb, kTrainThreads, sizeof(TrainSmem), s>>>(mlp->p, mlp->wb, rec, (int)n,
                                                                       (int)(row0 + (int64_t)b0 * kTrainRows),
                                                                       (int)(row0 + rows), rows, mlp->part,
                                                                       mlp->part_loss);
         MCK(cudaGetLastError());
-        k_mlp_reduce<<<(kNumParams + 255) / 256, 256, 0, s>>>(mlp->part, mlp->part_loss, nb, mlp->g, mlp->loss,
-                                                              b0 > 0 ? 1 : 0);
+        k_mlp_reduce<<<(kNumParams + kReduceParams - 1) / kReduceParams, kReduceParams * kReduceSplit, 0, s>>>(
+            mlp->part, mlp->part_loss, nb, mlp->g, mlp->loss, b0 > 0 ? 1 : 0);
         MCK(cudaGetLastError());
     }
     return AEP_OK;

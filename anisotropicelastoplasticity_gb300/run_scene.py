@@ -10,7 +10,11 @@ cloth_drape (65,536 vertices + 130,050 elements, 128^3), snow_sand_collision
 twice: once with a start and an end event each, then again with the library's
 events between its kernels (which add a few microseconds per step) for the
 per-kernel times.  `--arg name=value` passes a size argument to the scene's
-factory (scenes.py), for a smaller case of the same scene."""
+factory (scenes.py), for a smaller case of the same scene.  `--learned STEPS`
+runs the learned return map instead of the exact one: the network is trained for
+STEPS Adam steps on the exact mappings of 20 plain steps of the same scene (a
+separate run, harvested first) and checked with the strict bound (1e-4 of the
+predicted strain)."""
 import argparse
 import json
 import sys
@@ -33,6 +37,8 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--arg", action="append", default=[], metavar="NAME=VALUE",
                     help="integer size argument of the scene factory (n, res, nside, n_sand, seed)")
+    ap.add_argument("--learned", type=int, default=None, metavar="STEPS",
+                    help="learned return map, trained for STEPS steps on the scene's own exact mappings")
     args = ap.parse_args(argv)
     kw = {}
     for a in args.arg:
@@ -42,8 +48,20 @@ def main(argv=None) -> int:
         kw[name] = int(value)
     import torch
 
+    mlp = None
+    if args.learned is not None:
+        from .learned import ReturnMapMLP, harvest_records
+
+        recs = harvest_records(SCENES[args.scene](**kw), steps=20, capacity=2000000, stride=1)
+        mlp = ReturnMapMLP(seed=0)
+        if args.learned > 0:
+            mlp.train(recs.data_ptr(), len(recs), steps=args.learned, batch=8192, lr=2e-3, lr_final=2e-5)
+        del recs
+        torch.cuda.empty_cache()
     sc = SCENES[args.scene](**kw)
     s = HybridSolver(sc.particles, sc.grid, sc.params)
+    if mlp is not None:
+        s.set_return_map(mlp, 1e-4)
     if sc.mesh is not None:
         s.set_lagrangian_mesh(sc.mesh)
     s.set_level_set(sc.levelset)
@@ -76,7 +94,11 @@ def main(argv=None) -> int:
         "phases_ms_per_step": {p: v / max(k, 1) for p, v in phases.items()},
         "active_nodes": st["active_nodes"], "fp64_fallbacks_last_step": st["fp64_fallbacks"],
         "total_mass": st["total_mass"],
+        "return_map": "exact" if mlp is None else "learned",
+        "learned_accepted_last_step": st["learned_accepted"], "learned_fallbacks_last_step": st["learned_fallbacks"],
     }))
+    if mlp is not None:
+        mlp.close()
     return 0
 
 

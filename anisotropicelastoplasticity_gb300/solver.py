@@ -518,9 +518,11 @@ class HybridSolver:
 
     def set_return_map(self, mlp=None, tolerance: float = 1e-3, abs_tolerance: float | None = None):
         """Use a trained ReturnMapMLP (None: the exact mapping of the reference).  A
-        prediction is kept when it is within max(tolerance x |exact|, abs_tolerance)
-        of the exact projection (abs_tolerance None: 2^-23, the FP32 resolution of
-        ln s near 1); otherwise the exact value is used and counted as a fallback."""
+        prediction is kept when the residuals of the optimality conditions of the
+        projection it stands for (the yield condition and the flow rule, ln-strain
+        units) are within max(tolerance x |prediction|, abs_tolerance) (abs_tolerance
+        None: 2^-23, the FP32 resolution of ln s near 1); otherwise the exact
+        projection is used and counted as a fallback."""
         self._mlp_ref = mlp
         self._check(self._lib.aep_set_return_map(self._h, mlp.handle if mlp is not None else None, tolerance))
         if abs_tolerance is not None:

@@ -62,8 +62,8 @@ def algorithmic_bytes(kernel: str, counts: dict) -> float:
         return 152 * (p + v) + 24 * nodes
     if kernel == "cloth_g2p":  # per element: x, d3, faces, 3 vertex x + v; writes x, v, B, F, plastic
         return 160 * e + 36 * e
-    if kernel == "mlp":  # a queue row in (37 words) and its F_E, plastic out
-        return counts.get("rows", 0) * (148 + 40)
+    if kernel == "mlp":  # a queue row in (21 words, 2 slots), the row's F, plastic, tag in; F_E, plastic out
+        return counts.get("rows", 0) * (84 + 8 + 41 + 40)
     if kernel == "normalize":
         return 44 * nodes
     if kernel == "grid":
@@ -264,7 +264,8 @@ def run_reference(args):
 def train_mlp(args, torch):
     """Train the learned return map on (trial, projected) pairs that the plain mapping
     produces on the snow block (from its ground impact on), the sand column, the cloth
-    drape (cloth rows) and the snow + sand collision family (another seed)."""
+    drape (cloth rows), the snow + sand collision family and the sand + cloth scene
+    (each of the last two with another seed than the benchmark's)."""
     from anisotropicelastoplasticity_gb300 import scenes
     from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP, harvest_records
 
@@ -285,13 +286,16 @@ def train_mlp(args, torch):
              "collision": harvest_records(scenes.snow_sand_collision(n=262144, res=128, seed=5), steps=100,
                                           capacity=quarter // 2, stride=1),
              "collision_strained": harvest_records(strained(scenes.snow_sand_collision(n=262144, res=128, seed=5),
-                                                            12), steps=5, capacity=quarter // 2, stride=1)}
+                                                            12), steps=5, capacity=quarter // 2, stride=1),
+             "sand_cloth": harvest_records(scenes.sand_cloth(seed=5), steps=10, capacity=quarter, stride=8,
+                                           warm_steps=20)}
     recs = torch.cat(list(parts.values()))
     n_rec = len(recs)
     t1 = time.perf_counter()
     mlp = ReturnMapMLP(seed=0)
     _, loss0 = mlp.gradient(recs.data_ptr(), n_rec)
-    mlp.train(recs.data_ptr(), n_rec, steps=args.train_steps, batch=8192, lr=2e-3, lr_final=2e-5)
+    mlp.train(recs.data_ptr(), n_rec, steps=args.train_steps, batch=args.train_batch, lr=args.train_lr,
+              lr_final=args.train_lr * 1e-2)
     _, loss1 = mlp.gradient(recs.data_ptr(), n_rec)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
@@ -299,9 +303,11 @@ def train_mlp(args, torch):
     info = {"records": n_rec, "records_per_source": {k: len(v) for k, v in parts.items()},
             "sources": "snow_block steps 1700-2300 (ground impact) + sand_column 500 steps (stride 8) + cloth_drape "
                        "(128x128 sheet) 400 steps + snow_sand_collision (262,144 particles, 128^3, seed 5) 100 steps "
-                       "+ the same with +-1% strain (seed 12) 5 steps; plastic states without the constant "
-                       "projections (sand apex, cloth in tension)",
-            "steps": args.train_steps, "batch": 8192, "loss_before": loss0, "loss_after": loss1,
+                       "+ the same with +-1% strain (seed 12) 5 steps + sand_cloth (full size, seed 5: other "
+                       "particles than the benchmark's seed 4) steps 20-30 (stride 8); plastic states without the "
+                       "constant projections (sand apex, cloth in tension); a seeded uniform sample of each source",
+            "steps": args.train_steps, "batch": args.train_batch, "lr": args.train_lr, "loss_before": loss0,
+            "loss_after": loss1,
             "harvest_s": t1 - t0, "train_s": t2 - t1, "fit_error": fit}
     return mlp, info
 
@@ -695,6 +701,8 @@ def main():
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--train-steps", type=int, default=200000)
+    ap.add_argument("--train-batch", type=int, default=8192)
+    ap.add_argument("--train-lr", type=float, default=2e-3, help="Adam learning rate, decayed to 1/100 (cosine)")
     ap.add_argument("--harvest", type=int, default=4000000)
     ap.add_argument("--err-half", type=float, default=0.02)
     ap.add_argument("--err-steps", type=int, default=5)
