@@ -427,8 +427,11 @@ __device__ __forceinline__ int frc_slot(int p) { return p * kFrcRec + (p >= 16 ?
 // FP64 code, and its registers, out of k_force).
 // vel: the grid velocities (global) or the block's tile; X, Y, Z the stencil
 // offsets into it; w, dw the particle's weights
+// F_E, the plastic scalar and the volume of the particle come from the caller's
+// shared-memory copies (sF[k][t], sq[t], svol[t]: copied while the grid tile loads)
 __device__ void particle_stress_impulse(const KParams& P, const float4* vel, const uint32_t X[4], const uint32_t Y[4],
-                                        const uint32_t Z[4], const PArrays& cur, int pj, float dt_force, float S[9],
+                                        const uint32_t Z[4], const PArrays& cur, int pj, int mat, const float* sF,
+                                        int t, int tstride, float q_in, float vol, float dt_force, float S[9],
                                         const float w[3][4], const float dw[3][4], DevStats* st, int32_t* fp64_list,
                                         int fp64_cap) {
     // velocity gradient of the P2G velocity (the three SpMVs of HS:269-271),
@@ -467,13 +470,11 @@ __device__ void particle_stress_impulse(const KParams& P, const float4* vel, con
     }
     float F[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) F[k] = cur.F[k][pj];
+    for (int k = 0; k < 9; ++k) F[k] = sF[k * tstride + t];
     float GF[9], Fh[9];
     mat_mul(Gm, F, GF);
 #pragma unroll
     for (int k = 0; k < 9; ++k) Fh[k] = F[k] + dt_force * GF[k];  // EDG + EDG_modifier * EDG (:306)
-    const int mat = cur.mat[pj];
-    const float vol = cur.vol[pj];
     float Jp = 1.0f;
     if (mat == kSnow) {
         if (P.track_fp) {
@@ -482,7 +483,7 @@ __device__ void particle_stress_impulse(const KParams& P, const float4* vel, con
             for (int k = 0; k < 9; ++k) Fp[k] = cur.Fp[k][pj];
             Jp = mat_det(Fp);
         } else {
-            Jp = cur.plastic[pj];
+            Jp = q_in;
         }
     }
     float U[9], s[3], V[9];
@@ -586,6 +587,16 @@ __global__ void __launch_bounds__(kFrcThreads, 6) k_force(KParams P, PArrays cur
     const bool live = j < n;
     const int pj = live ? perm[j] : 0;
     const int mat = live ? (int)cur.mat[pj] : 0;
+    // a particle's F_E, plastic scalar and volume are copied to shared memory while
+    // the tile loads (each thread reads back only its own entries)
+    __shared__ float sF[9][kFrcThreads], sq[kFrcThreads], svol[kFrcThreads];
+    if (live && mat <= kSand) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) cp_async4(&sF[k][threadIdx.x], &cur.F[k][pj]);
+        cp_async4(&sq[threadIdx.x], &cur.plastic[pj]);
+        cp_async4(&svol[threadIdx.x], &cur.vol[pj]);
+        cp_async_commit();
+    }
     int cell[3];
     float w[3][4], dw[3][4];
     uint32_t X[4], Y[4], Z[4];
@@ -605,7 +616,9 @@ __global__ void __launch_bounds__(kFrcThreads, 6) k_force(KParams P, PArrays cur
         float S[9];
         float av[3] = {0.f, 0.f, 0.f};  // w-weighted impulse (cloth vertices)
         if (mat <= kSand) {
-            particle_stress_impulse(P, in_tile ? tile_v : G.vel, X, Y, Z, cur, pj, dt_force, S, w, dw, st, fp64_list,
+            cp_async_wait_all();
+            particle_stress_impulse(P, in_tile ? tile_v : G.vel, X, Y, Z, cur, pj, mat, &sF[0][0], threadIdx.x,
+                                    kFrcThreads, sq[threadIdx.x], svol[threadIdx.x], dt_force, S, w, dw, st, fp64_list,
                                     fp64_cap);
         } else {
             const int id = cur.id[pj];

@@ -268,6 +268,51 @@ def test_learned_step_matches_oracle_and_training_gains():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("scene", ["mixed", "cloth"])
+def test_learned_step_with_nothing_accepted_equals_the_plain_step(scene):
+    """With an acceptance bound of zero every prediction falls back, and the learned
+    pipeline (the trial check and queue in G2P, the exact projection in the finisher,
+    the cloth elements' exact cap) must give the plain step's state bit for bit."""
+    from anisotropicelastoplasticity_gb300.learned import ReturnMapMLP
+
+    from .parity_util import perturbed, small_scene
+
+    m = ReturnMapMLP(seed=5)
+    if scene == "mixed":
+        sc = perturbed(small_scene("mixed"), seed=31)
+        _strained(sc, 9)
+        mesh = None
+    else:
+        from .test_cloth_gpu import small_cloth
+
+        grid, ps, mesh, ls, prm = small_cloth(True, seed=12, E=1e4, weighting=1)
+        sc = type("S", (), {"particles": ps, "grid": grid, "params": prm, "levelset": ls, "dt": 2e-5})()
+    outs = []
+    for learned in (False, True):
+        s = HybridSolver(sc.particles, sc.grid, sc.params)
+        if mesh is not None:
+            s.set_lagrangian_mesh(mesh)
+        s.set_level_set(sc.levelset)
+        s.init_volumes()
+        if learned:
+            s.set_return_map(m, 0.0, abs_tolerance=0.0)
+        acc = fb = 0
+        for _ in range(6):
+            s.step(sc.dt)
+            st = s.stats()
+            acc += st["learned_accepted"]
+            fb += st["learned_fallbacks"]
+        outs.append((s.get_particles(), s.get_mesh() if mesh is not None else {}, acc, fb))
+        s.close()
+    (p0, m0, _, _), (p1, m1, acc, fb) = outs
+    assert acc == 0 and fb > 0, (acc, fb)
+    for k in p0:
+        assert np.array_equal(p0[k], p1[k]), k
+    for k in m0:
+        assert np.array_equal(m0[k], m1[k]), k
+
+
+@pytest.mark.gpu
 def test_learned_cloth_return_map():
     """Cloth rows of the network: harvested (trial, projected) QR columns of plastic
     elements train the map; with it attached the elements' return mapping is
