@@ -1481,7 +1481,7 @@ aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance)
     if (m && !(tolerance >= 0.0)) return fail(s, AEP_INVALID_ARG, "aep_set_return_map: tolerance >= 0");
     s->mlp = m;
     s->learned_tol = tolerance;
-    s->learned_abs = std::ldexp(1.0, -23);
+    s->learned_abs = std::ldexp(1.0, -24);  // FP32 spacing below 1: the rounding of a stretch near 1, in ln s
     return AEP_OK;
 }
 

@@ -521,7 +521,8 @@ class HybridSolver:
         prediction is kept when the residuals of the optimality conditions of the
         projection it stands for (the yield condition and the flow rule, ln-strain
         units) are within max(tolerance x |prediction|, abs_tolerance) (abs_tolerance
-        None: 2^-23, the FP32 resolution of ln s near 1); otherwise the exact
+        None: 2^-24, the spacing of FP32 numbers just below 1, what rounding a
+        stretch near 1 to FP32 costs in ln s); otherwise the exact
         projection is used and counted as a fallback."""
         self._mlp_ref = mlp
         self._check(self._lib.aep_set_return_map(self._h, mlp.handle if mlp is not None else None, tolerance))

@@ -42,11 +42,13 @@ L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 # acceptance bounds of the learned return map's in-kernel check (the residuals of
 # the projection's yield condition and flow rule, ln-strain units), as (relative to
 # the predicted |ln s|, absolute): "strict" accepts residuals within 1e-5 of the
-# projected strain the prediction gives (or the FP32 resolution of ln s, 2^-23):
-# the distance to the exact projection is at most a few residuals, so an accepted
-# state's stress stays within ~1e-4 of the exact one; "residual_1e-4" accepts an
-# absolute residual of 1e-4, the bound the learned-map configuration states
-LEARNED_BOUNDS = {"strict": (1e-5, 2.0 ** -23), "residual_1e-4": (0.0, 1e-4)}
+# projected strain the prediction gives, or 2^-24 (the spacing of FP32 numbers just
+# below 1: what rounding a stretch near 1 to FP32 costs in ln s): the distance to
+# the exact projection is at most a few residuals, so an accepted state's stress
+# stays within ~1e-4 of the exact one, or at the FP32 rounding of a nearly
+# unstrained state; "residual_1e-4" accepts an absolute residual of 1e-4, the bound
+# the learned-map configuration states
+LEARNED_BOUNDS = {"strict": (1e-5, 2.0 ** -24), "residual_1e-4": (0.0, 1e-4)}
 
 
 def algorithmic_bytes(kernel: str, counts: dict) -> float:

@@ -428,16 +428,16 @@ aep_status aep_get_harvest_count(aep_solver* s, int64_t* count);
  * inside the clamp bounds, kept where the trial is inside and on the bound it
  * crossed; cloth, r33 kept and the shear shrunk radially onto the frictional cap.
  * A prediction whose largest residual (ln-strain units; cloth: QR units) exceeds
- * max(tolerance x |prediction|, 2^-23) is replaced by the exact projection
+ * max(tolerance x |prediction|, 2^-24) is replaced by the exact projection
  * (aep_stats.learned_fallbacks).  Constant projections (sand apex, cloth in
  * tension) are taken exactly (aep_stats.learned_exact).  The handle must outlive
  * its use.                                                                     */
 aep_status aep_set_return_map(aep_solver* s, const aep_mlp* m, double tolerance);
 /* The two bounds of that check: relative to the predicted projected strain
- * (rel_tol; the stress is linear in it) and
- * absolute (abs_tol, in ln-strain units; 2^-23 after aep_set_return_map, the FP32
- * resolution of ln s near s = 1).  A residual bound of 1e-4 is rel_tol = 0,
- * abs_tol = 1e-4.                                                               */
+ * (rel_tol; the stress is linear in it) and absolute (abs_tol, in ln-strain
+ * units; 2^-24 after aep_set_return_map, the spacing of FP32 numbers just below 1,
+ * what rounding a stretch near 1 to FP32 costs in ln s).  A residual bound of
+ * 1e-4 is rel_tol = 0, abs_tol = 1e-4.                                          */
 aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_tol);
 
 /* ---- particle-to-grid without allocation --------------------------------------------- */
