@@ -103,9 +103,21 @@ __global__ void __launch_bounds__(kTrainThreads, 2) k_mlp_train_tile(const float
     const int base = row0 + blockIdx.x * kTrainRows;
     float* const grad = part + (long)blockIdx.x * kNumParams;
     // the bf16 copy of the weights (refreshed by every Adam step) has the layout of
-    // W1..W4 here: one 16-byte copy per 8 weights
-    static_assert(kNumWeights % 8 == 0, "weight copy in 16-byte pieces");
-    for (int i = tid; i < kNumWeights / 8; i += kTrainThreads)
+    // W1..W4 here: one 16-byte copy per 8 weights; the rows of W1^T repeat their 7
+    // weights in columns 7..13, against the lo halves of the features (mlp_features)
+    static_assert(kNumWeights % 8 == 0 && kOffW2 == 128 * 8, "weight copy in 16-byte pieces");
+    for (int r = tid; r < 64; r += kTrainThreads) {
+        const uint4 a = reinterpret_cast<const uint4*>(wb)[2 * r], b = reinterpret_cast<const uint4*>(wb)[2 * r + 1];
+        const uint32_t u[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        const bf16* w = reinterpret_cast<const bf16*>(u);
+        bf16 d[16];
+#pragma unroll
+        for (int k = 0; k < kMlpFeat; ++k) d[k] = d[kMlpFeat + k] = w[k];
+        d[14] = d[15] = __float2bfloat16(0.0f);
+        reinterpret_cast<uint4*>(S.W1 + 16 * r)[0] = reinterpret_cast<const uint4*>(d)[0];
+        reinterpret_cast<uint4*>(S.W1 + 16 * r)[1] = reinterpret_cast<const uint4*>(d)[1];
+    }
+    for (int i = 128 + tid; i < kNumWeights / 8; i += kTrainThreads)
         reinterpret_cast<uint4*>(S.W1)[i] = reinterpret_cast<const uint4*>(wb)[i];
     for (int i = tid; i < 200; i += kTrainThreads) S.b[i] = params[kOffB1 + i];
     for (int r = tid; r < kTrainRows; r += kTrainThreads) {
@@ -233,6 +245,13 @@ __global__ void __launch_bounds__(kTrainThreads, 2) k_mlp_train_tile(const float
             }
         }
         __syncthreads();
+        if (l == 0) {  // W1's gradient: the hi and lo columns of a feature share its weight
+            for (int i = tid; i < 64 * kMlpFeat; i += kTrainThreads) {
+                float* gw = grad + kOffW1 + (i / kMlpFeat) * 16 + i % kMlpFeat;
+                gw[0] += gw[kMlpFeat];
+                gw[kMlpFeat] = 0.0f;
+            }
+        }
         cur = 1 - cur;
     }
     if (tid == 0) {

@@ -4,9 +4,14 @@
 // Input features (one row per particle): the trial log singular values of F_E^tr
 // sorted descending (3; normalised for sand, scaled by kLnScale for snow, see
 // mlp_features), the sand plastic amount q (1), and the material one-hot (snow,
-// sand, cloth) (3); padded to 16 columns.  Cloth elements use the same network
-// on (r13, r23, r33 - 1) of their QR factor, normalised, with the ratio of the
-// friction cap to the trial shear force in column 3.  Output: the correction
+// sand, cloth) (3).  The first layer's A operand carries each FP32 feature as two
+// bfloat16 values, hi = bf16(x) in column k and lo = bf16(x - hi) in column 7 + k,
+// against the same weight in both columns (the shared-memory copy of W1^T repeats
+// columns 0..6 in 7..13): the tensor cores then see the features to ~2^-17 instead
+// of bfloat16's 2^-9, at no extra MMA (7 features use 14 of the 16 columns).
+// Cloth elements use the same network on (r13, r23, r33 - 1) of their QR factor,
+// normalised, with the ratio of the friction cap to the trial shear force in
+// column 3.  Output: the correction
 // (ln s_projected - ln s_trial) in the same order and the same scaling (3 of 8).
 // The return mappings it stands in for (HybridSolver.cpp:626-674) are invariant
 // under permutations of the singular values, so sorting canonicalises the input.
@@ -24,7 +29,8 @@
 
 namespace aep {
 
-constexpr int kMlpIn = 16;     // padded input width (6 used)
+constexpr int kMlpIn = 16;     // padded input width (7 features as hi + lo: 14 used)
+constexpr int kMlpFeat = 7;    // features
 constexpr int kMlpHidden = 64;
 constexpr int kMlpOut = 8;     // padded output width (3 used)
 constexpr int kStrideIn = 24;  // bf16 per row of a 16-wide operand in shared memory
@@ -86,8 +92,17 @@ __device__ __forceinline__ void mlp_load_smem(const MlpParams& p, const MlpSmem&
     const uint4* g2 = reinterpret_cast<const uint4*>(p.w2t);
     const uint4* g3 = reinterpret_cast<const uint4*>(p.w3t);
     const uint4* g4 = reinterpret_cast<const uint4*>(p.w4t);
-    for (int i = tid; i < 64 * 2; i += nthreads)
-        *reinterpret_cast<uint4*>(s.w1t + (i >> 1) * kStrideIn + (i & 1) * 8) = g1[i];
+    for (int n = tid; n < 64; n += nthreads) {  // W1^T row n: [w0..w6, w0..w6, 0, 0]
+        const uint4 a = g1[2 * n], b = g1[2 * n + 1];
+        const uint32_t r[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        const __nv_bfloat16* w = reinterpret_cast<const __nv_bfloat16*>(r);
+        __nv_bfloat16 d[16];
+#pragma unroll
+        for (int k = 0; k < kMlpFeat; ++k) d[k] = d[kMlpFeat + k] = w[k];
+        d[14] = d[15] = __float2bfloat16(0.0f);
+        *reinterpret_cast<uint4*>(s.w1t + n * kStrideIn) = *reinterpret_cast<const uint4*>(d);
+        *reinterpret_cast<uint4*>(s.w1t + n * kStrideIn + 8) = *reinterpret_cast<const uint4*>(d + 8);
+    }
     for (int i = tid; i < 64 * 8; i += nthreads) {
         *reinterpret_cast<uint4*>(s.w2t + (i >> 3) * kStrideH + (i & 7) * 8) = g2[i];
         *reinterpret_cast<uint4*>(s.w3t + (i >> 3) * kStrideH + (i & 7) * 8) = g3[i];
@@ -258,15 +273,16 @@ __device__ __forceinline__ float mlp_features(const float ln_sorted[3], float q,
         const float r = sqrtf(ln_sorted[0] * ln_sorted[0] + ln_sorted[1] * ln_sorted[1] + ln_sorted[2] * ln_sorted[2]);
         sc = 1.0f / fmaxf(r, 1e-30f);
     }
-    row[0] = __float2bfloat16(ln_sorted[0] * sc);
-    row[1] = __float2bfloat16(ln_sorted[1] * sc);
-    row[2] = __float2bfloat16(ln_sorted[2] * sc);
-    row[3] = __float2bfloat16(mat == 1 ? q * kQScale : mat == kMlpCloth ? q : 0.0f);
-    row[4] = __float2bfloat16(mat == 0 ? 1.0f : 0.0f);
-    row[5] = __float2bfloat16(mat == 1 ? 1.0f : 0.0f);
-    row[6] = __float2bfloat16(mat == kMlpCloth ? 1.0f : 0.0f);
+    const float x[kMlpFeat] = {ln_sorted[0] * sc, ln_sorted[1] * sc, ln_sorted[2] * sc,
+                               mat == 1 ? q * kQScale : mat == kMlpCloth ? q : 0.0f, mat == 0 ? 1.0f : 0.0f,
+                               mat == 1 ? 1.0f : 0.0f, mat == kMlpCloth ? 1.0f : 0.0f};
 #pragma unroll
-    for (int k = 7; k < kMlpIn; ++k) row[k] = __float2bfloat16(0.0f);
+    for (int k = 0; k < kMlpFeat; ++k) {  // hi, lo: x to ~2^-17 as a sum of two bfloat16
+        const __nv_bfloat16 hi = __float2bfloat16(x[k]);
+        row[k] = hi;
+        row[kMlpFeat + k] = __float2bfloat16(x[k] - __bfloat162float(hi));
+    }
+    row[14] = row[15] = __float2bfloat16(0.0f);
     return sc;
 }
 

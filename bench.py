@@ -62,6 +62,8 @@ def algorithmic_bytes(kernel: str, counts: dict) -> float:
         return 56 * p + 36 * v + 48 * e + 36 * nodes
     if kernel == "g2p":  # read x, F_E, plastic; write x, v, B, F_E, plastic (particles and vertices)
         return 152 * (p + v) + 24 * nodes
+    if kernel == "g2p_learned":  # the same, a queued row writing its queue entry (21 words, 2 slots)
+        return 152 * (p + v) + 24 * nodes + counts.get("rows", 0) * (84 + 8 - 40)  # instead of F_E, plastic
     if kernel == "cloth_g2p":  # per element: x, d3, faces, 3 vertex x + v; writes x, v, B, F, plastic
         return 160 * e + 36 * e
     if kernel == "mlp":  # a queue row in (21 words, 2 slots), the row's F, plastic, tag in; F_E, plastic out
@@ -448,13 +450,15 @@ def roofline_of(arm: dict, counts: dict) -> dict:
     km = arm["kernel_ms"]
     counts = dict(counts, rows=arm.get("mlp_rows_last_step", 0))
     dom = max(("p2g", "force", "g2p"), key=lambda k: km[k])
+    learned = counts["rows"] > 0
+    form = "g2p_learned" if (dom == "g2p" and learned) else dom  # the G2P of the learned step queues rows
     peak, peak_kind = measured_peak_gbs()
-    ach = algorithmic_bytes(dom, counts) / (km[dom] * 1e-3) / 1e9
+    ach = algorithmic_bytes(form, counts) / (km[dom] * 1e-3) / 1e9
     traffic = None
     tp = ROOT / "profiles" / "traffic.json"
     if tp.exists():
         try:
-            t = json.loads(tp.read_text()).get(arm.get("workload", ""), {}).get(dom)
+            t = json.loads(tp.read_text()).get(arm.get("workload", ""), {}).get(form)
             if t:  # DRAM bytes per item of an ncu capture of a smaller case, scaled to the items
                 traffic = t["bytes_per_item"] * (counts["particles"] + counts["verts"] + counts["elems"])
         except Exception:
@@ -462,11 +466,11 @@ def roofline_of(arm: dict, counts: dict) -> dict:
     kernels = {}
     for k, v in km.items():
         try:
-            b = algorithmic_bytes(k, counts)
+            b = algorithmic_bytes("g2p_learned" if (k == "g2p" and learned) else k, counts)
         except KeyError:
             b = None
         kernels[k] = {"ms_per_launch": v, "algorithmic_GBps": (b / (v * 1e-3) / 1e9) if b and v > 0 else None}
-    return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+    return {"bound": "hbm", "kernel": form, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
             "traffic": traffic, "peak_source": peak_kind, "profiled_ms_per_step": arm["profiled_ms_per_step"],
             "kernels": kernels}
 

@@ -4,8 +4,11 @@ backward) for the gradient checks of the GPU kernels.
 TEST INFRASTRUCTURE ONLY (the checker): used by tests/ only.  With bf16=True the
 weights and every GEMM input are rounded to bfloat16 (round to nearest even) at the
 same points as the tensor-core kernels (aep_mlp.cu), so the two differ only by FP32
-accumulation order; with bf16=False it is the exact FP64 function, which the tests
-pin against central finite differences.
+accumulation order: the hidden activations and the output gradients are rounded,
+and the FP32 input features enter the first layer as the sum of two bfloat16
+values, hi = bf16(x) and lo = bf16(x - hi), both against the feature's weight (the
+kernels' A operand carries hi and lo in separate columns).  With bf16=False it is
+the exact FP64 function, which the tests pin against central finite differences.
 
 Packed parameters (9928 floats): W1^T [64][16], W2^T [64][64], W3^T [64][64],
 W4^T [8][64], b1 [64], b2 [64], b3 [64], b4 [8].  Records: [ln s0, ln s1, ln s2,
@@ -59,18 +62,24 @@ def scales(rec):
 
 
 def features(rec, rnd=True):
+    """The FP32 feature rows [n, 16] (7 used); with rnd, each feature as the sum of
+    its bfloat16 hi and lo parts, as the first layer's tensor-core operand sees it."""
     rec = np.asarray(rec, np.float64)
     n = len(rec)
-    X = np.zeros((n, 16))
+    X = np.zeros((n, 16), np.float32)
     sc = scales(rec)
     X[:, 0:3] = rec[:, 0:3].astype(np.float32) * sc[:, None]
     mat = rec[:, 4].astype(int)
     q = rec[:, 3].astype(np.float32)
-    X[:, 3] = np.where(mat == 1, q * np.float32(Q_SCALE), np.where(mat == 2, q, 0.0))
+    X[:, 3] = np.where(mat == 1, q * np.float32(Q_SCALE), np.where(mat == 2, q, np.float32(0.0)))
     X[:, 4] = (mat == 0)
     X[:, 5] = (mat == 1)
     X[:, 6] = (mat == 2)
-    return bf16(X) if rnd else X
+    if not rnd:
+        return X.astype(np.float64)
+    hi = bf16(X)
+    lo = bf16((X.astype(np.float64) - hi).astype(np.float32))
+    return hi + lo
 
 
 def silu(z):
