@@ -475,6 +475,27 @@ def roofline_of(arm: dict, counts: dict) -> dict:
             "kernels": kernels}
 
 
+def host_link_gbps(torch, nbytes: int = 1 << 30) -> dict:
+    """The host link's copy rate: page-locked host memory to and from the device with
+    cudaMemcpyAsync (torch copies), best of three, each way."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        best = None
+        for _ in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = nbytes / (best * 1e-3) / 1e9
+    del h, d
+    return out
+
+
 def run_e2e(args, torch, arm, sc, world):
     """The learned step through the C-ABI with the caller's page-locked host arrays as
     the state: aep_set_particles + aep_set_mesh_state, aep_step, aep_get_particles +
@@ -499,7 +520,9 @@ def run_e2e(args, torch, arm, sc, world):
     part = [pinned(vec_to_ref(p["positions"])), pinned(vec_to_ref(p["velocities"])),
             pinned(rows_to_ref(p["affine_momenta"])), pinned(mats_to_ref(p["elastic_deformation_gradients"])),
             pinned(sc.particles.masses), pinned(p["volumes"]), pinned(p["plastic"])]
-    mat = np.ascontiguousarray(sc.particles.material, np.uint8)
+    mt = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    mt.numpy()[...] = np.asarray(sc.particles.material, np.uint8)
+    mat = mt.numpy()
     mesh = None
     if sc.mesh is not None:
         m = s.get_mesh()
@@ -531,7 +554,13 @@ def run_e2e(args, torch, arm, sc, world):
             assert lib.aep_get_mesh(h, *[dp(a) for a in mesh]) == 0
     el = time.perf_counter() - t0
     value, _ = job_throughput(sc.num_items(), steps, el, world)
+    link = host_link_gbps(torch)
+    # the least time a step's host round trip can take: its bytes at the link's copy
+    # rates plus the device step itself
+    bound_ms = (h2d / link["h2d"] + d2h / link["d2h"]) / 1e6 + arm["ms_per_step"]
     return {"value": value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": steps,
+            "ms_per_step": el / steps * 1e3, "host_link_GBps": link, "link_bound_ms_per_step": bound_ms,
+            "of_link_bound": bound_ms / (el / steps * 1e3),
             "path": "aep_set_particles + aep_set_mesh_state + aep_step (learned return map) + aep_get_particles + "
                     "aep_get_mesh, page-locked FP64 host arrays in the reference layouts"}
 
