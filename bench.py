@@ -747,7 +747,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--train-steps", type=int, default=400000)
     ap.add_argument("--train-batch", type=int, default=16384)
-    ap.add_argument("--train-lr", type=float, default=2e-3, help="Adam learning rate, decayed to 1/100 (cosine)")
+    ap.add_argument("--train-lr", type=float, default=1e-3, help="Adam learning rate, decayed to 1/100 (cosine)")
     ap.add_argument("--harvest", type=int, default=4000000)
     ap.add_argument("--err-half", type=float, default=0.02)
     ap.add_argument("--err-steps", type=int, default=5)
