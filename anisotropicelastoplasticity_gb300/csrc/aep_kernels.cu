@@ -1342,31 +1342,19 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
     } else {
         // the learned return map: the trial state and its yield check here; a plastic
         // state with a projection the network predicts is queued for k_mlp_finish
-        // (trial ln s, q, F, D, V), everything else is mapped exactly in place
+        // (trial ln s, D, V), everything else is mapped exactly in place
         float ln[3];
-        if (stretch_trial<float>(F, D, ln, V)) {
-            const int tk = trial_kind(P, mat, ln, q);
-            if (tk == 2) {
-                cg::coalesced_group g = cg::coalesced_threads();  // warp-aggregated queue append
-                unsigned qbase = 0;
-                if (g.thread_rank() == 0) qbase = atomicAdd(&st->mlp_rows, g.size());
-                const int r = (int)(g.shfl(qbase, 0) + g.thread_rank());
-                if (r < Qu.cap) {
-                    deferred = true;
-                    const long cap = Qu.cap;
-                    float* f = Qu.f + r;
-                    Qu.j[r] = j;
-                    Qu.pj[r] = pj;
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) f[(kQLn + a) * cap] = ln[a];
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) {
-                        f[(kQD + k) * cap] = D[k];
-                        f[(kQV + k) * cap] = V[k];
-                    }
-                }
-            }
-            if (!deferred) {
+        const bool in_range = stretch_trial<float>(F, D, ln, V);
+        const int tk = in_range ? trial_kind(P, mat, ln, q) : -1;
+        // the queue positions of the warp's plastic lanes: one atomic, issued here and
+        // read after the exact mappings of its other lanes, which hide its round trip
+        const unsigned qlanes = __activemask();
+        const unsigned qmask = __ballot_sync(qlanes, tk == 2);
+        const int qlane = threadIdx.x & 31, qleader = qmask ? __ffs(qmask) - 1 : __ffs(qlanes) - 1;
+        unsigned qbase = 0;
+        if (qmask && qlane == qleader) qbase = atomicAdd(&st->mlp_rows, (unsigned)__popc(qmask));
+        if (in_range) {
+            if (tk != 2) {
                 float lnn[3], qq = q;
                 const int kind = stretch_project<float>(P, mat, ln, lnn, qq);
                 stretch_finish<float>(mat, F, D, V, ln, lnn, kind != 0, qq, q, Fe, sig);
@@ -1379,6 +1367,25 @@ __global__ void __launch_bounds__(128, 4) k_g2p(KParams P, PArrays cur, PArrays 
         } else {
             cg::coalesced_group g = cg::coalesced_threads();  // beyond the stretch form: exact SVD form
             if (g.thread_rank() == 0) atomicAdd(&st->learned_exact, (unsigned long long)g.size());
+        }
+        qbase = __shfl_sync(qlanes, qbase, qleader);
+        if (tk == 2) {
+            // the queue has a row per particle, so every position is below its capacity
+            const int r = (int)(qbase + (unsigned)__popc(qmask & ((1u << qlane) - 1u)));
+            deferred = true;
+            if (r < Qu.cap) {
+                const long cap = Qu.cap;
+                float* f = Qu.f + r;
+                Qu.j[r] = j;
+                Qu.pj[r] = pj;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) f[(kQLn + a) * cap] = ln[a];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    f[(kQD + k) * cap] = D[k];
+                    f[(kQV + k) * cap] = V[k];
+                }
+            }
         }
     }
     bool ok = skind >= 0 || svd3<float>(Ftr, U, s, V, 8, 1e-7f, 2e-2f);
