@@ -54,6 +54,12 @@ __global__ void k_keys(KParams P, PArrays cur, int n, uint32_t* keys, DevStats* 
 // D^-1 = 3/h^2 (:177), x_i - x_p = (o - 1 - f) h  =>  w (b + Mh o) with
 // Mh[:,a] = m D^-1 h_a B[:,a] and b = m v - Mh (1 + f).
 constexpr int kP2GThreads = 128;
+// the P2G grid tile: 3 x 2 x 2 node blocks from the node block of the thread
+// block's first particle (the particles are ordered by node block, x fastest: a
+// block's 512 particles mostly sit in two x-adjacent node blocks, whose stencils
+// the tile holds)
+constexpr int kP2GTileBx = 3;
+constexpr int kP2GTileNodes = kP2GTileBx * 2 * 2 * 64;
 constexpr int kP2GMaxChunk = 128;  // particles per warp at most (the launch picks the chunk)
 // Prep record of one particle, 9 float4 (36 words, 16-byte aligned):
 //   q0 = (b, m)  q1 = Mh[0..3]  q2 = Mh[4..7]  q3 = (Mh[8], T lo, T hi, -)
@@ -88,8 +94,10 @@ __device__ __forceinline__ void mark_blocks(const KParams& P, const GArrays& G, 
 // FP32 registers.  At the end of a run (warp-uniform) the halves' sums are added,
 // half h takes the z-layers 2h, 2h + 1, and the node sums are rounded to fixed
 // point and added as integers: runs whose stencil lies in the block's grid tile
-// (the 2x2x2 node blocks of its middle particle, where most of its particles
-// sit) into a fixed-point copy of the tile in shared memory, which is
+// (3 x 2 x 2 node blocks from the node block of its first particle, which holds the
+// stencils of that node block's particles and of the next one's in x: ~91% of the
+// runs on the sand + cloth scene, against ~68% for the 2 x 2 x 2 blocks of the
+// middle particle) into a fixed-point copy of the tile in shared memory, which is
 // added to the grid once per node at the end; other runs into the grid directly.
 // Integer sums: the result does not depend on the order.
 // Exact mass: rounding the node masses one by one loses the difference between
@@ -104,18 +112,17 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
                                                      int32_t* __restrict__ slot_of, int32_t* __restrict__ curidx_of) {
     pdl_trigger();  // the normalisation may launch once every block has started
     __shared__ float4 sm4[(kP2GThreads / 32) * kP2GRegion];
-    __shared__ unsigned long long tacc[4 * kTileNodes];  // [channel][tile node]
+    __shared__ unsigned long long tacc[4 * kP2GTileNodes];  // [channel][tile node]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const region = sm4 + warp * kP2GRegion;
     const int half = lane >> 4, ox = lane & 3, oy = (lane >> 2) & 3;
     const long blk0 = (long)blockIdx.x * (kP2GThreads / 32) * chunk;
     const long chunk0 = blk0 + (long)warp * chunk;
     const int cnt_total = (int)max(0L, min((long)chunk, (long)n - chunk0));  // warp-uniform
-    // the tile: the node blocks of the block's middle particle (the particles are
-    // ordered by node block: across two node blocks, the middle one's holds half)
+    // the tile's origin: the node block of the block's first particle
     int org[3];
-    tile_origin(P, keys[blk0 + (min((long)n, blk0 + (long)(kP2GThreads / 32) * chunk) - 1 - blk0) / 2], org);
-    for (int i = threadIdx.x; i < 4 * kTileNodes; i += kP2GThreads) tacc[i] = 0ull;
+    tile_origin(P, keys[min(blk0, (long)n - 1)], org);
+    for (int i = threadIdx.x; i < 4 * kP2GTileNodes; i += kP2GThreads) tacc[i] = 0ull;
     __syncthreads();
 
     float am[4] = {0, 0, 0, 0}, ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, az[4] = {0, 0, 0, 0};
@@ -147,18 +154,21 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
         const unsigned s_lo = __reduce_add_sync(0xffffffffu, (unsigned)mf[0] + (unsigned)mf[1]);
         if (lane == 5) mf[1] += (long long)(int)((unsigned)run_T - s_lo);  // (ox, oy, oz) = (1, 1, 1)
         const int x = rb[0] + ox, y = rb[1] + oy;
-        if ((rb[0] >> 2) == org[0] && (rb[1] >> 2) == org[1] && (rb[2] >> 2) == org[2]) {
+        const int rbx = (rb[0] >> 2) - org[0];
+        if (rbx >= 0 && rbx < kP2GTileBx - 1 && (rb[1] >> 2) == org[1] && (rb[2] >> 2) == org[2]) {
+            // the run's stencil (base .. base + 3) lies in the tile: node blocks
+            // org.x + rbx, org.x + rbx + 1 in x, org.y, org.y + 1, org.z, org.z + 1
             const int tx = x - 4 * org[0], ty = y - 4 * org[1];
-            const int txy = (tx >> 2) * 64 + (tx & 3) + (ty >> 2) * 128 + ((ty & 3) << 2);
+            const int txy = (tx >> 2) * 64 + (tx & 3) + (ty >> 2) * (64 * kP2GTileBx) + ((ty & 3) << 2);
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
                 if (mf[k] != 0) {
                     const int tz = rb[2] + 2 * half + k - 4 * org[2];
-                    unsigned long long* a = tacc + txy + (tz >> 2) * 256 + ((tz & 3) << 4);
+                    unsigned long long* a = tacc + txy + (tz >> 2) * (128 * kP2GTileBx) + ((tz & 3) << 4);
                     atomicAdd(a, (unsigned long long)mf[k]);
-                    atomicAdd(a + kTileNodes, to_fixed(gx[k], P.mom_scale));
-                    atomicAdd(a + 2 * kTileNodes, to_fixed(gy[k], P.mom_scale));
-                    atomicAdd(a + 3 * kTileNodes, to_fixed(gz[k], P.mom_scale));
+                    atomicAdd(a + kP2GTileNodes, to_fixed(gx[k], P.mom_scale));
+                    atomicAdd(a + 2 * kP2GTileNodes, to_fixed(gy[k], P.mom_scale));
+                    atomicAdd(a + 3 * kP2GTileNodes, to_fixed(gz[k], P.mom_scale));
                 }
             }
         } else {
@@ -178,33 +188,19 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
         run_T = 0;
     };
 
-    // the next batch's particle state (x, m, v, B: 16 words per particle) is copied to
-    // shared memory with cp.async while the current batch's runs are scattered;
-    // each lane reads back only its own column
-    __shared__ float stage[kP2GThreads / 32][16][32];
-    float(*const stg)[32] = stage[warp];
-    auto prefetch = [&](int pj) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            cp_async4(&stg[a][lane], &cur.x[a][pj]);
-            cp_async4(&stg[4 + a][lane], &cur.v[a][pj]);
-        }
-        cp_async4(&stg[3][lane], &cur.m[pj]);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) cp_async4(&stg[7 + k][lane], &cur.B[k][pj]);
-        cp_async_commit();
-    };
-    int pj_cur = lane < cnt_total ? perm[chunk0 + lane] : 0;
-    prefetch(pj_cur);
     for (int b0 = 0; b0 < cnt_total; b0 += 32) {
         const long j = chunk0 + b0 + lane;
-        const int pj_next = b0 + 32 + lane < cnt_total ? perm[j + 32] : 0;
         uint32_t my_key = kInvalidKey;
-        cp_async_wait_all();
-        float xs_[16];
+        const int pj_cur = b0 + lane < cnt_total ? perm[j] : 0;
+        float xs_[16];  // the batch's particle state: x, m, v, B
 #pragma unroll
-        for (int k = 0; k < 16; ++k) xs_[k] = stg[k][lane];
-        if (b0 + 32 < cnt_total) prefetch(pj_next);
+        for (int a = 0; a < 3; ++a) {
+            xs_[a] = cur.x[a][pj_cur];
+            xs_[4 + a] = cur.v[a][pj_cur];
+        }
+        xs_[3] = cur.m[pj_cur];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) xs_[7 + k] = cur.B[k][pj_cur];
         if (b0 + lane < cnt_total) {
             const uint32_t key = keys[j];
             if (j == 0 || (keys[j - 1] >> 6) != (key >> 6)) mark_blocks(P, G, key);
@@ -296,20 +292,19 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(KParams P, PArrays cur, con
             t = e;
         }
         __syncwarp();
-        pj_cur = pj_next;
     }
-    cp_async_wait_all();  // a warp without particles still issued its first prefetch
     flush();
     __syncthreads();
     // the tile into the grid, one atomic per nonzero node and channel
-    for (int i = threadIdx.x; i < kTileNodes; i += kP2GThreads) {
-        const int t = i >> 6;
-        const uint32_t gblk = (uint32_t)(((org[2] + (t >> 2)) * P.nb[1] + org[1] + ((t >> 1) & 1)) * P.nb[0] + org[0] +
-                                         (t & 1));
+    for (int i = threadIdx.x; i < kP2GTileNodes; i += kP2GThreads) {
+        const int t = i >> 6;  // tile block (bx, by, bz) = (t % 3, (t / 3) % 2, t / 6)
+        const int bx = t % kP2GTileBx, by = (t / kP2GTileBx) & 1, bz = t / (2 * kP2GTileBx);
+        if (org[0] + bx >= P.nb[0]) continue;  // past the padded grid: nothing was added there
+        const uint32_t gblk = (uint32_t)(((org[2] + bz) * P.nb[1] + org[1] + by) * P.nb[0] + org[0] + bx);
         unsigned long long* a = G.acc + 4ull * ((gblk << 6) | (uint32_t)(i & 63));
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            const unsigned long long v = tacc[c * kTileNodes + i];
+            const unsigned long long v = tacc[c * kP2GTileNodes + i];
             if (v != 0ull) atomicAdd(a + c, v);
         }
     }
