@@ -88,28 +88,38 @@ def measured_peak_gbs():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 25 ms around the timed
+    region; the summary keeps the samples taken inside it (by nvidia-smi's own
+    timestamps), or the nearest ones when the region is shorter than a sample."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
         self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=self.tmp, stderr=subprocess.DEVNULL)
+            deadline = time.time() + 3.0  # the first sample is out before the region starts
+            while time.time() < deadline and os.path.getsize(self.tmp.name) == 0:
+                time.sleep(0.005)
         except (OSError, ValueError):
             self.proc = None
+        self.t0 = time.time()
         return self
 
     def __exit__(self, *exc):
+        self.t1 = time.time()
         if self.proc is not None:
+            time.sleep(0.03)  # the sample that closes the region
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -117,20 +127,35 @@ class ClockSampler:
                 self.proc.kill()
         self.tmp.flush()
 
+    @staticmethod
+    def _stamp(text: str):
+        import datetime
+
+        try:
+            return datetime.datetime.strptime(text.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
     def summary(self):
         try:
             rows = [r.split(",") for r in Path(self.tmp.name).read_text().strip().splitlines() if r.strip()]
         except OSError:
             rows = []
+        rows = [r for r in rows if len(r) >= 10]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
-        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
-        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
-                          and "Not" not in r[5 + i]})
+        inside = []
+        if self.t0 is not None and self.t1 is not None:
+            inside = [r for r in rows if (t := self._stamp(r[0])) is not None and self.t0 - 0.03 <= t <= self.t1 + 0.03]
+        use = inside or rows
+        num = lambda v: v.strip().replace(".", "").isdigit()  # noqa: E731
+        sm = [float(r[2]) for r in use if num(r[2])]
+        smax = [float(r[3]) for r in use if num(r[3])]
+        reasons = sorted({self.REASONS[i] for r in use for i in range(4)
+                          if "Active" in r[6 + i] and "Not" not in r[6 + i]})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(use),
+                "window": "timed region" if inside else "around the timed region"}
 
 
 def dist_env():
