@@ -1,4 +1,4 @@
-"""The learned return map: a 6 -> 64 -> 64 -> 64 -> 3 SiLU MLP with BF16 weights on
+"""The learned return map: a 7 -> 64 -> 64 -> 64 -> 3 SiLU MLP with BF16 weights on
 the tensor cores, trained on the GPU by libaep.so's own forward, backward and Adam
 kernels from (trial, projected) pairs that the exact return mapping produces
 (aep_set_harvest).  Device buffers are torch tensors (plumbing only); every

@@ -54,7 +54,7 @@ def main(argv=None) -> int:
 
         recs = harvest_records(SCENES[args.scene](**kw), steps=20, capacity=2000000, stride=1)
         mlp = ReturnMapMLP(seed=0)
-        if args.learned > 0:
+        if args.learned > 0 and len(recs) > 0:  # a scene at rest may have no plastic state yet
             mlp.train(recs.data_ptr(), len(recs), steps=args.learned, batch=8192, lr=2e-3, lr_final=2e-5)
         del recs
         torch.cuda.empty_cache()

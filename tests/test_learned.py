@@ -355,3 +355,18 @@ def test_learned_cloth_return_map():
     # at most ~1, in each of the 10 steps: the directions get 10 x 1e-3, the rest
     # keeps the exact-path tolerances
     _compare_mesh(g2.get_mesh(), orc.get_mesh(), 2e-6, 1e-3, 1e-2, 5e-3)
+
+
+@pytest.mark.gpu
+def test_scene_runner_with_the_learned_return_map(capsys):
+    """python -m anisotropicelastoplasticity_gb300.run_scene ... --learned STEPS trains
+    the network on the scene's own exact mappings and runs the learned step."""
+    import json
+
+    from anisotropicelastoplasticity_gb300 import run_scene
+
+    assert run_scene.main(["snow_sand_collision", "--arg", "n=8192", "--arg", "res=32", "--steps", "2",
+                           "--warmup", "1", "--learned", "200"]) == 0
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert out["return_map"] == "learned"
+    assert out["ms_per_step"] > 0 and out["phases_ms_per_step"]["mlp"] >= 0
