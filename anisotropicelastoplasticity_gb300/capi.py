@@ -166,6 +166,7 @@ SIGNATURES = {
     "aep_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int32, C.c_double, C.c_double,
                                 C.POINTER(C.c_double), C.c_void_p]),
     "aep_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "aep_mlp_forward_step_form": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "aep_mlp_last_error": (C.c_char_p, [C.c_void_p]),
     "aep_set_harvest": (C.c_int, [_solver_p, C.c_void_p, C.c_int64, C.c_int32]),
     "aep_get_harvest_count": (C.c_int, [_solver_p, C.POINTER(C.c_int64)]),

@@ -1577,7 +1577,7 @@ __global__ void __launch_bounds__(kFinThreads) k_mlp_finish(KParams P, PArrays c
         sort3_desc(ln, srt, pm);
         float q = cur.plastic[pj];
         const float osc = mlp_features(srt, q, mat, X + lane * kStrideIn);
-        mlp_forward_warp(W, X, Y, lane);
+        mlp_forward_warp<true>(W, X, Y, lane);
         if (live) {
             float pred[3];
 #pragma unroll
@@ -1757,7 +1757,7 @@ __global__ void __launch_bounds__(128) k_cloth_g2p(KParams P, PArrays cur, PArra
         if (__any_sync(0xffffffffu, plastic)) {  // warp-uniform
             const float in[3] = {r[0], r[1], r[2] - 1.0f};
             const float sc = mlp_features(in, cap, plastic ? kMlpCloth : 0, MX + lane * kStrideIn);
-            mlp_forward_warp(W, MX, MY, lane);
+            mlp_forward_warp<true>(W, MX, MY, lane);
             if (plastic) {
                 // optimality conditions of the frictional cap: r33 kept, the shear
                 // (r13, r23) a shrunk copy of the trial's, its length on the cap

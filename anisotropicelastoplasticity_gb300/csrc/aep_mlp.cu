@@ -316,7 +316,8 @@ __global__ void k_mlp_refresh_bf16(const float* __restrict__ p, bf16* __restrict
     if (i < kNumWeights) wb[i] = __float2bfloat16(p[i]);
 }
 
-// batched inference, 32 rows per warp (the fast path used inside G2P)
+// batched inference, 32 rows per warp; kStep: with the SiLU of the step's kernels
+template <bool kStep>
 __global__ void __launch_bounds__(128) k_mlp_infer(MlpParams P, const float* __restrict__ rec, int n,
                                                    float* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -337,7 +338,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(MlpParams P, const float* __r
         float ln[3] = {0, 0, 0};
         mlp_features(ln, 0.0f, 0, X + lane * kStrideIn);
     }
-    mlp_forward_warp(W, X, Y, lane);
+    mlp_forward_warp<kStep>(W, X, Y, lane);
     if (r < n)
         for (int k = 0; k < 3; ++k) out[3 * r + k] = Y[lane * kMlpOut + k] / sc;
 }
@@ -519,14 +520,25 @@ aep_status aep_mlp_train(aep_mlp* mlp, const float* d_records, int64_t n, int64_
     return AEP_OK;
 }
 
-aep_status aep_mlp_forward(aep_mlp* mlp, const float* d_records, int64_t n, float* d_out, void* cuda_stream) {
+static aep_status mlp_forward(aep_mlp* mlp, const float* d_records, int64_t n, float* d_out, void* cuda_stream,
+                              bool step_form) {
     if (!mlp || !d_records || !d_out || n <= 0 || n > (int64_t)INT32_MAX / 2) return AEP_INVALID_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     const int smem = kMlpSmemBytes + 4 * kMlpWarpBytes;
-    MCK(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    k_mlp_infer<<<(int)((n + 127) / 128), 128, smem, s>>>(mlp_device_params(mlp), d_records, (int)n, d_out);
+    const auto kernel = step_form ? k_mlp_infer<true> : k_mlp_infer<false>;
+    MCK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    kernel<<<(int)((n + 127) / 128), 128, smem, s>>>(mlp_device_params(mlp), d_records, (int)n, d_out);
     MCK(cudaGetLastError());
     return AEP_OK;
+}
+
+aep_status aep_mlp_forward(aep_mlp* mlp, const float* d_records, int64_t n, float* d_out, void* cuda_stream) {
+    return mlp_forward(mlp, d_records, n, d_out, cuda_stream, false);
+}
+
+aep_status aep_mlp_forward_step_form(aep_mlp* mlp, const float* d_records, int64_t n, float* d_out,
+                                     void* cuda_stream) {
+    return mlp_forward(mlp, d_records, n, d_out, cuda_stream, true);
 }
 
 const char* aep_mlp_last_error(aep_mlp* mlp) { return mlp ? mlp->err.c_str() : "null mlp"; }

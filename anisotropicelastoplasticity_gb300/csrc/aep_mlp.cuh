@@ -134,6 +134,24 @@ __device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16* p) {
 // are rounded to bfloat16 right after, 2^-8 relative, far above their error)
 __device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 
+// The step's SiLU: z sigmoid(z) = h + h tanh(h), h = z / 2, with the hardware tanh
+// (one MUFU operation instead of an exponential and a reciprocal; relative error of
+// tanh about 2^-11, so an activation is off by at most |z| 2^-12, below the
+// bfloat16 rounding it then takes for |z| of order one).  The forward API and the
+// training keep silu(); the step's predictions are checked against the projection's
+// optimality conditions whatever the arithmetic that made them.
+__device__ __forceinline__ float silu_step(float z) {
+    const float h = 0.5f * z;
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+    return fmaf(h, t, h);
+}
+
+template <bool kStep>
+__device__ __forceinline__ float silu_t(float z) {
+    return kStep ? silu_step(z) : silu(z);
+}
+
 // Per-warp scratch for one 32-row inference (halves / floats): the input rows and
 // the output rows; the hidden activations stay in registers (mlp_forward_warp)
 constexpr int kMlpWarpX = 32 * kStrideIn;   // bf16
@@ -163,6 +181,7 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 // fragment's register pair {0,1} (nt even) or {2,3} (nt odd) of k tile nt/2, so the
 // epilogue packs it in place.  B fragments come from the padded rows of W^T by
 // ldmatrix (two k tiles of one n tile per instruction).
+template <bool kStep>
 __device__ __forceinline__ void mlp_hidden_layer_reg(const uint32_t (&a)[2][4][4], uint32_t (&o)[2][4][4],
                                                      const __nv_bfloat16* Wt, const float* bias, int lane) {
     const int t = lane & 3;
@@ -187,8 +206,9 @@ __device__ __forceinline__ void mlp_hidden_layer_reg(const uint32_t (&a)[2][4][4
         const float bb0 = bias[n0], bb1 = bias[n0 + 1];
 #pragma unroll
         for (int mt = 0; mt < 2; ++mt) {
-            o[mt][nt >> 1][(nt & 1) * 2] = pack_bf16x2(silu(c[mt][0] + bb0), silu(c[mt][1] + bb1));
-            o[mt][nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(silu(c[mt][2] + bb0), silu(c[mt][3] + bb1));
+            o[mt][nt >> 1][(nt & 1) * 2] = pack_bf16x2(silu_t<kStep>(c[mt][0] + bb0), silu_t<kStep>(c[mt][1] + bb1));
+            o[mt][nt >> 1][(nt & 1) * 2 + 1] =
+                pack_bf16x2(silu_t<kStep>(c[mt][2] + bb0), silu_t<kStep>(c[mt][3] + bb1));
         }
     }
 }
@@ -197,7 +217,8 @@ __device__ __forceinline__ void mlp_hidden_layer_reg(const uint32_t (&a)[2][4][4
 // rows in Y (row r read back by lane r).  All 32 lanes must call it.  Each layer
 // accumulates its 16-wide k tiles in order in FP32 and rounds its SiLU outputs to
 // bfloat16 (the rounding points of the oracle's forward); the hidden activations
-// stay in registers between layers.
+// stay in registers between layers.  kStep: the step's SiLU (silu_step).
+template <bool kStep = false>
 __device__ __forceinline__ void mlp_forward_warp(const MlpSmem& W, __nv_bfloat16* X, float* Y, int lane) {
     const int g = lane >> 2, t = lane & 3;
     __syncwarp();
@@ -222,13 +243,13 @@ __device__ __forceinline__ void mlp_forward_warp(const MlpSmem& W, __nv_bfloat16
             for (int mt = 0; mt < 2; ++mt) {
                 float c[4] = {0, 0, 0, 0};
                 mma_bf16(c, x[mt][0], x[mt][1], x[mt][2], x[mt][3], b0, b1);
-                h0[mt][nt >> 1][(nt & 1) * 2] = pack_bf16x2(silu(c[0] + bb0), silu(c[1] + bb1));
-                h0[mt][nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(silu(c[2] + bb0), silu(c[3] + bb1));
+                h0[mt][nt >> 1][(nt & 1) * 2] = pack_bf16x2(silu_t<kStep>(c[0] + bb0), silu_t<kStep>(c[1] + bb1));
+                h0[mt][nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(silu_t<kStep>(c[2] + bb0), silu_t<kStep>(c[3] + bb1));
             }
         }
     }
-    mlp_hidden_layer_reg(h0, h1, W.w2t, W.b2, lane);
-    mlp_hidden_layer_reg(h1, h0, W.w3t, W.b3, lane);
+    mlp_hidden_layer_reg<kStep>(h0, h1, W.w2t, W.b2, lane);
+    mlp_hidden_layer_reg<kStep>(h1, h0, W.w3t, W.b3, lane);
     {  // output layer (64 -> 8), FP32 rows to Y
         float c[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
 #pragma unroll

@@ -80,9 +80,11 @@ class ReturnMapMLP:
                                             float(lr), float(lr_final), C.byref(loss), C.c_void_p(stream_ptr)))
         return loss.value
 
-    def forward(self, records_ptr: int, n: int, out_ptr: int, stream_ptr: int = 0):
-        self._check(self._lib.aep_mlp_forward(self.handle, C.c_void_p(records_ptr), int(n), C.c_void_p(out_ptr),
-                                              C.c_void_p(stream_ptr)))
+    def forward(self, records_ptr: int, n: int, out_ptr: int, stream_ptr: int = 0, step_form: bool = False):
+        """Predicted corrections of n device records; step_form: with the SiLU of the
+        step's learned return map (aep_mlp_forward_step_form)."""
+        fn = self._lib.aep_mlp_forward_step_form if step_form else self._lib.aep_mlp_forward
+        self._check(fn(self.handle, C.c_void_p(records_ptr), int(n), C.c_void_p(out_ptr), C.c_void_p(stream_ptr)))
 
 
 def canonical_order(recs):

@@ -410,6 +410,12 @@ aep_status aep_mlp_train(aep_mlp* m, const float* d_records, int64_t n, int64_t 
                          double lr, double lr_final, double* final_loss, void* cuda_stream);
 /* Predicted corrections d (3 floats per record, ln units) for n device records. */
 aep_status aep_mlp_forward(aep_mlp* m, const float* d_records, int64_t n, float* d_out, void* cuda_stream);
+/* The same predictions with the arithmetic of the step's learned return map: its
+ * SiLU is z/2 + (z/2) tanh(z/2) with the hardware tanh (relative error ~2^-11)
+ * instead of an exponential and a reciprocal.  For checking that arithmetic
+ * against aep_mlp_forward.                                                      */
+aep_status aep_mlp_forward_step_form(aep_mlp* m, const float* d_records, int64_t n, float* d_out,
+                                     void* cuda_stream);
 const char* aep_mlp_last_error(aep_mlp* m);
 
 /* Collect training records from the exact return mapping of every `stride`-th

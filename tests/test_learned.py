@@ -135,6 +135,14 @@ def test_gpu_forward_matches_oracle():
     torch.cuda.synchronize()
     ref = mo.predict(p.astype(np.float64), rec, bf=True)
     assert np.abs(out.cpu().numpy() - ref).max() < 2e-4 * max(np.abs(ref).max(), 1e-3)
+    # the step's arithmetic (its SiLU with the hardware tanh, relative error ~2^-11,
+    # so a hidden activation is off by up to |z| 2^-12 before its bfloat16 rounding):
+    # the same function to within the error that this feeds through two layers
+    m.forward(d.data_ptr(), len(rec), out.data_ptr(), step_form=True)
+    torch.cuda.synchronize()
+    err = np.abs(out.cpu().numpy() - ref).max() / max(np.abs(ref).max(), 1e-3)
+    print(f"step-form forward against the oracle: {err:.2e} of the largest output")
+    assert err < 3e-3, err
 
 
 def _strained(sc, seed):
