@@ -1,6 +1,7 @@
-"""The benchmark's clock record: the samples nvidia-smi wrote inside the timed
-region are kept (by their own timestamps) and the throttle reasons read from
-them; no GPU or nvidia-smi is needed to check the parsing."""
+"""The benchmark's bookkeeping, checked without a GPU or nvidia-smi: the clock
+record (the samples nvidia-smi wrote inside the timed region are kept, by their
+own timestamps, and the throttle reasons read from them) and the roofline's
+algorithmic bytes and DRAM traffic."""
 import datetime
 import importlib
 import sys
@@ -46,3 +47,23 @@ def test_clock_summary_without_samples_in_the_region(tmp_path):
     assert s["samples"] == 1 and s["window"] == "around the timed region"
     c2 = bench.ClockSampler(0)
     assert c2.summary()["samples"] == 0
+
+
+def test_roofline_of_the_learned_step_counts_its_queue_rows():
+    """The dominant kernel's algorithmic bytes: the plain G2P's per-item state, plus,
+    for the learned step, each queued row's queue entry instead of its F_E and
+    plastic scalar; the DRAM traffic per item comes from the committed ncu table."""
+    bench = _bench()
+    counts = {"particles": 1000, "verts": 10, "elems": 20, "nodes": 300}
+    plain = bench.algorithmic_bytes("g2p", counts)
+    assert plain == 152 * 1010 + 24 * 300
+    learned = bench.algorithmic_bytes("g2p_learned", dict(counts, rows=400))
+    assert learned == plain + 400 * (84 + 8 - 40)
+    arm = {"kernel_ms": {"p2g": 1.0, "force": 1.5, "g2p": 2.0, "mlp": 0.4}, "mlp_rows_last_step": 400,
+           "workload": "sand_cloth", "profiled_ms_per_step": 5.0}
+    r = bench.roofline_of(arm, counts)
+    assert r["kernel"] == "g2p_learned"
+    assert abs(r["achieved"] - learned / 2e-3 / 1e9) < 1e-9
+    assert r["traffic"] is not None and r["traffic"] > 0
+    arm_plain = dict(arm, mlp_rows_last_step=0)
+    assert bench.roofline_of(arm_plain, counts)["kernel"] == "g2p"
