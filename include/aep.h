@@ -469,8 +469,8 @@ aep_status aep_set_return_map_bounds(aep_solver* s, double rel_tol, double abs_t
  * Limits: the padded grid, ((res+2)/4 + 2)^3 * 64 nodes, must not exceed
  * AEP_NOALLOC_MAX_NODES (a 64^3 grid fits); larger grids return AEP_CAPACITY.
  * The first call on a device looks up the device address of the fixed array
- * (cudaGetSymbolAddress) and keeps it for the life of the process; make that
- * first call before any stream capture begins.  The kept address is not valid
+ * (cudaGetSymbolAddress) and keeps it for the life of the process.  The kept
+ * address is not valid
  * after cudaDeviceReset on that device: a process that resets a device must not
  * call this entry point on it again.  Every call shares the one array and clears
  * the part it uses at its start, so calls that can overlap on the GPU (different
